@@ -1,0 +1,246 @@
+/*
+ * bmg.h -- C ABI of libbmg, the GB300 (sm_103a) build of bmagwa's MCMC over
+ * SNP inclusion.
+ *
+ * The reference exposes no library API: its seams are the CLI
+ * `bmagwa INIFILE` (src/main.cpp:36-47), the INI schema parsed into
+ * bmagwa::Options (src/options.hpp:138-321), the PLINK inputs read by
+ * bmagwa::Data (src/data.cpp:141-273), the per-chain
+ * bmagwa::Sampler(const Options&, const Data*, const PrecomputedSNPCovariances*)
+ * + Sampler::sample() (src/sampler.hpp:107, src/sampler.cpp:551-880), and the
+ * binary trace files written by sample() (src/sampler.cpp:547-880).  Each
+ * entry point below names the reference interface it replaces.
+ *
+ * Conventions: plain pointers and sizes, no C++ or torch types.  Host pointers
+ * are copied; the caller keeps ownership.  All device memory is owned by the
+ * context.  Nothing throws across this boundary: every call returns a
+ * bmg_status and bmg_last_error() gives the message.  A context is not
+ * thread-safe; use one host thread per context.
+ */
+#ifndef BMG_H_
+#define BMG_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum bmg_status {
+  BMG_OK = 0,
+  BMG_EINVAL = 1,       /* bad argument or option (reference: std::runtime_error) */
+  BMG_EIO = 2,          /* file missing, truncated, wrong magic */
+  BMG_ECUDA = 3,        /* CUDA runtime error or missing device code */
+  BMG_ENOTPD = 4,       /* start state not positive definite */
+  BMG_ETIMEOUT = 5,     /* a bounded device wait gave up */
+  BMG_ENOMEM = 6,
+  BMG_EUNSUPPORTED = 7, /* option valid in the reference but not on this path */
+  BMG_ENUMERIC = 8      /* NaN met where the reference throws (src/sampler.cpp:213) */
+} bmg_status;
+
+/* effect types, numbering of DataModel::ef_t (src/data_model.hpp:41) */
+enum { BMG_TYPE_A = 0, BMG_TYPE_H = 1, BMG_TYPE_D = 2, BMG_TYPE_R = 3, BMG_TYPE_AH = 4 };
+
+/* proposal used for additions (BMG_PROPOSAL_ADAPTIVE is the reference's) */
+enum { BMG_PROPOSAL_ADAPTIVE = 0, BMG_PROPOSAL_LEARNED = 1 };
+
+/* p-wide scan implementation */
+enum { BMG_SCAN_TCGEN05 = 0, BMG_SCAN_SIMT = 1 };
+
+#define BMG_MAX_PATH 1024
+
+/*
+ * All INI options of bmagwa::Options (src/options.hpp:41-74), same names and
+ * meanings, plus the GPU knobs at the end.  bmg_options_default() fills the
+ * reference's defaults; bmg_options_from_ini() parses a reference INI file
+ * with the reference's keys, defaults, warnings and validation rules.
+ */
+typedef struct bmg_options {
+  /* [datafiles] */
+  char file_fam[BMG_MAX_PATH];
+  char file_g[BMG_MAX_PATH];
+  char file_e[BMG_MAX_PATH];
+  char file_y[BMG_MAX_PATH];
+  int32_t recode_g_to_minor_allele_count;
+  /* [sizes] */
+  uint64_t n;
+  uint64_t m_g;
+  uint32_t m_e;           /* covariates, excluding the constant */
+  /* [model] types, sorted ascending (src/options.hpp:236-252) */
+  uint32_t n_types;
+  int32_t types[5];
+  /* [sampler] */
+  int32_t sampler_type;   /* 0 PMV (only PMV is on this path) */
+  uint64_t do_n_iter;
+  uint64_t n_rao;
+  uint64_t n_rao_burnin;
+  uint64_t thin;
+  uint64_t n_sample_tau2_and_missing;
+  uint32_t max_move_size;
+  uint32_t max_SNP_neighborhood_size;
+  double p_move_size;
+  double p_move_size_nbs;
+  double p_move_size_nbc;
+  int32_t adapt_p_move_size;
+  double p_move_size_acpt_goal;
+  int32_t adaptation;
+  int32_t flat_proposal_dist;
+  int32_t save_beta;
+  uint64_t verbosity;
+  uint32_t delay_rejection;
+  /* [thread] */
+  char basename[BMG_MAX_PATH];
+  uint32_t n_chains;      /* n_threads */
+  const uint32_t* seeds;  /* n_chains seeds; caller-owned */
+  /* [prior] */
+  double e_qg;
+  double var_qg;
+  double nu_sigma2;
+  double s2_sigma2;
+  double R2mode_sigma2;
+  double mu_alpha;
+  double inv_tau2_e_const_val;
+  double inv_tau2_e_val;
+  int32_t use_individual_tau2;
+  double types_prior[5];  /* type_A, type_H, type_D, type_R, type_AH */
+  double nu_tau2[4];
+  double s2_tau2[4];
+  double eh_tau2[4];
+  /* GB300 knobs (no reference counterpart) */
+  uint32_t max_model_size;  /* columns of X_gamma incl. covariates (ref MAXMODELSIZE 1024) */
+  uint32_t scan_limbs;      /* 8-bit residual limbs in the scan GEMM, 3..7 (default 6) */
+  int32_t scan_impl;        /* BMG_SCAN_TCGEN05 or BMG_SCAN_SIMT */
+  int32_t proposal;         /* BMG_PROPOSAL_ADAPTIVE or BMG_PROPOSAL_LEARNED */
+  uint32_t graph_iters;     /* iterations captured per CUDA graph chunk */
+  int32_t write_files;      /* 1: bmg_run writes the reference's trace files */
+  int32_t quiet;            /* 1: no console warnings */
+} bmg_options;
+
+/* Trace of a chain over a run chunk, in the reference's file layouts
+ * (src/sampler.cpp:686-728; README "Output files and formats"). */
+typedef struct bmg_trace_chunk {
+  uint32_t chain;
+  uint64_t iter0;              /* first iteration of the chunk */
+  uint64_t n_iter;             /* per-iteration arrays below have n_iter entries */
+  const uint8_t* jumpdistance;
+  const uint8_t* move_type;
+  const uint8_t* move_size;
+  uint64_t n_thin;             /* thinned arrays below have n_thin entries */
+  const uint32_t* modelsize;
+  uint64_t n_loci;             /* sum of modelsize */
+  const uint32_t* loci;
+  const uint8_t* types;        /* type index per locus (multi-type runs only) */
+  const double* log_likelihood;
+  const double* log_prior;
+  const double* sigma2;
+  const double* alpha;
+  const double* pve;           /* 3 per thinned sample */
+  uint64_t n_beta;
+  const double* beta;          /* save_beta: all coefficients per thinned sample */
+} bmg_trace_chunk;
+
+typedef void (*bmg_trace_fn)(void* user, const bmg_trace_chunk* chunk);
+
+typedef struct bmg_trace_sink {
+  bmg_trace_fn fn;
+  void* user;
+} bmg_trace_sink;
+
+typedef struct bmg_ctx bmg_ctx;
+
+/* Reference defaults of every optional key (src/options.hpp:138-321). */
+bmg_status bmg_options_default(bmg_options* opt);
+
+/* Parse a reference INI file (replaces bmagwa::Options::Options,
+ * src/options.hpp:77-86, parse_options :138-321).  `seeds_buf` receives the
+ * seeds (capacity `seeds_cap`); opt->seeds points into it. */
+bmg_status bmg_options_from_ini(const char* path, bmg_options* opt,
+                                uint32_t* seeds_buf, uint32_t seeds_cap,
+                                char* err, size_t err_len);
+
+/* Read the data files an options struct names: .fam phenotypes (and the
+ * alternate phenotype file), covariates and the .bed payload, with the
+ * reference's matching and error rules (replaces Data::read_fam/read_y/
+ * read_e/read_g, src/data.cpp:141-273).  packed: m_g*ceil(n/4) bytes;
+ * y: n doubles; e: n*m_e doubles column-major (NULL when m_e == 0). */
+bmg_status bmg_read_plink(const bmg_options* opt, uint8_t* packed, double* y, double* e,
+                          char* err, size_t err_len);
+
+/* Create a context on the current CUDA device (replaces the per-chain
+ * Sampler construction, src/sampler.hpp:107-282, for all chains at once). */
+bmg_status bmg_create(const bmg_options* opt, bmg_ctx** out);
+
+/* Copy SNP-major packed PLINK genotypes (the .bed payload after its 3 magic
+ * bytes: p rows of ceil(n/4) bytes) to the device (replaces Data::read_g,
+ * src/data.cpp:245-273, and the recode/missing passes :324-376). */
+bmg_status bmg_load_bed(bmg_ctx* ctx, const uint8_t* packed, uint64_t n, uint64_t p);
+
+/* Phenotypes: n_pheno rows of n doubles (replaces Data::read_fam/read_y,
+ * src/data.cpp:141-200).  Chain c uses phenotype c % n_pheno.  `mask` is
+ * optional: n_pheno rows of n bytes, 1 = individual kept for that phenotype
+ * (no reference counterpart; the reference needs one run per phenotype). */
+bmg_status bmg_set_phenotypes(bmg_ctx* ctx, const double* y, const uint8_t* mask,
+                              uint32_t n_pheno);
+
+/* Covariates without the constant column: m_e columns of n doubles,
+ * column-major (replaces Data::read_e, src/data.cpp:202-243). */
+bmg_status bmg_set_covariates(bmg_ctx* ctx, const double* e, uint32_t m_e);
+
+/* Per-SNP sums and centred second moments of every allowed term
+ * (replaces PrecomputedSNPCovariances::precompute,
+ * src/precomputed_snp_covariances.hpp:95-131) and the start state of every
+ * chain (Sampler ctor + initialize_p_proposal_flat, src/sampler.hpp:351-362). */
+bmg_status bmg_precompute(bmg_ctx* ctx);
+
+/* Read back the precomputed per-SNP values: m_g rows of `offset` doubles in
+ * the reference's layout (PrecomputedSNPCovariances::xx, :42-84). */
+bmg_status bmg_get_precomputed(bmg_ctx* ctx, double* xx, uint32_t* offset);
+
+/* Rao-Blackwellised single-SNP scan of every chain at its current state
+ * (replaces RaoBlackwellizer::p_raoblackwell, src/sampler.cpp:32-261).
+ * p_r: n_chains x m_g; p_r_types: n_chains x m_g x n_types (may be NULL). */
+bmg_status bmg_scan(bmg_ctx* ctx, double* p_r, double* p_r_types);
+
+/* Advance every chain by n_iter MCMC iterations (replaces the main loop of
+ * Sampler::sample, src/sampler.cpp:626-834).  Traces go to `sink` (may be
+ * NULL) and, with opt.write_files, to the reference's files. */
+bmg_status bmg_run(bmg_ctx* ctx, uint64_t n_iter, const bmg_trace_sink* sink);
+
+/* Current state of one chain (the fields of bmagwa::Model the traces show). */
+typedef struct bmg_chain_state {
+  uint32_t model_size;
+  double log_likelihood;
+  double log_prior;
+  double sigma2;
+  double alpha;
+  uint64_t n_iter;
+  uint64_t n_accepted;
+  double p_move_size;
+} bmg_chain_state;
+
+/* loci (capacity loci_cap) receives the model's SNPs in model order. */
+bmg_status bmg_get_state(bmg_ctx* ctx, uint32_t chain, bmg_chain_state* st,
+                         uint32_t* loci, uint8_t* type_inds, uint32_t loci_cap);
+
+/* Rao-Blackwellised posterior of a chain (the _rao.dat / _rao_types.dat
+ * payloads, src/sampler.cpp:846-858).  p_rao_types may be NULL. */
+bmg_status bmg_get_rao(bmg_ctx* ctx, uint32_t chain, double* p_rao, double* p_rao_types);
+
+/* Write a chain's _rao.dat, _rao_types.dat, _samplerstats.txt and _prior.txt
+ * under opt.basename (src/sampler.cpp:838-858, src/sampler.hpp:384-390). */
+bmg_status bmg_finish(bmg_ctx* ctx);
+
+/* Device time of the phases of the last bmg_run, in milliseconds:
+ * [0] move kernel, [1] scan, [2] proposal rebuild, [3] total. */
+bmg_status bmg_get_timings(bmg_ctx* ctx, double* ms4);
+
+const char* bmg_last_error(const bmg_ctx* ctx);
+const char* bmg_status_string(bmg_status s);
+void bmg_destroy(bmg_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BMG_H_ */

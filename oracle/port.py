@@ -1,0 +1,166 @@
+"""Python handle on the CPU oracle (oracle/port) and on the reference build.
+
+ORACLE / TEST INFRASTRUCTURE: imported only by tests/, __graft_entry__.smoke()
+and bench.py's CPU-baseline leg, as the checker.  The product never imports it.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from bmagwa_gb300 import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_LIB = os.path.join(HERE, "_build", "libbmgport.so")
+REF_BIN = os.path.join(HERE, "_ref", "bmagwa_ref")
+REF_PROBE = os.path.join(HERE, "_ref", "ref_probe")
+
+_lib = None
+
+
+def build(verbose=False):
+    """Compile the port (and nothing else) into oracle/_build."""
+    os.makedirs(os.path.dirname(PORT_LIB), exist_ok=True)
+    inc = os.path.join(HERE, "..", "include")
+    cmd = ["g++", "-std=c++17", "-O3", "-fPIC", "-shared", "-I" + inc,
+           "-I" + os.path.join(HERE, "port"), os.path.join(HERE, "port", "port.cpp"),
+           "-x", "c", os.path.join(HERE, "linalg.c"), "-o", PORT_LIB, "-lpthread"]
+    subprocess.run(cmd, check=True, capture_output=not verbose)
+    return PORT_LIB
+
+
+def build_reference():
+    """Compile the reference sources (needs the reference tree) into oracle/_ref."""
+    subprocess.run(["make", "-s", "-C", HERE, "-j8"], check=True)
+    return REF_BIN
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(PORT_LIB):
+            build()
+        L = C.CDLL(PORT_LIB)
+        L.bmgport_create.argtypes = [C.POINTER(abi.Options), C.c_void_p, C.c_void_p, C.c_void_p,
+                                     C.POINTER(C.c_void_p), C.c_char_p, C.c_size_t]
+        L.bmgport_run.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32, C.POINTER(abi.TraceSink)]
+        L.bmgport_scan.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]
+        L.bmgport_get_state.argtypes = [C.c_void_p, C.c_uint32, C.POINTER(abi.ChainState),
+                                        C.c_void_p, C.c_void_p, C.c_uint32]
+        L.bmgport_get_rao.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]
+        L.bmgport_get_precomputed.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(C.c_uint32)]
+        L.bmgport_get_data_stats.argtypes = [C.c_void_p, C.c_void_p]
+        L.bmgport_get_genotypes.argtypes = [C.c_void_p, C.c_uint32, C.c_uint64, C.c_void_p]
+        L.bmgport_model_lml.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p,
+                                        C.c_void_p, C.c_void_p]
+        L.bmgport_destroy.argtypes = [C.c_void_p]
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+class Port:
+    """One oracle instance: all chains of an options struct on one dataset."""
+
+    def __init__(self, opt, packed, y, e=None):
+        self._keep = (np.ascontiguousarray(packed, dtype=np.uint8),
+                      np.ascontiguousarray(y, dtype=np.float64),
+                      None if e is None else np.ascontiguousarray(e, dtype=np.float64))
+        self.opt = opt
+        self.m_g = int(opt.m_g)
+        self.n_types = int(opt.n_types)
+        h = C.c_void_p()
+        err = C.create_string_buffer(512)
+        rc = lib().bmgport_create(C.byref(opt), _ptr(self._keep[0]), _ptr(self._keep[1]),
+                                  _ptr(self._keep[2]), C.byref(h), err, 512)
+        if rc != 0:
+            raise RuntimeError("oracle: " + err.value.decode())
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().bmgport_destroy(self.h)
+            self.h = None
+
+    def run(self, n_iter, threads=1):
+        col = abi.TraceCollector()
+        rc = lib().bmgport_run(self.h, n_iter, threads, C.byref(col.sink))
+        if rc != 0:
+            raise RuntimeError("oracle run failed")
+        return col
+
+    def scan(self, chain=0):
+        pr = np.zeros(self.m_g)
+        prt = np.zeros(self.m_g * self.n_types) if self.n_types > 1 else None
+        if lib().bmgport_scan(self.h, chain, _ptr(pr), _ptr(prt)) != 0:
+            raise RuntimeError("oracle scan failed")
+        return pr, (prt.reshape(self.m_g, self.n_types) if prt is not None else None)
+
+    def state(self, chain=0, cap=4096):
+        st = abi.ChainState()
+        loci = np.zeros(cap, dtype=np.uint32)
+        types = np.zeros(cap, dtype=np.uint8)
+        lib().bmgport_get_state(self.h, chain, C.byref(st), _ptr(loci), _ptr(types), cap)
+        k = st.model_size
+        return st, loci[:k].copy(), types[:k].copy()
+
+    def rao(self, chain=0):
+        p = np.zeros(self.m_g)
+        pt = np.zeros(self.m_g * self.n_types) if self.n_types > 1 else None
+        lib().bmgport_get_rao(self.h, chain, _ptr(p), _ptr(pt))
+        return p, (pt.reshape(self.m_g, self.n_types) if pt is not None else None)
+
+    def precomputed(self):
+        off = C.c_uint32()
+        lib().bmgport_get_precomputed(self.h, None, C.byref(off))
+        xx = np.zeros(self.m_g * off.value)
+        lib().bmgport_get_precomputed(self.h, _ptr(xx), C.byref(off))
+        return xx.reshape(self.m_g, off.value)
+
+    def data_stats(self):
+        out = np.zeros(4)
+        lib().bmgport_get_data_stats(self.h, _ptr(out))
+        return out
+
+    def genotypes(self, typ, snp):
+        out = np.zeros(int(self.opt.n))
+        if lib().bmgport_get_genotypes(self.h, typ, snp, _ptr(out)) != 0:
+            raise IndexError(snp)
+        return out
+
+    def model_lml(self, snps, t_inds, inv_pairs):
+        snps = np.ascontiguousarray(snps, dtype=np.uint32)
+        t_inds = np.ascontiguousarray(t_inds, dtype=np.uint8)
+        inv = np.ascontiguousarray(inv_pairs, dtype=np.float64).reshape(-1)
+        out = np.zeros(len(snps))
+        if lib().bmgport_model_lml(self.h, len(snps), _ptr(snps), _ptr(t_inds), _ptr(inv),
+                                   _ptr(out)) != 0:
+            raise RuntimeError("oracle model failed")
+        return out
+
+
+def read_ref_outputs(basename, chain, m_g, n_types=1):
+    """Read the binary trace files the reference (or libbmg) writes for a chain."""
+    b = "%s%d" % (basename, chain)
+    rd = lambda suf, dt: np.fromfile(b + suf, dtype=dt) if os.path.exists(b + suf) else None
+    out = {
+        "jumpdistance": rd("_jumpdistance.dat", np.uint8),
+        "move_type": rd("_move_type.dat", np.uint8),
+        "move_size": rd("_move_size.dat", np.uint8),
+        "modelsize": rd("_modelsize.dat", np.uint32),
+        "loci": rd("_loci.dat", np.uint32),
+        "log_likelihood": rd("_log_likelihood.dat", np.float64),
+        "log_prior": rd("_log_prior.dat", np.float64),
+        "sigma2": rd("_sigma2.dat", np.float64),
+        "alpha": rd("_alpha.dat", np.float64),
+        "pve": rd("_pve.dat", np.float64),
+        "rao": rd("_rao.dat", np.float64),
+        "types": rd("_types.dat", np.uint8),
+        "rao_types": rd("_rao_types.dat", np.float64),
+        "beta": rd("_beta.dat", np.float64),
+    }
+    return out

@@ -1,0 +1,54 @@
+/*
+ * oracle/port/port.h -- C API of the CPU restatement of bmagwa's sampler.
+ *
+ * ORACLE / TEST INFRASTRUCTURE.  This is the checker the GPU path is compared
+ * against and the CPU baseline bench.py times; it is never linked into, or
+ * called by, the product.  It restates the reference algorithm
+ * (src/sampler.hpp, src/sampler.cpp, src/model.hpp, src/prior.*, src/data*.cpp,
+ * src/precomputed_snp_covariances.hpp, src/discrete_distribution.hpp) in the
+ * reference's floating-point operation order, on the random stream of
+ * include/bmg_rng.h, so its traces equal those of the reference compiled in
+ * oracle/_ref bit for bit.  Scope: PMV sampler (moves 0-3), delayed rejection
+ * off, all effect types, missing genotypes, individual or shared tau2.
+ */
+#ifndef BMG_ORACLE_PORT_H_
+#define BMG_ORACLE_PORT_H_
+
+#include <stddef.h>
+#include <stdint.h>
+#include "bmg.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct bmgport bmgport;
+
+/* packed: m_g rows of ceil(n/4) bytes (PLINK SNP-major payload); y: n values;
+ * e: n x m_e covariates without the constant (column-major) or NULL. */
+int bmgport_create(const bmg_options* opt, const uint8_t* packed, const double* y,
+                   const double* e, bmgport** out, char* err, size_t err_len);
+/* advance every chain n_iter iterations (threads = min(chains, n_threads)) */
+int bmgport_run(bmgport* P, uint64_t n_iter, uint32_t n_threads,
+                const bmg_trace_sink* sink);
+/* RB scan of one chain against y - y_hat of its current model */
+int bmgport_scan(bmgport* P, uint32_t chain, double* p_r, double* p_r_types);
+int bmgport_get_state(bmgport* P, uint32_t chain, bmg_chain_state* st,
+                      uint32_t* loci, uint8_t* type_inds, uint32_t cap);
+int bmgport_get_rao(bmgport* P, uint32_t chain, double* p_rao, double* p_rao_types);
+int bmgport_get_precomputed(bmgport* P, double* xx, uint32_t* offset);
+/* var_x, mean_x, var_y, yy of the loaded data (src/data.hpp:66-71) */
+int bmgport_get_data_stats(bmgport* P, double* out4);
+/* decoded genotype column of one SNP for a term type (missing -> -1) */
+int bmgport_get_genotypes(bmgport* P, uint32_t type, uint64_t snp, double* out);
+/* LML after each add_term of a fresh model (src/model.hpp:239-268) */
+int bmgport_model_lml(bmgport* P, uint32_t n_add, const uint32_t* snps,
+                      const uint8_t* t_inds, const double* inv_tau2_alpha2,
+                      double* lml_after_each);
+void bmgport_destroy(bmgport* P);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif
