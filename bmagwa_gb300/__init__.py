@@ -1,0 +1,233 @@
+"""bmagwa_gb300: GB300 (sm_103a) build of bmagwa's MCMC over SNP inclusion.
+
+Python handle on libbmg (include/bmg.h).  The reference's entry points map as:
+
+    bmagwa INIFILE               -> run_ini(path)  /  bmagwa-gb300 INIFILE
+    bmagwa::Options(ini)         -> options_from_ini(path)
+    bmagwa::Data(...)            -> read_plink(opt) + Context.load_bed /
+                                    set_phenotypes / set_covariates
+    PrecomputedSNPCovariances    -> Context.precompute()
+    Sampler::sample()            -> Context.run(n_iter)
+    RaoBlackwellizer             -> Context.scan()
+
+Every call goes to the CUDA library; there is no CPU fallback.  If the
+library is not built, importing works but the first call raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+
+__all__ = ["lib", "options_from_ini", "default_options", "read_plink", "Context", "run_ini",
+           "BmgError", "build"]
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libbmg.so")
+_lib = None
+
+
+class BmgError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s: %s" % (abi.STATUS_NAMES.get(status, status), msg))
+        self.status = status
+
+
+def build(force=False, verbose=False):
+    from . import nvbuild as _b
+    return _b.build(force=force, verbose=verbose)
+
+
+def lib():
+    """The loaded libbmg (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libbmg is not built (run bmagwa_gb300.build() or __graft_entry__.build())")
+        L = C.CDLL(LIB_PATH)
+        abi.bind_common(L)
+        vp, u32, u64 = C.c_void_p, C.c_uint32, C.c_uint64
+        L.bmg_create.argtypes = [C.POINTER(abi.Options), C.POINTER(vp)]
+        L.bmg_load_bed.argtypes = [vp, vp, u64, u64]
+        L.bmg_set_phenotypes.argtypes = [vp, vp, vp, u32]
+        L.bmg_set_covariates.argtypes = [vp, vp, u32]
+        L.bmg_precompute.argtypes = [vp]
+        L.bmg_get_precomputed.argtypes = [vp, vp, C.POINTER(u32)]
+        L.bmg_scan.argtypes = [vp, vp, vp]
+        L.bmg_run.argtypes = [vp, u64, C.POINTER(abi.TraceSink)]
+        L.bmg_get_state.argtypes = [vp, u32, C.POINTER(abi.ChainState), vp, vp, u32]
+        L.bmg_get_rao.argtypes = [vp, u32, vp, vp]
+        L.bmg_finish.argtypes = [vp]
+        L.bmg_get_timings.argtypes = [vp, vp]
+        L.bmg_get_data_stats.argtypes = [vp, vp]
+        L.bmg_last_error.argtypes = [vp]
+        L.bmg_last_error.restype = C.c_char_p
+        L.bmg_status_string.argtypes = [C.c_int]
+        L.bmg_status_string.restype = C.c_char_p
+        L.bmg_destroy.argtypes = [vp]
+        L.bmg_destroy.restype = None
+        for name in ("bmg_create", "bmg_load_bed", "bmg_set_phenotypes", "bmg_set_covariates",
+                     "bmg_precompute", "bmg_get_precomputed", "bmg_scan", "bmg_run", "bmg_get_state",
+                     "bmg_get_rao", "bmg_finish", "bmg_get_timings", "bmg_get_data_stats"):
+            getattr(L, name).restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def default_options():
+    o = abi.Options()
+    lib().bmg_options_default(C.byref(o))
+    return o
+
+
+def options_from_ini(path, quiet=True):
+    """Parse a reference INI file; returns (options, seeds array)."""
+    o = abi.Options()
+    o.quiet = 1 if quiet else 0
+    seeds = (C.c_uint32 * 4096)()
+    err = C.create_string_buffer(1024)
+    rc = lib().bmg_options_from_ini(os.fsencode(path), C.byref(o), seeds, 4096, err, 1024)
+    if rc != 0:
+        raise BmgError(rc, err.value.decode())
+    o._seeds = seeds  # keep the buffer alive with the struct
+    return o
+
+
+def set_seeds(opt, seeds):
+    arr = (C.c_uint32 * len(seeds))(*[int(s) for s in seeds])
+    opt.seeds = C.cast(arr, C.POINTER(C.c_uint32))
+    opt.n_chains = len(seeds)
+    opt._seeds = arr
+    return opt
+
+
+def read_plink(opt):
+    """Read the .fam/.bed (and .y/.e) files an options struct names."""
+    n, p, me = int(opt.n), int(opt.m_g), int(opt.m_e)
+    packed = np.zeros(p * ((n + 3) // 4), dtype=np.uint8)
+    y = np.zeros(n)
+    e = np.zeros(n * me) if me else None
+    err = C.create_string_buffer(1024)
+    rc = lib().bmg_read_plink(C.byref(opt), _ptr(packed), _ptr(y), _ptr(e), err, 1024)
+    if rc != 0:
+        raise BmgError(rc, err.value.decode())
+    return packed, y, e
+
+
+class Context:
+    """All chains of one options struct on one dataset, on the current GPU."""
+
+    def __init__(self, opt):
+        self.opt = opt
+        self.m_g = int(opt.m_g)
+        self.n_types = int(opt.n_types)
+        self.n_chains = int(opt.n_chains)
+        h = C.c_void_p()
+        rc = lib().bmg_create(C.byref(opt), C.byref(h))
+        if rc != 0:
+            raise BmgError(rc, "bmg_create failed")
+        self.h = h
+
+    def _check(self, rc):
+        if rc != 0:
+            raise BmgError(rc, lib().bmg_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().bmg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def load_bed(self, packed):
+        packed = np.ascontiguousarray(packed, dtype=np.uint8)
+        self._check(lib().bmg_load_bed(self.h, _ptr(packed), int(self.opt.n), self.m_g))
+
+    def set_phenotypes(self, y, mask=None):
+        y = np.ascontiguousarray(y, dtype=np.float64)
+        m = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8)
+        n_pheno = 1 if y.ndim == 1 else y.shape[0]
+        self._check(lib().bmg_set_phenotypes(self.h, _ptr(y), _ptr(m), n_pheno))
+
+    def set_covariates(self, e):
+        if e is None:
+            self._check(lib().bmg_set_covariates(self.h, None, 0))
+            return
+        e = np.ascontiguousarray(e, dtype=np.float64).reshape(-1)
+        self._check(lib().bmg_set_covariates(self.h, _ptr(e), int(self.opt.m_e)))
+
+    def precompute(self):
+        self._check(lib().bmg_precompute(self.h))
+
+    def precomputed(self):
+        off = C.c_uint32()
+        self._check(lib().bmg_get_precomputed(self.h, None, C.byref(off)))
+        xx = np.zeros(self.m_g * off.value)
+        self._check(lib().bmg_get_precomputed(self.h, _ptr(xx), C.byref(off)))
+        return xx.reshape(self.m_g, off.value)
+
+    def run(self, n_iter, collect=True):
+        col = abi.TraceCollector() if collect else None
+        sink = C.byref(col.sink) if col else None
+        self._check(lib().bmg_run(self.h, int(n_iter), sink))
+        return col
+
+    def scan(self):
+        pr = np.zeros(self.n_chains * self.m_g)
+        prt = np.zeros(self.n_chains * self.m_g * self.n_types) if self.n_types > 1 else None
+        self._check(lib().bmg_scan(self.h, _ptr(pr), _ptr(prt)))
+        pr = pr.reshape(self.n_chains, self.m_g)
+        if prt is not None:
+            prt = prt.reshape(self.n_chains, self.m_g, self.n_types)
+        return pr, prt
+
+    def state(self, chain=0, cap=4096):
+        st = abi.ChainState()
+        loci = np.zeros(cap, dtype=np.uint32)
+        types = np.zeros(cap, dtype=np.uint8)
+        self._check(lib().bmg_get_state(self.h, chain, C.byref(st), _ptr(loci), _ptr(types), cap))
+        k = st.model_size
+        return st, loci[:k].copy(), types[:k].copy()
+
+    def rao(self, chain=0):
+        p = np.zeros(self.m_g)
+        pt = np.zeros(self.m_g * self.n_types) if self.n_types > 1 else None
+        self._check(lib().bmg_get_rao(self.h, chain, _ptr(p), _ptr(pt)))
+        return p, (pt.reshape(self.m_g, self.n_types) if pt is not None else None)
+
+    def data_stats(self):
+        out = np.zeros(4)
+        self._check(lib().bmg_get_data_stats(self.h, _ptr(out)))
+        return out
+
+    def timings(self):
+        out = np.zeros(4)
+        self._check(lib().bmg_get_timings(self.h, _ptr(out)))
+        return out
+
+    def finish(self):
+        self._check(lib().bmg_finish(self.h))
+
+
+def run_ini(path, n_iter=None, write_files=True):
+    """Run a reference INI end to end on the GPU, writing the reference's files."""
+    opt = options_from_ini(path, quiet=False)
+    opt.write_files = 1 if write_files else 0
+    packed, y, e = read_plink(opt)
+    ctx = Context(opt)
+    ctx.load_bed(packed)
+    ctx.set_phenotypes(y)
+    ctx.set_covariates(e)
+    ctx.precompute()
+    ctx.run(opt.do_n_iter if n_iter is None else n_iter, collect=False)
+    ctx.finish()
+    return ctx

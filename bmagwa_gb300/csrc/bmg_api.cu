@@ -1,0 +1,1081 @@
+// libbmg host side: context, device memory, the iteration schedule and the
+// reference's output files.
+//
+// Launch schedule per chunk of iterations: the move kernel (one CTA per
+// chain) runs iterations up to and including the next Rao-Blackwellisation
+// step (src/sampler.cpp:731: (iter + 1) % n_rao == 0); then the p-wide scan
+// and the proposal-prefix rebuild run for all chains at once.  The schedule
+// is the same for every chain, so it is known on the host; the launches of a
+// chunk are captured once in a CUDA graph and replayed.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <ctime>
+#include <fstream>
+#include <iomanip>
+#include <memory>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "bmg.h"
+#include "bmg_internal.h"
+#include "dev/state.h"
+
+extern "C" __global__ void bmg_prep_kernel(uint8_t* geno, uint64_t n, uint64_t p, uint32_t gs,
+                                           int recode, int32_t* cnt, int32_t* missing);
+extern "C" __global__ void bmg_trace_reset_kernel(DevChain* ch, int n_chains);
+extern "C" __global__ void bmg_init_kernel(DevConst K);
+extern "C" __global__ void bmg_rbprep_kernel(DevConst K);
+extern "C" __global__ void bmg_move_kernel(DevConst K, int max_iters);
+extern "C" __global__ void bmg_scan_simt_kernel(DevConst K, const int64_t* resid_t);
+extern "C" __global__ void bmg_resid_transpose_kernel(DevConst K, int64_t* resid_t);
+extern "C" __global__ void bmg_rebuild_kernel(DevConst K, int force);
+// tensor-core scan (scan_tc.cu)
+extern "C" int bmg_scan_tc_launch(const DevConst* K, cudaStream_t stream);
+extern "C" int bmg_scan_tc_supported(const DevConst* K);
+
+using bmg_host::bmg_error;
+
+namespace {
+
+#define CK(x)                                                                       \
+  do {                                                                              \
+    cudaError_t e_ = (x);                                                           \
+    if (e_ != cudaSuccess)                                                          \
+      throw bmg_error(BMG_ECUDA, std::string(#x) + ": " + cudaGetErrorString(e_));  \
+  } while (0)
+
+struct ChainFiles {
+  std::ofstream log, loci, modelsize, jumpdistance, log_likelihood, log_prior, move_type,
+      move_size, pve, alpha, sigma2, types, beta;
+  bool open = false;
+};
+
+const char* kTypeName[5] = {"A", "H", "D", "R", "AH"};
+
+}  // namespace
+
+struct bmg_ctx {
+  bmg_options opt;
+  std::vector<uint32_t> seeds;
+  std::string err;
+  uint64_t n = 0, p = 0;
+  uint32_t C = 0, km = 0, L = 6, gs = 0, n_pad = 0;
+  bool have_geno = false, have_y = false, have_e = false, ready = false;
+  std::vector<int32_t> cnt_h;
+  std::vector<double> y_h, e_h, pre_h;
+  double var_x = 0, mean_x = 0, var_y = 0, yy = 0;
+  double g_a = 0, g_b = 0, s2_sigma2 = 0, s2_tau2[4] = {0, 0, 0, 0};
+  std::vector<void*> allocs;
+  DevConst K;
+  int64_t* resid_t = nullptr;
+  cudaStream_t stream = nullptr;
+  std::vector<ChainFiles> files;
+  std::vector<DevChain> ch_h;
+  double ms[4] = {0, 0, 0, 0};
+  uint64_t n_iter = 0;
+  time_t t_start = 0;
+  int max_ms = 0;
+  // host copies of the trace buffers
+  std::vector<uint8_t> h_jump, h_mtype, h_msize, h_types;
+  std::vector<uint32_t> h_msz, h_loci;
+  std::vector<double> h_ll, h_lp, h_s2, h_alpha, h_pve, h_beta, h_log;
+
+  template <class T>
+  T* dalloc(size_t count, bool zero = true)
+  {
+    void* ptr = nullptr;
+    size_t bytes = std::max<size_t>(1, count * sizeof(T));
+    CK(cudaMalloc(&ptr, bytes));
+    allocs.push_back(ptr);
+    if (zero) CK(cudaMemset(ptr, 0, bytes));
+    return static_cast<T*>(ptr);
+  }
+  ~bmg_ctx()
+  {
+    for (void* a : allocs) cudaFree(a);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+static bmg_status fail(bmg_ctx* ctx, const bmg_error& e)
+{
+  if (ctx) ctx->err = e.what();
+  return e.status;
+}
+
+#define API_BEGIN try {
+#define API_END                                                    \
+  }                                                                \
+  catch (const bmg_error& e) { return fail(ctx, e); }             \
+  catch (const std::exception& e) { return fail(ctx, bmg_error(BMG_EINVAL, e.what())); }
+
+// ------------------------------------------------------------------ helpers
+
+/* src/utils.cpp:144-152 */
+static void geometric_cdf(int maxsize, double p, double* values)
+{
+  double q = 1 - p, qp = q;
+  for (int i = 0; i < maxsize; ++i) {
+    values[i] = 1 - q;
+    q *= qp;
+  }
+}
+
+// in-order rank of every node of a heap-shaped binary tree with p nodes
+static void inorder_ranks(uint64_t p, std::vector<int32_t>& pos, std::vector<int32_t>& inv)
+{
+  pos.assign(p, 0);
+  inv.assign(p, 0);
+  std::vector<uint64_t> stack;
+  uint64_t node = 0;
+  int32_t rank = 0;
+  while (node < p || !stack.empty()) {
+    while (node < p) {
+      stack.push_back(node);
+      node = 2 * node + 1;
+    }
+    node = stack.back();
+    stack.pop_back();
+    pos[node] = rank;
+    inv[rank] = (int32_t)node;
+    ++rank;
+    node = 2 * node + 2;
+  }
+}
+
+static int fixed_exponent(double absmax, uint64_t n)
+{
+  // largest s with n * absmax * 2^s < 2^61 (so sums of 2|x| fit in int64)
+  if (!(absmax > 0)) return 0;
+  return (int)std::floor(61.0 - std::log2((double)n) - std::log2(absmax)) - 1;
+}
+
+static void check_ready(bmg_ctx* ctx)
+{
+  if (!ctx->ready) throw bmg_error(BMG_EINVAL, "bmg_precompute has not run");
+}
+
+static void device_error_check(bmg_ctx* ctx)
+{
+  CK(cudaMemcpyAsync(ctx->ch_h.data(), ctx->K.ch, sizeof(DevChain) * ctx->C, cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  for (uint32_t c = 0; c < ctx->C; ++c) {
+    int e = ctx->ch_h[c].error;
+    if (e == BMG_DERR_NONE) continue;
+    const char* what = "device error";
+    bmg_status st = BMG_ECUDA;
+    switch (e) {
+      case BMG_DERR_CAPACITY: what = "Not enough memory for adding term (max_model_size)"; st = BMG_EINVAL; break;
+      case BMG_DERR_NAN: what = "raob max_types is nan"; st = BMG_ENUMERIC; break;
+      case BMG_DERR_RNG: what = "gamma sampler ran out of attempts"; st = BMG_ENUMERIC; break;
+      case BMG_DERR_PEND: what = "proposal flip list overflow"; st = BMG_ECUDA; break;
+      case BMG_DERR_TRACE: what = "trace buffer overflow"; st = BMG_ECUDA; break;
+      case BMG_DERR_REMSET: what = "model too large for the removal proposal set"; st = BMG_EINVAL; break;
+      case BMG_DERR_START: what = "Sampler cannot start from non-finite likelihood."; st = BMG_ENOTPD; break;
+    }
+    throw bmg_error(st, std::string(what) + " (chain " + std::to_string(c) + ")");
+  }
+}
+
+// ---------------------------------------------------------------- create
+
+extern "C" bmg_status bmg_create(const bmg_options* opt, bmg_ctx** out)
+{
+  bmg_ctx* ctx = nullptr;
+  try {
+    if (!opt || !out) throw bmg_error(BMG_EINVAL, "null argument");
+    std::unique_ptr<bmg_ctx> c(new bmg_ctx());
+    ctx = c.get();
+    c->opt = *opt;
+    if (opt->n_chains == 0 || !opt->seeds) throw bmg_error(BMG_EINVAL, "n_chains and seeds are required");
+    c->seeds.assign(opt->seeds, opt->seeds + opt->n_chains);
+    c->opt.seeds = c->seeds.data();
+    if (opt->sampler_type != 0)
+      throw bmg_error(BMG_EUNSUPPORTED, "only the PMV sampler runs on the GPU path");
+    if (opt->delay_rejection != 0)
+      throw bmg_error(BMG_EUNSUPPORTED, "delayed rejection is not on the GPU path (set delay_rejection = 0)");
+    if (opt->n == 0 || opt->m_g == 0) throw bmg_error(BMG_EINVAL, "n and m_g must be positive");
+    if (opt->n_types == 0 || opt->n_types > 5) throw bmg_error(BMG_EINVAL, "types");
+    if (opt->thin == 0 || opt->n_rao == 0 || opt->n_sample_tau2_and_missing == 0)
+      throw bmg_error(BMG_EINVAL, "thin, n_rao and n_sample_tau2_and_missing must be positive");
+    if (opt->n_rao % opt->thin != 0) throw bmg_error(BMG_EINVAL, "Config error: n_rao should be a multiple of thin");
+    c->n = opt->n;
+    c->p = opt->m_g;
+    c->C = opt->n_chains;
+    c->km = opt->max_model_size ? opt->max_model_size : 1024;
+    c->L = opt->scan_limbs ? opt->scan_limbs : 6;
+    if (c->L < 3 || c->L > 7) throw bmg_error(BMG_EINVAL, "scan_limbs must be 3..7");
+    c->max_ms = (int)std::min<uint64_t>(std::min<uint64_t>(c->p, 255), opt->max_move_size);
+    if (c->km + (uint32_t)c->max_ms > BMG_REMSET_MAX)
+      throw bmg_error(BMG_EINVAL, "max_model_size + max_move_size exceeds the device limit");
+    if (c->km < opt->m_e + 3) throw bmg_error(BMG_EINVAL, "max_model_size too small");
+    if (c->p >= (1ull << 31)) throw bmg_error(BMG_EINVAL, "m_g too large");
+    c->n_pad = (uint32_t)(((c->n + 127) / 128) * 128);
+    c->gs = c->n_pad / 4;
+    CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    c->ch_h.resize(c->C);
+    *out = c.release();
+    return BMG_OK;
+  } catch (const bmg_error& e) {
+    if (out) *out = nullptr;
+    return e.status;
+  } catch (const std::exception& e) {
+    if (out) *out = nullptr;
+    return BMG_EINVAL;
+  }
+}
+
+extern "C" void bmg_destroy(bmg_ctx* ctx) { delete ctx; }
+
+extern "C" const char* bmg_last_error(const bmg_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+extern "C" const char* bmg_status_string(bmg_status s)
+{
+  switch (s) {
+    case BMG_OK: return "BMG_OK";
+    case BMG_EINVAL: return "BMG_EINVAL";
+    case BMG_EIO: return "BMG_EIO";
+    case BMG_ECUDA: return "BMG_ECUDA";
+    case BMG_ENOTPD: return "BMG_ENOTPD";
+    case BMG_ETIMEOUT: return "BMG_ETIMEOUT";
+    case BMG_ENOMEM: return "BMG_ENOMEM";
+    case BMG_EUNSUPPORTED: return "BMG_EUNSUPPORTED";
+    case BMG_ENUMERIC: return "BMG_ENUMERIC";
+  }
+  return "unknown";
+}
+
+// ------------------------------------------------------------------ data
+
+extern "C" bmg_status bmg_load_bed(bmg_ctx* ctx, const uint8_t* packed, uint64_t n, uint64_t p)
+{
+  if (!ctx) return BMG_EINVAL;
+  API_BEGIN
+  if (!packed) throw bmg_error(BMG_EINVAL, "null genotypes");
+  if (n != ctx->n || p != ctx->p) throw bmg_error(BMG_EINVAL, "genotype sizes differ from the options");
+  const uint64_t stride = (n + 3) / 4, gs = ctx->gs;
+  std::vector<uint8_t> rows(gs * p, 0);
+  const int tail = (int)(n % 4);
+  for (uint64_t j = 0; j < p; ++j) {
+    std::memcpy(&rows[j * gs], packed + j * stride, stride);
+    if (tail) rows[j * gs + stride - 1] &= (uint8_t)((1u << (2 * tail)) - 1);
+  }
+  uint8_t* g = ctx->dalloc<uint8_t>(gs * p, false);
+  int32_t* cnt = ctx->dalloc<int32_t>(2 * p);
+  int32_t* miss = ctx->dalloc<int32_t>(p);
+  CK(cudaMemcpyAsync(g, rows.data(), rows.size(), cudaMemcpyHostToDevice, ctx->stream));
+  unsigned blocks = (unsigned)std::min<uint64_t>((p + 7) / 8, 152 * 16);
+  bmg_prep_kernel<<<blocks, 256, 0, ctx->stream>>>(g, n, p, ctx->gs, ctx->opt.recode_g_to_minor_allele_count,
+                                                   cnt, miss);
+  CK(cudaGetLastError());
+  ctx->cnt_h.resize(2 * p);
+  std::vector<int32_t> miss_h(p);
+  CK(cudaMemcpyAsync(ctx->cnt_h.data(), cnt, 8 * p, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(miss_h.data(), miss, 4 * p, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  for (uint64_t j = 0; j < p; ++j)
+    if (miss_h[j] != 0)
+      throw bmg_error(BMG_EUNSUPPORTED, "missing genotype calls are not on the GPU path (SNP " +
+                                            std::to_string(j) + ")");
+  /* src/data.cpp:403-434 from the counts (no missing calls) */
+  double total_var = 0, total_mean = 0;
+  uint64_t nv = 0, nm = 0;
+  for (uint64_t j = 0; j < p; ++j) {
+    double n1 = ctx->cnt_h[2 * j], n2 = ctx->cnt_h[2 * j + 1];
+    double sq = n1 + 4.0 * n2, s = n1 + 2.0 * n2;
+    double ng = (double)n;
+    if (n > 1) {
+      total_mean += s / ng;
+      total_var += (sq - s * s / ng) / (ng - 1);
+      ++nm;
+      ++nv;
+    } else {
+      total_mean += s / ng;
+      ++nm;
+    }
+  }
+  ctx->var_x = total_var / nv;
+  ctx->mean_x = total_mean / nm;
+  ctx->K.geno = g;
+  ctx->K.cnt = cnt;
+  ctx->have_geno = true;
+  return BMG_OK;
+  API_END
+}
+
+extern "C" bmg_status bmg_set_phenotypes(bmg_ctx* ctx, const double* y, const uint8_t* mask, uint32_t n_pheno)
+{
+  if (!ctx) return BMG_EINVAL;
+  API_BEGIN
+  if (!y) throw bmg_error(BMG_EINVAL, "null phenotypes");
+  if (n_pheno != 1 || mask)
+    throw bmg_error(BMG_EUNSUPPORTED, "one phenotype without mask per context on this path");
+  const uint64_t n = ctx->n;
+  ctx->y_h.assign(y, y + n);
+  double yy = 0, sq = 0, s = 0, amax = 0;
+  for (uint64_t i = 0; i < n; ++i) {
+    if (!std::isfinite(y[i])) throw bmg_error(BMG_EINVAL, "non-finite phenotype");
+    yy += y[i] * y[i];
+    amax = std::max(amax, std::fabs(y[i]));
+  }
+  for (uint64_t i = 0; i < n; ++i) { sq += y[i] * y[i]; s += y[i]; }
+  ctx->yy = yy;
+  ctx->var_y = (sq - s * s / n) / (n - 1);
+  int sy = fixed_exponent(amax, n);
+  std::vector<int64_t> yint(n);
+  for (uint64_t i = 0; i < n; ++i) yint[i] = (int64_t)std::llrint(std::ldexp(y[i], sy));
+  double* yd = ctx->dalloc<double>(n);
+  int64_t* yi = ctx->dalloc<int64_t>(n);
+  CK(cudaMemcpyAsync(yd, y, 8 * n, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(yi, yint.data(), 8 * n, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->K.y = yd;
+  ctx->K.yint = yi;
+  ctx->K.sy = sy;
+  ctx->K.y_absmax = amax;
+  ctx->have_y = true;
+  return BMG_OK;
+  API_END
+}
+
+extern "C" bmg_status bmg_set_covariates(bmg_ctx* ctx, const double* e, uint32_t m_e)
+{
+  if (!ctx) return BMG_EINVAL;
+  API_BEGIN
+  if (m_e != ctx->opt.m_e) throw bmg_error(BMG_EINVAL, "m_e differs from the options");
+  if (m_e > 7) throw bmg_error(BMG_EUNSUPPORTED, "at most 7 covariates on this path");
+  if (m_e > 0 && !e) throw bmg_error(BMG_EINVAL, "null covariates");
+  ctx->e_h.assign(e, e + (size_t)ctx->n * m_e);
+  ctx->have_e = true;
+  return BMG_OK;
+  API_END
+}
+
+// ------------------------------------------------------------- precompute
+
+extern "C" bmg_status bmg_precompute(bmg_ctx* ctx)
+{
+  if (!ctx) return BMG_EINVAL;
+  API_BEGIN
+  if (!ctx->have_geno || !ctx->have_y) throw bmg_error(BMG_EINVAL, "genotypes and phenotypes must be loaded first");
+  if (ctx->opt.m_e > 0 && !ctx->have_e) throw bmg_error(BMG_EINVAL, "covariates must be set (m_e > 0)");
+  const bmg_options& o = ctx->opt;
+  const uint64_t n = ctx->n, p = ctx->p;
+  const uint32_t C = ctx->C, km = ctx->km, me = o.m_e + 1;
+  DevConst& K = ctx->K;
+  K.n = n;
+  K.p = p;
+  K.gs = ctx->gs;
+  K.nw = ctx->gs / 4;
+  K.m_e = me;
+  K.km = km;
+  K.n_chains = C;
+  K.n_types = o.n_types;
+  int allow_types[5] = {0, 0, 0, 0, 0}, allow_terms[4] = {0, 0, 0, 0};
+  for (uint32_t t = 0; t < o.n_types; ++t) {
+    K.types[t] = o.types[t];
+    allow_types[o.types[t]] = 1;
+    if (o.types[t] == BMG_TYPE_AH) { allow_terms[0] = allow_terms[1] = 1; }
+    else allow_terms[o.types[t]] = 1;
+  }
+  for (int t = 0; t < 5; ++t) K.allow_types[t] = allow_types[t];
+  for (int t = 0; t < 4; ++t) K.allow_terms[t] = allow_terms[t];
+  /* src/precomputed_snp_covariances.hpp:58-84 */
+  bool ah = allow_types[4], a = allow_types[0], h = allow_types[1];
+  int offset = 2 * (int)o.n_types + (ah ? 1 : 0) * (1 + ((a && h) ? -2 : 0) + ((a || h) ? 0 : 2));
+  K.offset = offset;
+  int oi = 0;
+  K.n_terms = 0;
+  for (int t = 0; t < 4; ++t) {
+    K.offset_type[t] = allow_terms[t] ? oi++ : -1;
+    if (allow_terms[t]) K.term_of[K.n_terms++] = t;
+  }
+  // per-SNP sums and centred second moments from the counts (exact integers)
+  ctx->pre_h.assign(p * offset, 0.0);
+  for (uint64_t j = 0; j < p; ++j) {
+    double n1 = ctx->cnt_h[2 * j], n2 = ctx->cnt_h[2 * j + 1];
+    double* loc = &ctx->pre_h[j * offset];
+    for (int t = 0; t < 4; ++t) {
+      if (!allow_terms[t]) continue;
+      double ch_ = (t == 3) ? 0 : 1, cr = (t == 0) ? 2 : (t == 1 ? 0 : 1);
+      double xs = ch_ * n1 + cr * n2;
+      double xx = ch_ * ch_ * n1 + cr * cr * n2;
+      *loc++ = xs;
+      *loc++ = xx - xs * xs / (double)n;
+    }
+    if (ah) {
+      double as = n1 + 2 * n2, hs = n1;
+      *loc++ = n1 - as * hs / (double)n;
+    }
+  }
+  double* pre = ctx->dalloc<double>(p * offset, false);
+  CK(cudaMemcpyAsync(pre, ctx->pre_h.data(), 8 * p * offset, cudaMemcpyHostToDevice, ctx->stream));
+  K.pre = pre;
+  K.lvar = nullptr;
+  // in-order ranks of the proposal tree
+  std::vector<int32_t> pos, inv;
+  inorder_ranks(p, pos, inv);
+  int32_t* dpos = ctx->dalloc<int32_t>(p, false);
+  int32_t* dinv = ctx->dalloc<int32_t>(p, false);
+  CK(cudaMemcpyAsync(dpos, pos.data(), 4 * p, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(dinv, inv.data(), 4 * p, cudaMemcpyHostToDevice, ctx->stream));
+  K.pos = dpos;
+  K.inv = dinv;
+  // covariates with the constant column (src/data.hpp:48,53)
+  std::vector<double> E((size_t)n * me, 1.0);
+  for (uint32_t j = 1; j < me; ++j)
+    for (uint64_t i = 0; i < n; ++i) E[(size_t)j * n + i] = ctx->e_h[(size_t)(j - 1) * n + i];
+  std::vector<double> ee((size_t)me * me, 0.0), ey(me, 0.0), emax(me, 1.0);
+  for (uint32_t j = 0; j < me; ++j)
+    for (uint32_t i = 0; i <= j; ++i) {
+      double t = 0;
+      for (uint64_t l = 0; l < n; ++l) t += E[(size_t)i * n + l] * E[(size_t)j * n + l];
+      ee[(size_t)j * me + i] = t;
+    }
+  for (uint32_t j = 0; j < me; ++j) {
+    double t = 0;
+    for (uint64_t l = 0; l < n; ++l) t += E[(size_t)j * n + l] * ctx->y_h[l];
+    ey[j] = t;
+  }
+  std::vector<int64_t> eint((size_t)n * me, 0);
+  std::vector<int32_t> se(me, 0);
+  for (uint32_t j = 1; j < me; ++j) {
+    double am = 0;
+    for (uint64_t l = 0; l < n; ++l) am = std::max(am, std::fabs(E[(size_t)j * n + l]));
+    emax[j] = am;
+    se[j] = fixed_exponent(am, n);
+    for (uint64_t l = 0; l < n; ++l) eint[(size_t)j * n + l] = (int64_t)std::llrint(std::ldexp(E[(size_t)j * n + l], se[j]));
+  }
+  double* dE = ctx->dalloc<double>(E.size(), false);
+  int64_t* dEi = ctx->dalloc<int64_t>(eint.size(), false);
+  int32_t* dse = ctx->dalloc<int32_t>(me, false);
+  double* dee = ctx->dalloc<double>(ee.size(), false);
+  double* dey = ctx->dalloc<double>(me, false);
+  double* demax = ctx->dalloc<double>(me, false);
+  std::vector<double> ite(me, o.inv_tau2_e_val);
+  ite[0] = o.inv_tau2_e_const_val;
+  double* dite = ctx->dalloc<double>(me, false);
+  CK(cudaMemcpyAsync(dE, E.data(), 8 * E.size(), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(dEi, eint.data(), 8 * eint.size(), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(dse, se.data(), 4 * me, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(dee, ee.data(), 8 * ee.size(), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(dey, ey.data(), 8 * me, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(demax, emax.data(), 8 * me, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(dite, ite.data(), 8 * me, cudaMemcpyHostToDevice, ctx->stream));
+  K.e = dE;
+  K.eint = dEi;
+  K.se = dse;
+  K.ee = dee;
+  K.ey = dey;
+  K.e_absmax = demax;
+  K.inv_tau2_e = dite;
+  K.yy = ctx->yy;
+  /* src/sampler.hpp:173-199 */
+  double s2s = (o.s2_sigma2 > 0) ? o.s2_sigma2
+                                 : ctx->var_y * (1 - o.R2mode_sigma2) * (o.nu_sigma2 + 2) / o.nu_sigma2;
+  ctx->s2_sigma2 = s2s;
+  double s2t[4] = {0, 0, 0, 0};
+  for (int t = 0; t < 4; ++t) {
+    if (!allow_terms[t]) continue;
+    if (o.s2_tau2[t] > 0) s2t[t] = o.s2_tau2[t];
+    else
+      s2t[t] = o.eh_tau2[t] * (o.nu_tau2[t] - 2) /
+               (o.nu_tau2[t] * (ctx->var_x + ctx->mean_x * ctx->mean_x) * (1 - o.R2mode_sigma2));
+    ctx->s2_tau2[t] = s2t[t];
+  }
+  /* src/prior.hpp:45-122 */
+  if (s2s <= 0)
+    throw bmg_error(BMG_EINVAL, "Prior specification error: s2_sigma2 is not positive (Probably option s2_sigma2 is "
+                                "not specified and using R2mode_sigma2 leads to the invalid value).");
+  if (o.nu_sigma2 < 0) throw bmg_error(BMG_EINVAL, "Prior specification error: nu_sigma2 is negative.");
+  double ga, gb;
+  {
+    double eq = o.e_qg, vq = o.var_qg;
+    if (p > 1) {
+      double z = (vq - eq * (1 - eq)) / ((p - 1) * eq);
+      ga = (z - 1) / (1 - p * z / eq);
+      gb = (p / eq - 1) * ga;
+    } else {
+      double z = eq / (1 - eq);
+      gb = z / vq / std::pow(1 + z, 3) - 1 / (1 + z);
+      ga = z * gb;
+    }
+    if (ga <= 0 || gb <= 0 || std::isnan(ga) || std::isnan(gb)) throw bmg_error(BMG_EINVAL, "Invalid a or b.");
+  }
+  ctx->g_a = ga;
+  ctx->g_b = gb;
+  K.g_a = ga;
+  K.g_b = gb;
+  double tps = 0;
+  for (int t = 0; t < 5; ++t) {
+    K.types_prior[t] = allow_types[t] ? o.types_prior[t] : NAN;
+    if (allow_types[t]) tps += o.types_prior[t];
+  }
+  K.types_prior_sum = tps;
+  double alpha0 = std::max(0.5, o.mu_alpha), alpha2 = alpha0 * alpha0;
+  double inv0[4];
+  for (int t = 0; t < 4; ++t) {
+    if (allow_terms[t]) {
+      if (s2t[t] <= 0)
+        throw bmg_error(BMG_EINVAL, std::string("Prior specification error: s2_tau2 for ") + kTypeName[t] +
+                                        " is not positive.");
+      if (o.nu_tau2[t] <= 0)
+        throw bmg_error(BMG_EINVAL, std::string("Prior specification error: nu_tau2 for ") + kTypeName[t] +
+                                        " is not positive.");
+      K.nu_tau2[t] = o.nu_tau2[t];
+      K.s2_tau2[t] = s2t[t];
+      K.nus2_tau2[t] = o.nu_tau2[t] * s2t[t];
+      double tau2_init = K.nus2_tau2[t] / std::max(0.1, (o.nu_tau2[t] - 2));
+      inv0[t] = 1.0 / (alpha2 * tau2_init);
+    } else {
+      K.nu_tau2[t] = K.s2_tau2[t] = K.nus2_tau2[t] = NAN;
+      inv0[t] = NAN;
+    }
+  }
+  K.n_plus_nu = (double)n + o.nu_sigma2;
+  K.minus_n_plus_nu_2 = -0.5 * K.n_plus_nu;
+  K.nus2_plus_yy = o.nu_sigma2 * s2s + ctx->yy;
+  K.mu_alpha = o.mu_alpha;
+  K.use_individual_tau2 = o.use_individual_tau2;
+  K.rng_nu = (double)n + o.nu_sigma2;
+  K.n_rao = o.n_rao;
+  K.thin = o.thin;
+  K.n_sample_tau2 = o.n_sample_tau2_and_missing;
+  K.verbosity = o.verbosity;
+  K.max_move_size = (uint32_t)ctx->max_ms;
+  K.max_nbh = o.max_SNP_neighborhood_size;
+  K.p_move_size_nbs = o.p_move_size_nbs;
+  K.p_move_size_nbc = o.p_move_size_nbc;
+  K.adapt_p_move_size = o.adapt_p_move_size && ctx->max_ms > 1;
+  K.acpt_goal = o.p_move_size_acpt_goal;
+  K.adaptation = o.adaptation;
+  K.flat_proposal_dist = o.flat_proposal_dist;
+  K.save_beta = o.save_beta;
+  K.q_add_min = 1.0 / (p - o.e_qg);
+  K.q_rem_min = 1.0 / o.e_qg;
+  // prior tables, evaluated with the reference's expressions (src/prior.hpp:144-183)
+  const uint32_t tw = km + 2;
+  K.tw = tw;
+  std::vector<double> tab((size_t)22 * tw, 0.0);
+  auto T = [&](int which, uint32_t k) -> double& { return tab[(size_t)which * tw + k]; };
+  const double mg = (double)p;
+  for (uint32_t k = 0; k < tw; ++k) {
+    int nl = (int)k;
+    T(0, k) = std::log(ga + nl) - std::log(gb + p - nl - 1);
+    T(1, k) = std::log(gb + p - nl) - std::log(ga + nl - 1);
+    for (int t = 0; t < 5; ++t) {
+      double tp = K.types_prior[t];
+      T(2 + t, k) = std::log(tp + nl);
+      T(7 + t, k) = std::log(tp + nl - 1);
+      T(14 + t, k) = std::lgamma(tp + (double)nl);
+    }
+    T(12, k) = std::log(tps + nl);
+    T(13, k) = std::log(tps + nl - 1);
+    T(19, k) = std::lgamma(ga + (double)nl);
+    T(20, k) = std::lgamma(gb + mg - (double)nl);
+    T(21, k) = std::lgamma(tps + (double)nl);
+  }
+  double* dtab = ctx->dalloc<double>(tab.size(), false);
+  CK(cudaMemcpyAsync(dtab, tab.data(), 8 * tab.size(), cudaMemcpyHostToDevice, ctx->stream));
+  K.tab = dtab;
+  int qbits = 0;
+  while ((1ull << qbits) < p + 1) ++qbits;
+  K.qs = 61 - qbits;
+  // per-chain state
+  K.cur = ctx->dalloc<DevModel>(C);
+  K.nm = ctx->dalloc<DevModel>(C);
+  K.ch = ctx->dalloc<DevChain>(C);
+  K.rb = ctx->dalloc<RbParams>(C);
+  const size_t pc = (size_t)p * C;
+  K.p_prop = ctx->dalloc<double>(pc, false);
+  K.p_prop_types = ctx->dalloc<double>(o.n_types > 1 ? pc * o.n_types : 1, false);
+  K.p_rao = ctx->dalloc<double>(pc);
+  K.p_rao_types = ctx->dalloc<double>(o.n_types > 1 ? pc * o.n_types : 1);
+  K.p_r = ctx->dalloc<double>(pc);
+  K.p_r_types = ctx->dalloc<double>(o.n_types > 1 ? pc * o.n_types : 1);
+  K.q_ms = ctx->dalloc<double>((size_t)C * 256);
+  K.q_nbs = ctx->dalloc<double>((size_t)C * 128);
+  K.q_nbc = ctx->dalloc<double>((size_t)C * 256);
+  K.r_ms_sum = ctx->dalloc<double>((size_t)C * 256);
+  K.r_ms_n = ctx->dalloc<double>((size_t)C * 256);
+  K.q_p0_ms = ctx->dalloc<double>((size_t)C * 256);
+  K.cadd = ctx->dalloc<int64_t>((size_t)(p + 1) * C);
+  const size_t words = (p + 31) / 32;
+  K.inbits = ctx->dalloc<uint32_t>(words * C);
+  K.basebits = ctx->dalloc<uint32_t>(words * C);
+  K.model_inds = ctx->dalloc<int32_t>(pc, false);
+  CK(cudaMemsetAsync(K.model_inds, 0xff, 4 * pc, ctx->stream));
+  K.n_pad = ctx->n_pad;
+  K.limbs_n = ctx->L;
+  K.resid = ctx->dalloc<int64_t>((size_t)C * ctx->n_pad);
+  K.limbs = ctx->dalloc<uint16_t>((size_t)C * ctx->L * ctx->n_pad);
+  ctx->resid_t = ctx->dalloc<int64_t>((size_t)C * ctx->n_pad);
+  K.scratch = ctx->dalloc<double>((size_t)C * 2 * km);
+  // trace buffers of one chunk
+  uint32_t gi = o.graph_iters ? o.graph_iters : 64;
+  ctx->opt.graph_iters = gi;
+  DevTrace& tr = K.tr;
+  tr.iter_cap = gi;
+  tr.thin_cap = (uint32_t)(gi / o.thin + 2);
+  tr.loci_cap = tr.thin_cap * km;
+  tr.beta_cap = o.save_beta ? tr.thin_cap * km : 1;
+  tr.log_cap = o.verbosity ? (uint32_t)(gi / o.verbosity + 2) : 1;
+  tr.jump = ctx->dalloc<uint8_t>((size_t)C * tr.iter_cap);
+  tr.mtype = ctx->dalloc<uint8_t>((size_t)C * tr.iter_cap);
+  tr.msize = ctx->dalloc<uint8_t>((size_t)C * tr.iter_cap);
+  tr.msz = ctx->dalloc<uint32_t>((size_t)C * tr.thin_cap);
+  tr.loci = ctx->dalloc<uint32_t>((size_t)C * tr.loci_cap);
+  tr.types = ctx->dalloc<uint8_t>((size_t)C * tr.loci_cap);
+  tr.ll = ctx->dalloc<double>((size_t)C * tr.thin_cap);
+  tr.lp = ctx->dalloc<double>((size_t)C * tr.thin_cap);
+  tr.s2 = ctx->dalloc<double>((size_t)C * tr.thin_cap);
+  tr.alpha = ctx->dalloc<double>((size_t)C * tr.thin_cap);
+  tr.pve = ctx->dalloc<double>((size_t)C * tr.thin_cap * 3);
+  tr.beta = ctx->dalloc<double>((size_t)C * tr.beta_cap);
+  tr.logrec = ctx->dalloc<double>((size_t)C * tr.log_cap * BMG_LOGREC);
+  // models and chains
+  std::vector<DevModel> models(2 * C);
+  for (uint32_t c = 0; c < 2 * C; ++c) {
+    DevModel& M = models[c];
+    std::memset(&M, 0, sizeof(M));
+    M.xx = ctx->dalloc<double>((size_t)km * km);
+    M.l = ctx->dalloc<double>((size_t)km * km);
+    M.xy = ctx->dalloc<double>(km);
+    M.v = ctx->dalloc<double>(km);
+    M.inv = ctx->dalloc<double>(km);
+    M.beta = ctx->dalloc<double>(km);
+    M.mu_beta = ctx->dalloc<double>(km);
+    M.loci = ctx->dalloc<uint32_t>(km);
+    M.type_inds = ctx->dalloc<uint8_t>(km);
+    M.x_ind1 = ctx->dalloc<uint32_t>(km);
+    M.x_ind2 = ctx->dalloc<uint32_t>(km);
+    M.xc_snp = ctx->dalloc<uint32_t>(km);
+    M.xc_type = ctx->dalloc<int32_t>(km);
+    M.xcols = (int)me;
+    M.llen = M.vlen = M.blen = (int)me;
+    M.ll = NAN;
+    // covariate block (src/model.hpp:92-105)
+    std::vector<double> xx((size_t)me * km, 0.0);
+    for (uint32_t j = 0; j < me; ++j)
+      for (uint32_t i = 0; i <= j; ++i) xx[(size_t)j * km + i] = ee[(size_t)j * me + i];
+    CK(cudaMemcpyAsync(M.xx, xx.data(), 8 * xx.size(), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(M.xy, ey.data(), 8 * me, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(M.inv, ite.data(), 8 * me, cudaMemcpyHostToDevice, ctx->stream));
+    std::vector<int32_t> xt(me, 4);
+    CK(cudaMemcpyAsync(M.xc_type, xt.data(), 4 * me, cudaMemcpyHostToDevice, ctx->stream));
+  }
+  CK(cudaMemcpyAsync(K.cur, models.data(), sizeof(DevModel) * C, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(K.nm, models.data() + C, sizeof(DevModel) * C, cudaMemcpyHostToDevice, ctx->stream));
+  std::vector<DevChain> chs(C);
+  std::vector<double> qms((size_t)C * 256, 0.0), qnbs((size_t)C * 128, 0.0), qnbc((size_t)C * 256, 0.0);
+  const int mm2 = (ctx->max_ms + 1) / 2;
+  for (uint32_t c = 0; c < C; ++c) {
+    DevChain& h = chs[c];
+    std::memset(&h, 0, sizeof(h));
+    bmg_rng_init(&h.rng, ctx->seeds[c]);
+    h.n_rao_burnin = o.n_rao_burnin;
+    h.p_proposal_n = 1;
+    h.p_rao_n = 0;
+    h.n_moves[0] = h.n_moves[1] = h.n_moves[2] = 2;
+    h.n_acpt[0] = h.n_acpt[1] = h.n_acpt[2] = 1;
+    h.alpha = alpha0;
+    h.alpha2 = alpha2;
+    for (int t = 0; t < 4; ++t) h.inv_t2a2[t] = inv0[t];
+    h.p_move_size = o.p_move_size;
+    h.k_move_size = 1000.0 / (double)o.n_rao_burnin;
+    geometric_cdf(ctx->max_ms, o.p_move_size, &qms[(size_t)c * 256]);
+    geometric_cdf(mm2, o.p_move_size_nbs, &qnbs[(size_t)c * 128]);
+    geometric_cdf(ctx->max_ms, o.p_move_size_nbc, &qnbc[(size_t)c * 256]);
+  }
+  CK(cudaMemcpyAsync(K.ch, chs.data(), sizeof(DevChain) * C, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(K.q_ms, qms.data(), 8 * qms.size(), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(K.q_nbs, qnbs.data(), 8 * qnbs.size(), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(K.q_nbc, qnbc.data(), 8 * qnbc.size(), cudaMemcpyHostToDevice, ctx->stream));
+  /* src/sampler.hpp:351-362 */
+  double val = (ga / (ga + gb) * p) / (double)p;
+  std::vector<double> flat(pc, val);
+  CK(cudaMemcpyAsync(K.p_prop, flat.data(), 8 * pc, cudaMemcpyHostToDevice, ctx->stream));
+  if (o.n_types > 1) {
+    std::vector<double> ft(pc * o.n_types, 1.0 / o.n_types);
+    CK(cudaMemcpyAsync(K.p_prop_types, ft.data(), 8 * ft.size(), cudaMemcpyHostToDevice, ctx->stream));
+  }
+  bmg_init_kernel<<<C, 32, 0, ctx->stream>>>(K);
+  CK(cudaGetLastError());
+  bmg_rebuild_kernel<<<C, 1024, 0, ctx->stream>>>(K, 1);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  device_error_check(ctx);
+  ctx->ready = true;
+  return BMG_OK;
+  API_END
+}
+
+extern "C" bmg_status bmg_get_precomputed(bmg_ctx* ctx, double* xx, uint32_t* offset)
+{
+  if (!ctx) return BMG_EINVAL;
+  API_BEGIN
+  check_ready(ctx);
+  if (offset) *offset = (uint32_t)ctx->K.offset;
+  if (xx) std::memcpy(xx, ctx->pre_h.data(), 8 * ctx->pre_h.size());
+  return BMG_OK;
+  API_END
+}
+
+// ------------------------------------------------------------------- run
+
+static void launch_scan(bmg_ctx* ctx)
+{
+  DevConst& K = ctx->K;
+  bool tc = ctx->opt.scan_impl == BMG_SCAN_TCGEN05 && bmg_scan_tc_supported(&K);
+  if (tc) {
+    if (bmg_scan_tc_launch(&K, ctx->stream) != 0) throw bmg_error(BMG_ECUDA, "tensor-core scan launch failed");
+  } else {
+    bmg_resid_transpose_kernel<<<1024, 256, 0, ctx->stream>>>(K, ctx->resid_t);
+    unsigned blocks = 152 * 8;
+    bmg_scan_simt_kernel<<<blocks, 256, 0, ctx->stream>>>(K, ctx->resid_t);
+  }
+  CK(cudaGetLastError());
+}
+
+static void open_files(bmg_ctx* ctx)
+{
+  if (!ctx->opt.write_files || !ctx->files.empty()) return;
+  ctx->files.resize(ctx->C);
+  for (uint32_t c = 0; c < ctx->C; ++c) {
+    ChainFiles& f = ctx->files[c];
+    std::string b = std::string(ctx->opt.basename) + std::to_string(c);
+    auto ob = [&](std::ofstream& s, const char* suf, bool bin) {
+      s.open((b + suf).c_str(), bin ? std::ios::binary : std::ios::out);
+      if (!s.is_open()) throw bmg_error(BMG_EIO, "Failed to open file: " + b + suf);
+    };
+    ob(f.log, "_log.txt", false);
+    f.log << std::setprecision(3) << std::fixed;
+    ob(f.loci, "_loci.dat", true);
+    ob(f.modelsize, "_modelsize.dat", true);
+    ob(f.jumpdistance, "_jumpdistance.dat", true);
+    ob(f.log_likelihood, "_log_likelihood.dat", true);
+    ob(f.log_prior, "_log_prior.dat", true);
+    ob(f.move_type, "_move_type.dat", true);
+    ob(f.move_size, "_move_size.dat", true);
+    ob(f.pve, "_pve.dat", true);
+    ob(f.alpha, "_alpha.dat", true);
+    ob(f.sigma2, "_sigma2.dat", true);
+    if (ctx->opt.n_types > 1) ob(f.types, "_types.dat", true);
+    if (ctx->opt.save_beta) ob(f.beta, "_beta.dat", true);
+    f.log << "output " << b << std::endl
+          << "seed " << ctx->seeds[c] << std::endl
+          << "type (PMV = 0, NK = 1, KSC = 2, G = 3) " << 0 << std::endl
+          << "----------------------------------------------------" << std::endl;
+    f.open = true;
+  }
+}
+
+template <class T>
+static void d2h(bmg_ctx* ctx, std::vector<T>& h, const T* d, size_t count)
+{
+  h.resize(count);
+  if (count) CK(cudaMemcpyAsync(h.data(), d, sizeof(T) * count, cudaMemcpyDeviceToHost, ctx->stream));
+}
+
+static void drain_traces(bmg_ctx* ctx, uint64_t iter0, const bmg_trace_sink* sink)
+{
+  const DevTrace& tr = ctx->K.tr;
+  const uint32_t C = ctx->C;
+  d2h(ctx, ctx->h_jump, tr.jump, (size_t)C * tr.iter_cap);
+  d2h(ctx, ctx->h_mtype, tr.mtype, (size_t)C * tr.iter_cap);
+  d2h(ctx, ctx->h_msize, tr.msize, (size_t)C * tr.iter_cap);
+  d2h(ctx, ctx->h_msz, tr.msz, (size_t)C * tr.thin_cap);
+  d2h(ctx, ctx->h_ll, tr.ll, (size_t)C * tr.thin_cap);
+  d2h(ctx, ctx->h_lp, tr.lp, (size_t)C * tr.thin_cap);
+  d2h(ctx, ctx->h_s2, tr.s2, (size_t)C * tr.thin_cap);
+  d2h(ctx, ctx->h_alpha, tr.alpha, (size_t)C * tr.thin_cap);
+  d2h(ctx, ctx->h_pve, tr.pve, (size_t)C * tr.thin_cap * 3);
+  d2h(ctx, ctx->h_log, tr.logrec, (size_t)C * tr.log_cap * BMG_LOGREC);
+  CK(cudaMemcpyAsync(ctx->ch_h.data(), ctx->K.ch, sizeof(DevChain) * C, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  // loci / types / beta: only the used prefix of each chain
+  ctx->h_loci.resize((size_t)C * tr.loci_cap);
+  ctx->h_types.resize((size_t)C * tr.loci_cap);
+  ctx->h_beta.resize((size_t)C * tr.beta_cap);
+  for (uint32_t c = 0; c < C; ++c) {
+    const DevChain& h = ctx->ch_h[c];
+    if (h.tr_loci) {
+      CK(cudaMemcpyAsync(&ctx->h_loci[(size_t)c * tr.loci_cap], tr.loci + (size_t)c * tr.loci_cap,
+                         4 * (size_t)h.tr_loci, cudaMemcpyDeviceToHost, ctx->stream));
+      CK(cudaMemcpyAsync(&ctx->h_types[(size_t)c * tr.loci_cap], tr.types + (size_t)c * tr.loci_cap,
+                         (size_t)h.tr_loci, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    if (h.tr_beta)
+      CK(cudaMemcpyAsync(&ctx->h_beta[(size_t)c * tr.beta_cap], tr.beta + (size_t)c * tr.beta_cap,
+                         8 * (size_t)h.tr_beta, cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  for (uint32_t c = 0; c < C; ++c) {
+    const DevChain& h = ctx->ch_h[c];
+    bmg_trace_chunk k;
+    std::memset(&k, 0, sizeof(k));
+    k.chain = c;
+    k.iter0 = iter0;
+    k.n_iter = h.tr_iter;
+    k.jumpdistance = &ctx->h_jump[(size_t)c * tr.iter_cap];
+    k.move_type = &ctx->h_mtype[(size_t)c * tr.iter_cap];
+    k.move_size = &ctx->h_msize[(size_t)c * tr.iter_cap];
+    k.n_thin = h.tr_thin;
+    k.modelsize = &ctx->h_msz[(size_t)c * tr.thin_cap];
+    k.n_loci = h.tr_loci;
+    k.loci = &ctx->h_loci[(size_t)c * tr.loci_cap];
+    k.types = ctx->opt.n_types > 1 ? &ctx->h_types[(size_t)c * tr.loci_cap] : nullptr;
+    k.log_likelihood = &ctx->h_ll[(size_t)c * tr.thin_cap];
+    k.log_prior = &ctx->h_lp[(size_t)c * tr.thin_cap];
+    k.sigma2 = &ctx->h_s2[(size_t)c * tr.thin_cap];
+    k.alpha = &ctx->h_alpha[(size_t)c * tr.thin_cap];
+    k.pve = &ctx->h_pve[(size_t)c * tr.thin_cap * 3];
+    k.n_beta = h.tr_beta;
+    k.beta = ctx->opt.save_beta ? &ctx->h_beta[(size_t)c * tr.beta_cap] : nullptr;
+    if (sink && sink->fn) sink->fn(sink->user, &k);
+    if (ctx->opt.write_files) {
+      ChainFiles& f = ctx->files[c];
+      f.jumpdistance.write((const char*)k.jumpdistance, k.n_iter);
+      f.move_type.write((const char*)k.move_type, k.n_iter);
+      f.move_size.write((const char*)k.move_size, k.n_iter);
+      size_t lo = 0;
+      for (uint64_t t = 0; t < k.n_thin; ++t) {
+        uint32_t ms = k.modelsize[t];
+        f.modelsize.write((const char*)&k.modelsize[t], 4);
+        f.loci.write((const char*)&k.loci[lo], 4 * (size_t)ms);
+        if (ctx->opt.n_types > 1) f.types.write((const char*)&k.types[lo], ms);
+        lo += ms;
+        f.log_likelihood.write((const char*)&k.log_likelihood[t], 8);
+        f.log_prior.write((const char*)&k.log_prior[t], 8);
+        f.sigma2.write((const char*)&k.sigma2[t], 8);
+        f.pve.write((const char*)&k.pve[3 * t], 24);
+        f.alpha.write((const char*)&k.alpha[t], 8);
+      }
+      if (ctx->opt.save_beta && k.n_beta) f.beta.write((const char*)k.beta, 8 * k.n_beta);
+      // _log.txt lines (src/sampler.cpp:813-833)
+      for (uint32_t g = 0; g < h.tr_log; ++g) {
+        const double* r = &ctx->h_log[((size_t)c * tr.log_cap + g) * BMG_LOGREC];
+        f.log << "(" << (uint64_t)r[0] << ")"
+              << " acc.rate " << r[1] / r[0] << " acc.rate2 " << r[2] / r[3] << " acc.rate3 " << r[4] / r[5]
+              << " p_move_size " << r[6] << " model size " << (uint64_t)r[7] << " log p " << r[8] << " PVE "
+              << r[9] << "/" << r[10] << "/" << r[11] << " sigma2 " << r[12] << std::endl;
+      }
+      f.log.flush();
+    }
+  }
+}
+
+extern "C" bmg_status bmg_run(bmg_ctx* ctx, uint64_t n_iter, const bmg_trace_sink* sink)
+{
+  if (!ctx) return BMG_EINVAL;
+  API_BEGIN
+  check_ready(ctx);
+  if (ctx->n_iter == 0) ctx->t_start = time(nullptr);
+  open_files(ctx);
+  DevConst& K = ctx->K;
+  const uint64_t n_rao = ctx->opt.n_rao;
+  const uint32_t gi = ctx->opt.graph_iters;
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  CK(cudaEventRecord(e0, ctx->stream));
+  uint64_t done = 0;
+  while (done < n_iter) {
+    uint64_t chunk = std::min<uint64_t>(n_iter - done, gi);
+    uint64_t iter0 = ctx->n_iter;
+    bmg_trace_reset_kernel<<<(ctx->C + 127) / 128, 128, 0, ctx->stream>>>(K.ch, (int)ctx->C);
+    uint64_t i = 0;
+    while (i < chunk) {
+      uint64_t t = ctx->n_iter;
+      uint64_t next_rb = ((t / n_rao) + 1) * n_rao - 1;  // first iter >= t with (iter+1) % n_rao == 0
+      uint64_t seg = std::min<uint64_t>(chunk - i, next_rb - t + 1);
+      bmg_move_kernel<<<ctx->C, BMG_MOVE_THREADS, 0, ctx->stream>>>(K, (int)seg);
+      CK(cudaGetLastError());
+      ctx->n_iter += seg;
+      i += seg;
+      if (ctx->n_iter - 1 == next_rb) {
+        launch_scan(ctx);
+        bmg_rebuild_kernel<<<ctx->C, 1024, 0, ctx->stream>>>(K, 0);
+        CK(cudaGetLastError());
+      }
+    }
+    drain_traces(ctx, iter0, sink);
+    device_error_check(ctx);
+    done += chunk;
+  }
+  CK(cudaEventRecord(e1, ctx->stream));
+  CK(cudaEventSynchronize(e1));
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, e0, e1));
+  ctx->ms[3] = ms;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return BMG_OK;
+  API_END
+}
+
+extern "C" bmg_status bmg_scan(bmg_ctx* ctx, double* p_r, double* p_r_types)
+{
+  if (!ctx) return BMG_EINVAL;
+  API_BEGIN
+  check_ready(ctx);
+  DevConst& K = ctx->K;
+  bmg_rbprep_kernel<<<ctx->C, BMG_MOVE_THREADS, 0, ctx->stream>>>(K);
+  CK(cudaGetLastError());
+  launch_scan(ctx);
+  const size_t pc = (size_t)ctx->p * ctx->C;
+  if (p_r) CK(cudaMemcpyAsync(p_r, K.p_r, 8 * pc, cudaMemcpyDeviceToHost, ctx->stream));
+  if (p_r_types && ctx->opt.n_types > 1)
+    CK(cudaMemcpyAsync(p_r_types, K.p_r_types, 8 * pc * ctx->opt.n_types, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  device_error_check(ctx);
+  return BMG_OK;
+  API_END
+}
+
+extern "C" bmg_status bmg_get_state(bmg_ctx* ctx, uint32_t chain, bmg_chain_state* st, uint32_t* loci,
+                                    uint8_t* type_inds, uint32_t loci_cap)
+{
+  if (!ctx) return BMG_EINVAL;
+  API_BEGIN
+  check_ready(ctx);
+  if (chain >= ctx->C || !st) throw bmg_error(BMG_EINVAL, "chain index");
+  DevModel M;
+  DevChain h;
+  CK(cudaMemcpyAsync(&M, ctx->K.cur + chain, sizeof(M), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(&h, ctx->K.ch + chain, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  std::vector<uint32_t> lc(M.k);
+  std::vector<uint8_t> ti(M.k);
+  if (M.k) {
+    CK(cudaMemcpyAsync(lc.data(), M.loci, 4 * (size_t)M.k, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(ti.data(), M.type_inds, (size_t)M.k, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  st->model_size = (uint32_t)M.k;
+  st->log_likelihood = M.ll;
+  // log prior from the same tables the device uses
+  {
+    double lp = 0;
+    int ng = 0;
+    const uint32_t tw = ctx->K.tw;
+    std::vector<double> tab((size_t)22 * tw);
+    CK(cudaMemcpy(tab.data(), ctx->K.tab, 8 * tab.size(), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < 5; ++i)
+      if (ctx->K.allow_types[i]) { lp += tab[(size_t)(14 + i) * tw + M.Ns[i]]; ng += M.Ns[i]; }
+    lp += tab[(size_t)19 * tw + ng] + tab[(size_t)20 * tw + ng] - tab[(size_t)21 * tw + ng];
+    st->log_prior = lp;
+  }
+  st->sigma2 = M.sigma2;
+  st->alpha = h.alpha;
+  st->n_iter = h.n_iter;
+  st->n_accepted = h.n_accepted;
+  st->p_move_size = h.p_move_size;
+  for (int i = 0; i < M.k && (uint32_t)i < loci_cap; ++i) {
+    if (loci) loci[i] = lc[i];
+    if (type_inds) type_inds[i] = ti[i];
+  }
+  return BMG_OK;
+  API_END
+}
+
+extern "C" bmg_status bmg_get_rao(bmg_ctx* ctx, uint32_t chain, double* p_rao, double* p_rao_types)
+{
+  if (!ctx) return BMG_EINVAL;
+  API_BEGIN
+  check_ready(ctx);
+  if (chain >= ctx->C) throw bmg_error(BMG_EINVAL, "chain index");
+  const size_t p = ctx->p;
+  if (p_rao) CK(cudaMemcpyAsync(p_rao, ctx->K.p_rao + chain * p, 8 * p, cudaMemcpyDeviceToHost, ctx->stream));
+  if (p_rao_types && ctx->opt.n_types > 1)
+    CK(cudaMemcpyAsync(p_rao_types, ctx->K.p_rao_types + chain * p * ctx->opt.n_types, 8 * p * ctx->opt.n_types,
+                       cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return BMG_OK;
+  API_END
+}
+
+extern "C" bmg_status bmg_get_timings(bmg_ctx* ctx, double* ms4)
+{
+  if (!ctx || !ms4) return BMG_EINVAL;
+  for (int i = 0; i < 4; ++i) ms4[i] = ctx->ms[i];
+  return BMG_OK;
+}
+
+extern "C" bmg_status bmg_finish(bmg_ctx* ctx)
+{
+  if (!ctx) return BMG_EINVAL;
+  API_BEGIN
+  check_ready(ctx);
+  const bmg_options& o = ctx->opt;
+  const uint32_t C = ctx->C;
+  CK(cudaMemcpy(ctx->ch_h.data(), ctx->K.ch, sizeof(DevChain) * C, cudaMemcpyDeviceToHost));
+  double elapsed = ctx->t_start ? difftime(time(nullptr), ctx->t_start) : 0.0;
+  for (uint32_t c = 0; c < C; ++c) {
+    std::string b = std::string(o.basename) + std::to_string(c);
+    const DevChain& h = ctx->ch_h[c];
+    {  // src/samplerstats.hpp:92-110
+      std::ofstream f((b + "_samplerstats.txt").c_str());
+      if (!f.is_open()) throw bmg_error(BMG_EIO, "Failed to open file: " + b + "_samplerstats.txt");
+      f << "n_likelihood_updates_on_add " << h.n_lik_add << std::endl
+        << "n_likelihood_updates_on_rem " << h.n_lik_rem << std::endl
+        << "n_likelihood_computations " << h.n_lik_full + 3 << std::endl
+        << "sampling_time_in_seconds " << elapsed << std::endl
+        << "mhmove_time_in_seconds " << ctx->ms[0] / 1000.0 << std::endl
+        << "rao_time_in_seconds " << ctx->ms[1] / 1000.0 << std::endl
+        << "clock_resolution_in_seconds " << 1e-9 << std::endl
+        << "p_movesize " << h.p_move_size << std::endl;
+    }
+    if (!ctx->files.empty() && ctx->files[c].open) {
+      ctx->files[c].log << "Elapsed time: " << elapsed << " seconds." << std::endl;
+      ctx->files[c] = ChainFiles();
+    }
+    std::vector<double> rao(ctx->p), raot;
+    if (o.n_types > 1) raot.resize(ctx->p * o.n_types);
+    bmg_get_rao(ctx, c, rao.data(), o.n_types > 1 ? raot.data() : nullptr);
+    std::ofstream fr((b + "_rao.dat").c_str(), std::ios::binary);
+    if (!fr.is_open()) throw bmg_error(BMG_EIO, "Failed to open file: " + b + "_rao.dat");
+    fr.write((const char*)rao.data(), 8 * rao.size());
+    if (o.n_types > 1) {
+      std::ofstream ft((b + "_rao_types.dat").c_str(), std::ios::binary);
+      ft.write((const char*)raot.data(), 8 * raot.size());
+    }
+  }
+  ctx->files.clear();
+  {  // Prior::print (src/prior.hpp:221-243), basename of chain 0 without its index
+    std::ofstream f((std::string(o.basename) + "_prior.txt").c_str());
+    if (f.is_open()) {
+      f << "a_omega = " << ctx->g_a << std::endl
+        << "b_omega = " << ctx->g_b << std::endl
+        << "nu_sigma2 = " << o.nu_sigma2 << std::endl
+        << "s2_sigma2 = " << ctx->s2_sigma2 << std::endl
+        << "mu_alpha = " << o.mu_alpha << std::endl;
+      for (int t = 0; t < 5; ++t)
+        f << "type_" << kTypeName[t] << " = " << ctx->K.types_prior[t] << " (allowed? " << ctx->K.allow_types[t]
+          << ")" << std::endl;
+      for (int t = 0; t < 4; ++t)
+        f << "term_" << kTypeName[t] << " allowed = " << ctx->K.allow_terms[t] << std::endl
+          << "nu_tau2_" << kTypeName[t] << " = " << ctx->K.nu_tau2[t] << std::endl
+          << "s2_tau2_" << kTypeName[t] << " = " << ctx->K.s2_tau2[t] << std::endl;
+    }
+  }
+  return BMG_OK;
+  API_END
+}
+
+// data statistics the reference prints at start (src/main.cpp:58-62)
+extern "C" bmg_status bmg_get_data_stats(bmg_ctx* ctx, double* out4)
+{
+  if (!ctx || !out4) return BMG_EINVAL;
+  out4[0] = ctx->var_x;
+  out4[1] = ctx->mean_x;
+  out4[2] = ctx->var_y;
+  out4[3] = ctx->yy;
+  return BMG_OK;
+}

@@ -1,0 +1,1826 @@
+// The MCMC move kernel of libbmg: one CTA per chain.
+//
+// Warp 0 runs the reference's sampler control flow (src/sampler.cpp:551-834,
+// src/sampler.hpp:899-1769) with every lane executing the scalar code, so the
+// warp stays converged and all lanes hold the same values; lane-parallel
+// loops do the O(k) and O(k^2) linear algebra.  All eight warps join for the
+// n-wide phases (fitted values, PVE sums, alpha sufficient statistics, the
+// fixed-point residual and its limbs for the scan).  Random numbers come from
+// bmg_rng.h in the reference's draw order, so a chain reproduces the oracle's
+// trajectory for the same seed.
+//
+// FP64 is used wherever the reference uses it on the move path: the Cholesky
+// factor, its up/downdates (src/symmmatrix.cpp:144-195, src/dchex.f), the
+// marginal likelihood and the MH ratio.  Genotype products are exact integers
+// (popcounts on the 2-bit codes), and products with phenotypes or covariates
+// use fixed-point integers.
+#include <math.h>
+
+#include "common.cuh"
+
+#define TAB_ADD_A 0
+#define TAB_REM_A 1
+#define TAB_LT 2
+#define TAB_LTM1 7
+#define TAB_LS 12
+#define TAB_LSM1 13
+#define TAB_LGT 14
+#define TAB_LGA 19
+#define TAB_LGB 20
+#define TAB_LGS 21
+
+#define LOG_HALF_D -0.69314718055994528622676398299518041312694549560546875
+
+struct MoveShared {
+  uint32_t move_inds[BMG_MAX_MS + 1];
+  uint32_t move_add[BMG_MAX_MS + 1];
+  uint32_t move_rem[BMG_MAX_MS + 1];
+  long long move_map[BMG_MAX_MS + 1];
+  uint8_t move_isadd[BMG_MAX_MS + 1];
+  // dd_add flips relative to the prefix base
+  int n_pend;
+  int pend_snp[BMG_PEND_MAX];
+  int pend_pos[BMG_PEND_MAX];
+  long long pend_d[BMG_PEND_MAX];
+  // dd_rem non-zero set, in in-order position order
+  int n_rs;
+  uint32_t rs_snp[BMG_REMSET_MAX];
+  int rs_pos[BMG_REMSET_MAX];
+  double rs_w[BMG_REMSET_MAX];
+  uint8_t rs_on[BMG_REMSET_MAX];
+  // bulk phase exchange
+  long long bl[8][2];
+  double bd[8][6];
+  double bsum[6];
+  long long bsuml[2];
+  int bulk_mode;
+  int bulk_s;           // fixed-point exponent of the bulk phase
+  int bulk_nterm;       // genotype columns in the bulk phase
+  int err;
+  int iter_stop;        // stop after this iteration (RB step follows)
+  int n_done;
+  double bulk_b0;       // constant-term coefficient
+  long long bulk_b0i;
+  double bulk_e[8];     // covariate coefficients (m_e <= 8 in bulk phases)
+};
+
+// genotype columns of the bulk phase: snp, term, fixed-point coefficient
+#define BULK_MAXCOL 1024
+struct BulkCols {
+  uint32_t snp[BULK_MAXCOL];
+  int8_t term[BULK_MAXCOL];
+  long long coef[BULK_MAXCOL];
+};
+
+// ------------------------------------------------------------------ helpers
+
+struct Warp {
+  const DevConst& K;
+  int c;
+  DevChain* ch;
+  DevModel* cur;
+  DevModel* nm;
+  MoveShared& s;
+  int lane;
+  bmg_rng_t rng;
+  unsigned km;
+
+  __device__ Warp(const DevConst& k, int chain, MoveShared& sh)
+  : K(k), c(chain), ch(k.ch + chain), cur(k.cur + chain), nm(k.nm + chain), s(sh),
+    lane(threadIdx.x & 31), km(k.km)
+  {
+    rng = ch->rng;
+  }
+
+  __device__ void fail(int code)
+  {
+    if (lane == 0 && s.err == 0) s.err = code;
+    __syncwarp();
+  }
+
+  __device__ double u01() { return bmg_uniform01(&rng); }
+  __device__ double nrm() { return bmg_normal(&rng); }
+
+  /* src/rand.hpp:61-78 */
+  __device__ double sinvchi2(double s2)
+  {
+    for (int t = 0; t < 64; ++t) {
+      double g = bmg_gamma(&rng, 0.5 * K.rng_nu);
+      if (isnan(g)) { fail(BMG_DERR_RNG); return 1.0; }
+      double val = K.rng_nu * s2 / (2.0 * g);
+      if (val > 0 && isfinite(val)) return val;
+    }
+    fail(BMG_DERR_RNG);
+    return 1.0;
+  }
+  /* src/rand.hpp:85-97 */
+  __device__ double sinvchi2(double nu, double s2)
+  {
+    for (int t = 0; t < 64; ++t) {
+      double g = bmg_gamma(&rng, 0.5 * nu);
+      if (isnan(g)) { fail(BMG_DERR_RNG); return 1.0; }
+      double val = nu * s2 / (2.0 * g);
+      if (val > 0 && isfinite(val)) return val;
+    }
+    fail(BMG_DERR_RNG);
+    return 1.0;
+  }
+  /* src/utils.cpp:46-57 */
+  __device__ int sample_naive(const double* cumsum, int m)
+  {
+    double z = cumsum[m - 1];
+    double r = u01() * z;
+    for (int i = 0; i < m; ++i)
+      if (r < cumsum[i]) return i;
+    fail(BMG_DERR_NAN);
+    return m - 1;
+  }
+
+  __device__ const double* tab(int which) const { return K.tab + (size_t)which * K.tw; }
+
+  /* src/prior.hpp:144-167 from the host tables */
+  __device__ double lchange_add(const int* Ns, int nl, int type) const
+  {
+    return tab(TAB_ADD_A)[nl] + (tab(TAB_LT + type)[Ns[type]] - tab(TAB_LS)[nl]);
+  }
+  __device__ double lchange_rem(const int* Ns, int nl, int type) const
+  {
+    return tab(TAB_REM_A)[nl] + (tab(TAB_LSM1)[nl] - tab(TAB_LTM1 + type)[Ns[type]]);
+  }
+  __device__ double lchange_swi(const int* Ns, int ta, int tr) const
+  {
+    return (ta == tr) ? 0 : tab(TAB_LT + ta)[Ns[ta]] - tab(TAB_LTM1 + tr)[Ns[tr]];
+  }
+  /* src/prior.hpp:169-183 */
+  __device__ double log_model(const int* Ns) const
+  {
+    double lp = 0;
+    int ng = 0;
+    for (int i = 0; i < 5; ++i) {
+      if (K.allow_types[i]) {
+        lp += tab(TAB_LGT + i)[Ns[i]];
+        ng += Ns[i];
+      }
+    }
+    lp += tab(TAB_LGA)[ng] + tab(TAB_LGB)[ng] - tab(TAB_LGS)[ng];
+    return lp;
+  }
+  __device__ double sample_inv_tau2_prior(int type)
+  {
+    if (K.use_individual_tau2) return 1.0 / (ch->alpha2 * sinvchi2(K.nu_tau2[type], K.s2_tau2[type]));
+    return ch->inv_t2a2[type];
+  }
+
+  // dd_add weight of a SNP (fixed point) and as double
+  __device__ long long qadd_int(uint32_t snp) const
+  {
+    double pp = K.p_prop[(size_t)c * K.p + K.pos[snp]];
+    double w = fmax(pp, K.q_add_min);
+    return __double2ll_rn(w * ldexp(1.0, K.qs));
+  }
+  __device__ double qadd(uint32_t snp) const { return (double)qadd_int(snp) * ldexp(1.0, -K.qs); }
+  __device__ double qrem(uint32_t snp) const
+  {
+    double pp = K.p_prop[(size_t)c * K.p + K.pos[snp]];
+    return fmax(1.0 - pp, K.q_rem_min);
+  }
+  // q_add_types and their cumulative sums (src/sampler.cpp:526-544)
+  __device__ void qtypes(uint32_t snp, double* qa, double* qcum) const
+  {
+    const double* pt = K.p_prop_types + ((size_t)c * K.p + snp) * K.n_types;
+    for (unsigned t = 0; t < K.n_types; ++t) {
+      qa[t] = fmax(pt[t], K.q_add_min);
+      qcum[t] = (t == 0) ? qa[t] : qcum[t - 1] + qa[t];
+    }
+  }
+
+  // ------------------------------------------------------- model arrays
+  __device__ double& XX(DevModel* M, int r, int col) const { return M->xx[(size_t)col * km + r]; }
+  __device__ double& L(DevModel* M, int r, int col) const { return M->l[(size_t)col * km + r]; }
+
+  /* src/model.hpp:115-162: copy the active parts of a model */
+  __device__ void copy_model(DevModel* d, const DevModel* src)
+  {
+    int xc = src->xcols, ll = src->llen;
+    for (int col = 0; col < xc; ++col)
+      for (int r = lane; r <= col; r += 32) d->xx[(size_t)col * km + r] = src->xx[(size_t)col * km + r];
+    for (int col = 0; col < ll; ++col)
+      for (int r = lane; r <= col; r += 32) d->l[(size_t)col * km + r] = src->l[(size_t)col * km + r];
+    for (int i = lane; i < xc; i += 32) {
+      d->xy[i] = src->xy[i];
+      d->inv[i] = src->inv[i];
+      d->xc_snp[i] = src->xc_snp[i];
+      d->xc_type[i] = src->xc_type[i];
+    }
+    int vb = max(src->vlen, src->blen);
+    for (int i = lane; i < vb; i += 32) {
+      d->v[i] = src->v[i];
+      d->beta[i] = src->beta[i];
+      d->mu_beta[i] = src->mu_beta[i];
+    }
+    for (int i = lane; i < src->k; i += 32) {
+      d->loci[i] = src->loci[i];
+      d->type_inds[i] = src->type_inds[i];
+      d->x_ind1[i] = src->x_ind1[i];
+      d->x_ind2[i] = src->x_ind2[i];
+    }
+    if (lane == 0) {
+      d->k = src->k;
+      d->xcols = src->xcols;
+      d->llen = src->llen;
+      d->vlen = src->vlen;
+      d->blen = src->blen;
+      for (int i = 0; i < 5; ++i) d->Ns[i] = src->Ns[i];
+      d->mu_beta_computed = src->mu_beta_computed;
+      d->sigma2 = src->sigma2;
+      d->syx = src->syx;
+      d->ldq = src->ldq;
+      d->ldqx = src->ldqx;
+      d->ll = src->ll;
+    }
+    __syncwarp();
+  }
+
+  // ------------------------------------------------------- linear algebra
+  // solve U' x = b in place (forward substitution), U = first len of L
+  __device__ void trsv_T(const DevModel* M, double* x, int len)
+  {
+    for (int j = 0; j < len; ++j) {
+      double part = 0.0;
+      for (int i = lane; i < j; i += 32) part += M->l[(size_t)j * km + i] * x[i];
+      part = warp_sum_d(part);
+      double xj = (x[j] - part) / M->l[(size_t)j * km + j];
+      __syncwarp();
+      if (lane == 0) x[j] = xj;
+      __syncwarp();
+    }
+  }
+  // solve U x = b in place (back substitution, column sweep)
+  __device__ void trsv_N(const DevModel* M, double* x, int len)
+  {
+    for (int j = len - 1; j >= 0; --j) {
+      double xj = x[j];
+      __syncwarp();
+      if (xj != 0.0) {
+        xj = xj / M->l[(size_t)j * km + j];
+        for (int i = lane; i < j; i += 32) x[i] -= xj * M->l[(size_t)j * km + i];
+        if (lane == 0) x[j] = xj;
+      }
+      __syncwarp();
+    }
+  }
+  __device__ double dot(const double* a, const double* b, int len)
+  {
+    double part = 0.0;
+    for (int i = lane; i < len; i += 32) part += a[i] * b[i];
+    return warp_sum_d(part);
+  }
+
+  /* src/model.hpp:199-237, src/model.hpp:558-576 (Cholesky: LAPACK dpotf2, 'U') */
+  __device__ void compute_log_likelihood(DevModel* M)
+  {
+    int m = M->xcols;
+    if (m < 1) {
+      if (lane == 0) M->ll = NAN;
+      __syncwarp();
+      return;
+    }
+    if (lane == 0) ch->n_lik_full++;
+    for (int col = 0; col < m; ++col)
+      for (int r = lane; r <= col; r += 32) M->l[(size_t)col * km + r] = M->xx[(size_t)col * km + r];
+    __syncwarp();
+    double log_sum_2 = 0;
+    if (lane == 0) M->l[0] += M->inv[0];
+    for (int i = 1; i < m; ++i) {
+      if (lane == 0) M->l[(size_t)i * km + i] += M->inv[i];
+      log_sum_2 += log(M->inv[i]);
+    }
+    __syncwarp();
+    double ldq = 0.5 * log_sum_2;
+    bool ok = true;
+    for (int j = 0; j < m && ok; ++j) {
+      double ajj = M->l[(size_t)j * km + j] - dot(&M->l[(size_t)j * km], &M->l[(size_t)j * km], j);
+      if (ajj <= 0.0 || isnan(ajj)) { ok = false; break; }
+      ajj = sqrt(ajj);
+      __syncwarp();
+      if (lane == 0) M->l[(size_t)j * km + j] = ajj;
+      for (int cc = j + 1 + lane; cc < m; cc += 32) {
+        double t = M->l[(size_t)cc * km + j];
+        for (int q = 0; q < j; ++q) t -= M->l[(size_t)j * km + q] * M->l[(size_t)cc * km + q];
+        M->l[(size_t)cc * km + j] = t / ajj;
+      }
+      __syncwarp();
+    }
+    if (lane == 0) {
+      M->llen = m;
+      M->ldq = ldq;
+    }
+    __syncwarp();
+    if (!ok) {
+      if (lane == 0) {
+        M->ll = -INFINITY;
+        M->syx = INFINITY;
+        M->mu_beta_computed = 0;
+      }
+      __syncwarp();
+      return;
+    }
+    for (int i = lane; i < m; i += 32) M->v[i] = M->xy[i];
+    __syncwarp();
+    trsv_T(M, M->v, m);
+    double vv = dot(M->v, M->v, m);
+    double ldqx = 0;
+    for (int i = 0; i < m; ++i) ldqx += log(M->l[(size_t)i * km + i]);
+    double syx = K.nus2_plus_yy - vv;
+    if (lane == 0) {
+      M->vlen = m;
+      M->syx = syx;
+      M->ldqx = ldqx;
+      M->ll = ldq - ldqx + K.minus_n_plus_nu_2 * log(syx);
+      M->mu_beta_computed = 0;
+    }
+    __syncwarp();
+  }
+
+  // ------------------------------------------------- genotype products
+  // sum_i x_t(g_i) * Y_i with a fixed-point vector Y (length n)
+  __device__ long long geno_dot_fixed(uint32_t snp, int term, const int64_t* Y)
+  {
+    const uint8_t* row = K.geno + (size_t)snp * K.gs;
+    long long acc;
+    // lanes take individuals lane, lane+32, ...: each reads its own 2 bits
+    acc = 0;
+    for (uint64_t i = lane; i < K.n; i += 32) {
+      int code = (row[i >> 2] >> ((i & 3) * 2)) & 3;
+      int v = term_value(code, term);
+      if (v == 1) acc += Y[i];
+      else if (v == 2) acc += 2 * Y[i];
+    }
+    return warp_sum_ll(acc);
+  }
+  // exact sum_i x_t(g_a,i) x_u(g_b,i) from the 2-bit codes
+  __device__ long long geno_cross(uint32_t a, int t, uint32_t b, int u)
+  {
+    if (a == b) return term_cross_same(K.cnt, a, t, u);
+    const uint64_t* ra = (const uint64_t*)(K.geno + (size_t)a * K.gs);
+    const uint64_t* rb = (const uint64_t*)(K.geno + (size_t)b * K.gs);
+    unsigned nw64 = K.gs / 8;
+    long long hh = 0, hr = 0, rh = 0, rr = 0;
+    const uint64_t m5 = 0x5555555555555555ull;
+    for (unsigned w = lane; w < nw64; w += 32) {
+      uint64_t x = ra[w], y = rb[w];
+      uint64_t xh = (x >> 1) & m5, xl = x & m5, yh = (y >> 1) & m5, yl = y & m5;
+      uint64_t Hx = xh & ~xl, Rx = xh & xl, Hy = yh & ~yl, Ry = yh & yl;
+      hh += __popcll(Hx & Hy);
+      hr += __popcll(Hx & Ry);
+      rh += __popcll(Rx & Hy);
+      rr += __popcll(Rx & Ry);
+    }
+    long long v = (long long)coefH(t) * coefH(u) * hh + (long long)coefH(t) * coefR(u) * hr +
+                  (long long)coefR(t) * coefH(u) * rh + (long long)coefR(t) * coefR(u) * rr;
+    return warp_sum_ll(v);
+  }
+  // X' column entry between model column r and a new genotype column (snp, term)
+  __device__ double cross_col(const DevModel* M, int r, uint32_t snp, int term)
+  {
+    if (r < (int)K.m_e) {
+      if (r == 0) return (double)term_sum(K.cnt, snp, term);
+      long long acc = geno_dot_fixed(snp, term, K.eint + (size_t)r * K.n);
+      return (double)acc * ldexp(1.0, -K.se[r]);
+    }
+    return (double)geno_cross(M->xc_snp[r], M->xc_type[r], snp, term);
+  }
+
+  // --------------------------------------------------------- model updates
+  /* src/model.hpp:432-506 with src/symmmatrix.cpp:144-164 */
+  __device__ void upd_add(DevModel* M, uint32_t snp, int mi, int term, bool is2, double invv, bool update)
+  {
+    int col = M->xcols;
+    if (lane == 0) {
+      if (is2) M->x_ind2[mi] = col;
+      else { M->x_ind1[mi] = col; M->x_ind2[mi] = 0; }
+      M->xc_snp[col] = snp;
+      M->xc_type[col] = term;
+      M->xcols = col + 1;
+      M->inv[col] = invv;
+    }
+    long long xyi = geno_dot_fixed(snp, term, K.yint);
+    double xyc = (double)xyi * ldexp(1.0, -K.sy);
+    __syncwarp();
+    if (lane == 0) M->xy[col] = xyc;
+    double* xxcol = &M->xx[(size_t)col * km];
+    for (int r = 0; r <= col; ++r) {
+      double v = (r == col) ? (double)term_cross_same(K.cnt, snp, term, term) : cross_col(M, r, snp, term);
+      if (lane == 0) xxcol[r] = v;
+    }
+    __syncwarp();
+    if (!update) {
+      if (lane == 0) { M->llen = col + 1; M->vlen = col + 1; }
+      __syncwarp();
+      return;
+    }
+    if (lane == 0) ch->n_lik_add++;
+    double* lcol = &M->l[(size_t)col * km];
+    for (int r = lane; r <= col; r += 32) lcol[r] = xxcol[r];
+    __syncwarp();
+    trsv_T(M, lcol, col);
+    double lmm2 = xxcol[col] + invv - dot(lcol, lcol, col);
+    if (lane == 0) M->llen = col + 1;
+    __syncwarp();
+    if (lmm2 <= 0) {
+      if (lane == 0) {
+        M->ll = -INFINITY;
+        M->syx = INFINITY;
+        M->mu_beta_computed = 0;
+        M->vlen = col + 1;
+      }
+      __syncwarp();
+      return;
+    }
+    double lcc = sqrt(lmm2);
+    double vm2 = M->xy[col] - dot(lcol, M->v, col);
+    double vc = vm2 / lcc;
+    double syx = M->syx - vc * vc;
+    double ldq = M->ldq + 0.5 * log(invv);
+    double ldqx = M->ldqx + log(lcc);
+    __syncwarp();
+    if (lane == 0) {
+      lcol[col] = lcc;
+      M->vlen = col + 1;
+      M->v[col] = vc;
+      M->syx = syx;
+      M->ldq = ldq;
+      M->ldqx = ldqx;
+      M->ll = ldq - ldqx + K.minus_n_plus_nu_2 * log(syx);
+    }
+    __syncwarp();
+  }
+
+  /* src/model.hpp:239-268 */
+  __device__ void add_term(DevModel* M, uint32_t snp, int t_ind, const double* itv)
+  {
+    int type = K.types[t_ind];
+    bool ah = (type == 4);
+    int mi = M->k;
+    if (M->xcols + 1 + (ah ? 1 : 0) > (int)km) { fail(BMG_DERR_CAPACITY); return; }
+    if (lane == 0) {
+      M->loci[mi] = snp;
+      M->Ns[type]++;
+      M->type_inds[mi] = (uint8_t)t_ind;
+      M->k = mi + 1;
+      M->mu_beta_computed = 0;
+    }
+    __syncwarp();
+    if (ah) {
+      upd_add(M, snp, mi, 0, false, itv[0], true);
+      if (isfinite(M->syx)) upd_add(M, snp, mi, 1, true, itv[1], true);
+    } else {
+      upd_add(M, snp, mi, type, false, itv[0], true);
+    }
+  }
+
+  // remove element `at` of an array of length len (warp)
+  template <class T>
+  __device__ void erase(T* a, int len, int at)
+  {
+    for (int base = at; base < len - 1; base += 32) {
+      int i = base + lane;
+      T v = (i < len - 1) ? a[i + 1] : T();
+      __syncwarp();
+      if (i < len - 1) a[i] = v;
+      __syncwarp();
+    }
+  }
+
+  /* src/dchex.f:130-220 (job 2) on L with k = x_ind + 1, l = p = order */
+  __device__ void dchex_left(DevModel* M, int x_ind, int order, double* cs, double* sn)
+  {
+    // one lane: the rotation chain is sequential
+    if (lane == 0) {
+      const int k = x_ind + 1, l = order, p = order;
+      const int km1 = k - 1, lmk = l - k;
+      double* r = M->l;
+#define R_(i, j) r[(size_t)((j) - 1) * km + (size_t)((i) - 1)]
+      for (int i = 1; i <= k; ++i) sn[lmk + i - 1] = R_(i, k);
+      for (int j = k; j <= l - 1; ++j) {
+        for (int i = 1; i <= j; ++i) R_(i, j) = R_(i, j + 1);
+        sn[j - km1 - 1] = R_(j + 1, j + 1);
+      }
+      for (int i = 1; i <= k; ++i) R_(i, l) = sn[lmk + i - 1];
+      for (int i = k + 1; i <= l; ++i) R_(i, l) = 0.0;
+      for (int j = k; j <= p; ++j) {
+        if (j != k) {
+          int iu = min(j - 1, l - 1);
+          for (int i = k; i <= iu; ++i) {
+            int ii = i - k + 1;
+            double t = cs[ii - 1] * R_(i, j) + sn[ii - 1] * R_(i + 1, j);
+            R_(i + 1, j) = cs[ii - 1] * R_(i + 1, j) - sn[ii - 1] * R_(i, j);
+            R_(i, j) = t;
+          }
+        }
+        if (j < l) {
+          int jj = j - k + 1;
+          // drotg(r(j,j), s(jj)) -> c(jj), s(jj), netlib semantics
+          double sa = R_(j, j), sb = sn[jj - 1];
+          double roe = (fabs(sa) > fabs(sb)) ? sa : sb;
+          double scale = fabs(sa) + fabs(sb);
+          double rr, cc, ss;
+          if (scale == 0.0) {
+            cc = 1.0; ss = 0.0; rr = 0.0;
+          } else {
+            double ta = sa / scale, tb = sb / scale;
+            rr = scale * sqrt(ta * ta + tb * tb);
+            if (roe < 0.0) rr = -rr;
+            cc = sa / rr;
+            ss = sb / rr;
+          }
+          R_(j, j) = rr;
+          cs[jj - 1] = cc;
+          sn[jj - 1] = ss;
+        }
+      }
+#undef R_
+    }
+    __syncwarp();
+  }
+
+  /* src/model.hpp:508-556 with src/symmmatrix.cpp:126-195 */
+  __device__ void upd_rem(DevModel* M, int x_ind, double* cs, double* sn)
+  {
+    int len = M->xcols;
+    double invv = M->inv[x_ind];
+    __syncwarp();
+    erase(M->xc_snp, len, x_ind);
+    erase(M->xc_type, len, x_ind);
+    erase(M->xy, len, x_ind);
+    erase(M->inv, len, x_ind);
+    // xx.remove_colrow
+    for (int i = x_ind; i < len - 1; ++i) {
+      for (int j = lane; j <= i; j += 32) {
+        double v = (j < x_ind) ? M->xx[(size_t)(i + 1) * km + j] : M->xx[(size_t)(i + 1) * km + j + 1];
+        M->xx[(size_t)i * km + j] = v;
+      }
+      __syncwarp();
+    }
+    int xc = len - 1;
+    if (lane == 0) { M->xcols = xc; ch->n_lik_rem++; }
+    __syncwarp();
+    if (x_ind == xc) {
+      double lxx = M->l[(size_t)x_ind * km + x_ind];
+      double vx = M->v[x_ind];
+      double ldqx = M->ldqx - log(lxx);
+      double syx = M->syx + vx * vx;
+      __syncwarp();
+      if (lane == 0) {
+        M->ldqx = ldqx;
+        M->syx = syx;
+        M->llen = xc;
+        M->vlen = xc;
+      }
+      __syncwarp();
+    } else {
+      int order = M->llen;
+      dchex_left(M, x_ind, order, cs, sn);
+      int nl = order - 1;
+      for (int i = x_ind; i < nl; ++i) {
+        if (M->l[(size_t)i * km + i] < 0) {
+          for (int j = i + lane; j < nl; j += 32) M->l[(size_t)j * km + i] *= -1;
+        }
+        __syncwarp();
+      }
+      for (int i = lane; i < xc; i += 32) M->v[i] = M->xy[i];
+      __syncwarp();
+      trsv_T(M, M->v, nl);
+      double ldqx = 0;
+      for (int i = 0; i < nl; ++i) ldqx += log(M->l[(size_t)i * km + i]);
+      double syx = K.nus2_plus_yy - dot(M->v, M->v, xc);
+      if (lane == 0) {
+        M->llen = nl;
+        M->vlen = xc;
+        M->ldqx = ldqx;
+        M->syx = syx;
+      }
+      __syncwarp();
+    }
+    double ldq = M->ldq - 0.5 * log(invv);
+    double ll = ldq - M->ldqx + K.minus_n_plus_nu_2 * log(M->syx);
+    __syncwarp();
+    if (lane == 0) {
+      M->ldq = ldq;
+      M->ll = ll;
+    }
+    __syncwarp();
+  }
+
+  /* src/model.hpp:270-312 */
+  __device__ void remove_term(DevModel* M, int mi, double* cs, double* sn)
+  {
+    int type = K.types[M->type_inds[mi]];
+    int xi1 = M->x_ind1[mi], xi2 = M->x_ind2[mi];
+    int k = M->k;
+    __syncwarp();
+    if (lane == 0) M->Ns[type]--;
+    erase(M->loci, k, mi);
+    erase(M->type_inds, k, mi);
+    erase(M->x_ind1, k, mi);
+    erase(M->x_ind2, k, mi);
+    int xmove = (type == 4) ? 2 : 1;
+    for (int i = mi + lane; i < k - 1; i += 32) {
+      M->x_ind1[i] -= xmove;
+      M->x_ind2[i] -= xmove;
+    }
+    if (lane == 0) M->k = k - 1;
+    __syncwarp();
+    if (type == 4) {
+      if (xi1 > xi2) { upd_rem(M, xi1, cs, sn); upd_rem(M, xi2, cs, sn); }
+      else { upd_rem(M, xi2, cs, sn); upd_rem(M, xi1, cs, sn); }
+    } else {
+      upd_rem(M, xi1, cs, sn);
+    }
+    if (lane == 0) M->mu_beta_computed = 0;
+    __syncwarp();
+  }
+
+  // model index of a SNP in a model (linear search; -1 if absent)
+  __device__ int find_locus(const DevModel* M, uint32_t snp)
+  {
+    int found = -1;
+    for (int base = 0; base < M->k; base += 32) {
+      int i = base + lane;
+      bool hit = (i < M->k) && (M->loci[i] == snp);
+      unsigned b = __ballot_sync(FULL_MASK, hit);
+      if (b) { found = base + __ffs(b) - 1; break; }
+    }
+    return found;
+  }
+
+  /* src/model.hpp:314-342, src/rand.hpp:144-168 */
+  __device__ void sample_beta_sigma2(DevModel* M)
+  {
+    double s2 = sinvchi2(M->syx / K.n_plus_nu);
+    int len = M->vlen;
+    if (!M->mu_beta_computed) {
+      for (int i = lane; i < len; i += 32) M->mu_beta[i] = M->v[i];
+      __syncwarp();
+      trsv_N(M, M->mu_beta, M->llen);
+      if (lane == 0) M->mu_beta_computed = 1;
+    }
+    // the normals are drawn in order by every lane; lane i keeps draw i
+    for (int base = 0; base < len; base += 32) {
+      double z = 0;
+      for (int i = 0; i < 32 && base + i < len; ++i) {
+        double d = nrm();
+        if (i == lane) z = d;
+      }
+      if (base + lane < len) M->beta[base + lane] = z;
+    }
+    __syncwarp();
+    trsv_N(M, M->beta, M->llen);
+    double sc = sqrt(s2);
+    for (int i = lane; i < len; i += 32) M->beta[i] = sc * M->beta[i] + M->mu_beta[i];
+    if (lane == 0) {
+      M->sigma2 = s2;
+      M->blen = len;
+    }
+    __syncwarp();
+  }
+
+  /* src/prior.cpp:71-114 */
+  __device__ void sample_tau2(DevModel* M)
+  {
+    double a2s2 = ch->alpha2 * M->sigma2;
+    int me = K.m_e, bl = M->blen;
+    if (K.use_individual_tau2) {
+      for (int i = me; i < bl; ++i) {
+        int t = M->xc_type[i];
+        double nu = K.nu_tau2[t] + 1.0;
+        double b = M->beta[i];
+        double s2 = (K.nus2_tau2[t] + b * b / a2s2) / nu;
+        double v = 1.0 / (ch->alpha2 * sinvchi2(nu, s2));
+        __syncwarp();
+        if (lane == 0) M->inv[i] = v;
+      }
+    } else {
+      double b2s[4] = {0, 0, 0, 0};
+      int mt[4] = {0, 0, 0, 0};
+      for (int i = me; i < bl; ++i) {
+        int t = M->xc_type[i];
+        b2s[t] += M->beta[i] * M->beta[i];
+        ++mt[t];
+      }
+      double it[4];
+      for (int t = 0; t < 4; ++t) {
+        it[t] = ch->inv_t2a2[t];
+        if (!K.allow_terms[t]) continue;
+        double nu = K.nu_tau2[t] + mt[t];
+        double s2 = (K.nus2_tau2[t] + b2s[t] / a2s2) / nu;
+        it[t] = 1.0 / (ch->alpha2 * sinvchi2(nu, s2));
+      }
+      __syncwarp();
+      if (lane == 0)
+        for (int t = 0; t < 4; ++t) ch->inv_t2a2[t] = it[t];
+      for (int i = me + lane; i < bl; i += 32) M->inv[i] = it[M->xc_type[i]];
+    }
+    if (lane == 0) M->mu_beta_computed = 0;
+    __syncwarp();
+  }
+
+  /* src/prior.cpp:116-141 */
+  __device__ void set_alpha(double val, DevModel* M)
+  {
+    double old2 = ch->alpha2;
+    double a2 = val * val;
+    int me = K.m_e, bl = M->blen;
+    __syncwarp();
+    if (K.use_individual_tau2) {
+      for (int i = me + lane; i < bl; i += 32) M->inv[i] = M->inv[i] * old2 / a2;
+    } else {
+      double it[4];
+      for (int t = 0; t < 4; ++t) it[t] = K.allow_terms[t] ? ch->inv_t2a2[t] * old2 / a2 : ch->inv_t2a2[t];
+      __syncwarp();
+      if (lane == 0)
+        for (int t = 0; t < 4; ++t) ch->inv_t2a2[t] = it[t];
+      for (int i = me + lane; i < bl; i += 32) M->inv[i] = it[M->xc_type[i]];
+    }
+    if (lane == 0) { ch->alpha = val; ch->alpha2 = a2; }
+    __syncwarp();
+  }
+
+  /* src/prior.cpp:30-69; xbxb and ebxb come from the bulk phase */
+  __device__ double sample_alpha(DevModel* M, double xbxb, double ebxb)
+  {
+    int nterms = M->blen - (int)K.m_e;
+    double a = ch->alpha;
+    for (int t = 0; t < 64; ++t) {
+      if (nterms > 0) {
+        if ((a <= 0.0) || log(u01()) <= -2.0 * K.mu_alpha * a) a = -a;
+        double as2 = a * M->sigma2;
+        double var = 1.0 / (1.0 + xbxb / (a * as2));
+        double mu = var * (K.mu_alpha - ebxb / as2);
+        a = sqrt(var) * nrm() + mu;
+      } else {
+        a = nrm() + K.mu_alpha;
+      }
+      if (!(a == 0 || a * a == 0)) break;
+    }
+    if (lane == 0) M->mu_beta_computed = 0;
+    __syncwarp();
+    return a;
+  }
+
+  // --------------------------------------------------------- proposals
+  __device__ bool pend_find(uint32_t snp, int* at) const
+  {
+    int found = -1;
+    for (int base = 0; base < s.n_pend; base += 32) {
+      int i = base + lane;
+      bool hit = (i < s.n_pend) && (s.pend_snp[i] == (int)snp);
+      unsigned b = __ballot_sync(FULL_MASK, hit);
+      if (b) { found = base + __ffs(b) - 1; break; }
+    }
+    *at = found;
+    return found >= 0;
+  }
+  __device__ bool base_zero(uint32_t snp) const
+  {
+    return (K.basebits[(size_t)c * ((K.p + 31) / 32) + (snp >> 5)] >> (snp & 31)) & 1u;
+  }
+  // dd_add zero state toggles (src/discrete_distribution.hpp:156-199)
+  __device__ void add_set_zero(uint32_t snp, bool zero)
+  {
+    int at;
+    bool in_list = pend_find(snp, &at);
+    bool zeroed = base_zero(snp) != in_list;
+    if (zeroed == zero) return;
+    if (in_list) {
+      int last = s.n_pend - 1;
+      __syncwarp();
+      if (lane == 0) {
+        s.pend_snp[at] = s.pend_snp[last];
+        s.pend_pos[at] = s.pend_pos[last];
+        s.pend_d[at] = s.pend_d[last];
+        s.n_pend = last;
+      }
+    } else {
+      if (s.n_pend >= BMG_PEND_MAX) { fail(BMG_DERR_PEND); return; }
+      long long w = qadd_int(snp);
+      __syncwarp();
+      if (lane == 0) {
+        int i = s.n_pend;
+        s.pend_snp[i] = (int)snp;
+        s.pend_pos[i] = K.pos[snp];
+        s.pend_d[i] = base_zero(snp) ? w : -w;
+        s.n_pend = i + 1;
+      }
+    }
+    __syncwarp();
+  }
+  __device__ long long add_total_int()
+  {
+    long long t = 0;
+    for (int i = lane; i < s.n_pend; i += 32) t += s.pend_d[i];
+    return ch->cadd_total + warp_sum_ll(t);
+  }
+  __device__ double add_total() { return (double)add_total_int() * ldexp(1.0, -K.qs); }
+
+  // C'(q): weight of in-order positions < q after the pending flips
+  __device__ long long cum_at(long long q) const
+  {
+    long long v = K.cadd[(size_t)c * (K.p + 1) + q];
+    for (int i = 0; i < s.n_pend; ++i)
+      if (s.pend_pos[i] < q) v += s.pend_d[i];
+    return v;
+  }
+  /* src/discrete_distribution.hpp:125-153 on the in-order prefix */
+  __device__ uint32_t add_sample()
+  {
+    long long totali = add_total_int();
+    double total = (double)totali * ldexp(1.0, -K.qs);
+    double r = u01() * total;
+    double scale = ldexp(1.0, -K.qs);
+    long long lo = 0, hi = (long long)K.p;
+    for (int it = 0; it < 16 && hi - lo > 1; ++it) {
+      long long span = hi - lo;
+      long long step = (span + 31) / 32;
+      long long q = lo + (long long)lane * step;
+      bool ok = false;
+      if (q < hi) ok = ((double)cum_at(q) * scale) <= r;
+      unsigned b = __ballot_sync(FULL_MASK, ok);
+      int last = 31 - __clz(b);  // lane 0 always satisfies (C'(lo) <= r)
+      lo = lo + (long long)last * step;
+      hi = min(hi, lo + step);
+    }
+    // guard against rounding at the top: step back to a position with weight
+    long long q = lo;
+    for (int t = 0; t < 64 && q > 0; ++t) {
+      long long w = cum_at(q + 1) - cum_at(q);
+      if (w > 0) break;
+      --q;
+    }
+    return (uint32_t)K.inv[q];
+  }
+
+  // dd_rem set (src/discrete_distribution.hpp semantics on the few non-zero SNPs)
+  __device__ void rs_build_from(const DevModel* M)
+  {
+    int k = M->k;
+    if (k > BMG_REMSET_MAX - 2 * BMG_MAX_MS) { fail(BMG_DERR_REMSET); return; }
+    // rank by in-order position (positions are distinct)
+    for (int i = lane; i < k; i += 32) {
+      uint32_t si = M->loci[i];
+      int pi = K.pos[si];
+      int rank = 0;
+      for (int j = 0; j < k; ++j) rank += (K.pos[M->loci[j]] < pi);
+      s.rs_snp[rank] = si;
+      s.rs_pos[rank] = pi;
+      s.rs_w[rank] = qrem(si);
+      s.rs_on[rank] = 1;
+    }
+    if (lane == 0) s.n_rs = k;
+    __syncwarp();
+  }
+  __device__ void rs_set(uint32_t snp, bool on)
+  {
+    int n = s.n_rs;
+    int found = -1;
+    for (int base = 0; base < n; base += 32) {
+      int i = base + lane;
+      bool hit = (i < n) && (s.rs_snp[i] == snp);
+      unsigned b = __ballot_sync(FULL_MASK, hit);
+      if (b) { found = base + __ffs(b) - 1; break; }
+    }
+    if (found >= 0) {
+      __syncwarp();
+      if (lane == 0) s.rs_on[found] = on ? 1 : 0;
+      __syncwarp();
+      return;
+    }
+    if (!on) return;
+    if (n >= BMG_REMSET_MAX) { fail(BMG_DERR_REMSET); return; }
+    int p = K.pos[snp];
+    double w = qrem(snp);
+    __syncwarp();
+    if (lane == 0) {
+      int i = n;
+      while (i > 0 && s.rs_pos[i - 1] > p) {
+        s.rs_snp[i] = s.rs_snp[i - 1];
+        s.rs_pos[i] = s.rs_pos[i - 1];
+        s.rs_w[i] = s.rs_w[i - 1];
+        s.rs_on[i] = s.rs_on[i - 1];
+        --i;
+      }
+      s.rs_snp[i] = snp;
+      s.rs_pos[i] = p;
+      s.rs_w[i] = w;
+      s.rs_on[i] = 1;
+      s.n_rs = n + 1;
+    }
+    __syncwarp();
+  }
+  __device__ double rs_total()
+  {
+    double t = 0;
+    for (int i = 0; i < s.n_rs; ++i)
+      if (s.rs_on[i]) t += s.rs_w[i];
+    return t;
+  }
+  __device__ uint32_t rs_sample()
+  {
+    double total = rs_total();
+    double r = u01() * total;
+    double acc = 0;
+    int last = -1;
+    for (int i = 0; i < s.n_rs; ++i) {
+      if (!s.rs_on[i]) continue;
+      last = i;
+      acc += s.rs_w[i];
+      if (r < acc) return s.rs_snp[i];
+    }
+    return last >= 0 ? s.rs_snp[last] : 0;
+  }
+
+  // ------------------------------------------------------------ moves
+  __device__ void prepare_add(uint32_t snp, int type, double* itv, bool missing_draw)
+  {
+    (void)snp; (void)missing_draw;  // no missing genotypes on the device path
+    if (type == 4) {
+      itv[0] = sample_inv_tau2_prior(0);
+      itv[1] = sample_inv_tau2_prior(1);
+    } else {
+      itv[0] = sample_inv_tau2_prior(type);
+    }
+  }
+
+  // commit the proposed model as the current one (Model::operator=)
+  __device__ void accept_model()
+  {
+    // membership map of the current model: clear old, set new
+    int32_t* mi = K.model_inds + (size_t)c * K.p;
+    uint32_t* ib = K.inbits + (size_t)c * ((K.p + 31) / 32);
+    for (int i = lane; i < cur->k; i += 32) {
+      uint32_t sn = cur->loci[i];
+      mi[sn] = -1;
+      atomicAnd(&ib[sn >> 5], ~(1u << (sn & 31)));
+    }
+    __syncwarp();
+    for (int i = lane; i < nm->k; i += 32) {
+      uint32_t sn = nm->loci[i];
+      mi[sn] = i;
+      atomicOr(&ib[sn >> 5], 1u << (sn & 31));
+    }
+    __syncwarp();
+    copy_model(cur, nm);
+  }
+
+  /* src/sampler.hpp:1126-1165 */
+  __device__ int prepare_addrem(double& lqf, int ms)
+  {
+    long long max_adds = (long long)K.p - cur->k, max_rems = cur->k;
+    int nrem = 0;
+    for (int i = 0; i < ms; ++i) {
+      bool add;
+      if (max_rems == 0) add = true;
+      else if (max_adds == 0) add = false;
+      else { lqf += LOG_HALF_D; add = (u01() < 0.5); }
+      uint32_t ind;
+      if (add) {
+        --max_adds;
+        double tot = add_total();
+        ind = add_sample();
+        lqf += log(qadd(ind)) - log(tot);
+        add_set_zero(ind, true);
+        if (lane == 0) { s.move_isadd[i] = 1; s.move_inds[i] = ind; s.move_map[i] = ind; }
+      } else {
+        ++nrem;
+        --max_rems;
+        double tot = rs_total();
+        ind = rs_sample();
+        lqf += log(qrem(ind)) - log(tot);
+        rs_set(ind, false);
+        if (lane == 0) { s.move_isadd[i] = 0; s.move_inds[i] = ind; s.move_map[i] = -1; }
+      }
+      __syncwarp();
+    }
+    return nrem;
+  }
+  /* src/sampler.hpp:1204-1268 */
+  __device__ void do_addrem(double& lqf, double& lqb, double& lmpc, int ms, double* cs, double* sn)
+  {
+    int last_map = ms - 1;
+    for (int i = 0; i < ms; ++i) {
+      if (s.move_isadd[i]) continue;
+      uint32_t ind = s.move_inds[i];
+      add_set_zero(ind, false);
+      while (s.move_map[last_map] >= 0) --last_map;
+      __syncwarp();
+      if (lane == 0) s.move_map[last_map] = ind;
+      __syncwarp();
+      int mi = find_locus(nm, ind);
+      int t_ind = nm->type_inds[mi];
+      int type = K.types[t_ind];
+      lmpc += lchange_rem(nm->Ns, nm->k, type);
+      if (K.n_types > 1) {
+        double qa[5], qc[5];
+        qtypes(ind, qa, qc);
+        lqb += log(qa[t_ind] / qc[K.n_types - 1]);
+      }
+      remove_term(nm, mi, cs, sn);
+    }
+    double itv[2];
+    for (int i = 0; i < ms; ++i) {
+      if (!s.move_isadd[i]) continue;
+      uint32_t ind = s.move_inds[i];
+      rs_set(ind, true);
+      int t_ind = 0;
+      double qa[5], qc[5];
+      if (K.n_types > 1) {
+        qtypes(ind, qa, qc);
+        t_ind = sample_naive(qc, K.n_types);
+      }
+      int type = K.types[t_ind];
+      lmpc += lchange_add(nm->Ns, nm->k, type);
+      if (K.n_types > 1) lqf += log(qa[t_ind] / qc[K.n_types - 1]);
+      prepare_add(ind, type, itv, true);
+      add_term(nm, ind, t_ind, itv);
+    }
+  }
+  /* src/sampler.hpp:1168-1202 */
+  __device__ void backward_prepare_addrem(double& lqb, int ms)
+  {
+    long long max_adds = (long long)K.p - nm->k, max_rems = nm->k;
+    double w_add = add_total(), w_rem = rs_total();
+    int last_rem = ms - 1;
+    for (int i = 0; i < ms; ++i) {
+      if (max_adds > 0 && max_rems > 0) lqb += LOG_HALF_D;
+      uint32_t ind;
+      if (s.move_isadd[i]) {
+        --max_rems;
+        while (!s.move_isadd[last_rem]) --last_rem;
+        ind = (uint32_t)s.move_map[last_rem];
+        --last_rem;
+        double q = qrem(ind);
+        lqb += log(q) - log(w_rem);
+        w_rem -= q;
+      } else {
+        --max_adds;
+        ind = (uint32_t)s.move_map[i];
+        double q = qadd(ind);
+        lqb += log(q) - log(w_add);
+        w_add -= q;
+      }
+    }
+  }
+  /* src/sampler.hpp:899-1123 (delayed rejection off) */
+  __device__ int do_addrem_move(double* cs, double* sn)
+  {
+    int ms = sample_naive(K.q_ms + (size_t)c * 256, K.max_move_size) + 1;
+    if (lane == 0) ch->movesize = ms;
+    __syncwarp();
+    double lqf = 0, lqb = 0, lmpc = 0;
+    rs_build_from(cur);
+    prepare_addrem(lqf, ms);
+    do_addrem(lqf, lqb, lmpc, ms, cs, sn);
+    backward_prepare_addrem(lqb, ms);
+    double log_r = lqb - lqf;
+    log_r += lmpc + nm->ll - cur->ll;
+    double* rs = K.r_ms_sum + (size_t)c * 256;
+    double* rn = K.r_ms_n + (size_t)c * 256;
+    double addv = (log_r >= 0 ? 1.0 : exp(log_r));
+    __syncwarp();
+    if (lane == 0) { rs[ms - 1] += addv; rn[ms - 1] += 1.0; }
+    __syncwarp();
+    if (log_r >= 0 || log(u01()) <= log_r) {
+      accept_model();
+      return ms;
+    }
+    copy_model(nm, cur);
+    for (int i = 0; i < ms; ++i) {
+      uint32_t ind = s.move_inds[i];
+      if (s.move_isadd[i]) add_set_zero(ind, false);
+      else add_set_zero(ind, true);
+    }
+    return 0;
+  }
+
+  /* src/sampler.hpp:1271-1418 */
+  __device__ int do_swap_move(double* cs, double* sn)
+  {
+    long long full = (long long)K.p - cur->k;
+    int mm2 = (K.max_move_size + 1) / 2;
+    int mms = (int)min((long long)mm2, (full + 1) / 2);
+    mms = min(mms, cur->k);
+    int ms = sample_naive(K.q_nbs + (size_t)c * 128, mms) + 1;
+    if (lane == 0) ch->movesize = ms;
+    __syncwarp();
+    long long nbh = max(1ll, (full - ms) / 2);
+    nbh = min((long long)K.max_nbh, nbh);
+    int32_t* cmi = K.model_inds + (size_t)c * K.p;
+    const long long p = (long long)K.p;
+    for (int im = 0; im < ms; ++im) {
+      int mir = (int)floor(u01() * nm->k);
+      uint32_t ind_rem = nm->loci[mir];
+      long long ind_add;
+      int j = 0;
+      int mv = (int)floor(u01() * (double)nbh) + 1;
+      if (u01() < 0.5) {
+        ind_add = ind_rem;
+        j = 0;
+        while (j < mv) {
+          ++ind_add;
+          if (ind_add < p) { if (cmi[ind_add] < 0) ++j; }
+          else break;
+        }
+        if (ind_add == p) {
+          ind_add = ind_rem;
+          mv = mv + mv - j;
+          j = 0;
+          while (j < mv) {
+            --ind_add;
+            while (ind_add > 0 && cmi[ind_add] >= 0) --ind_add;
+            ++j;
+          }
+        }
+      } else {
+        ind_add = ind_rem;
+        j = 0;
+        if (ind_add > 0) {
+          while (j < mv) {
+            --ind_add;
+            if (ind_add > 0) { if (cmi[ind_add] < 0) ++j; }
+            else break;
+          }
+        }
+        if (j < mv) {
+          if (cmi[ind_add] < 0) ++j;
+          if (j < mv) {
+            ind_add = ind_rem;
+            mv = mv + mv - j;
+            j = 0;
+            while (j < mv) {
+              ++ind_add;
+              while (ind_add < p - 1 && cmi[ind_add] >= 0) ++ind_add;
+              ++j;
+            }
+          }
+        }
+      }
+      int t_ind = nm->type_inds[mir];
+      __syncwarp();
+      if (lane == 0) {
+        s.move_rem[im] = ind_rem;
+        s.move_add[im] = (uint32_t)ind_add;
+      }
+      __syncwarp();
+      remove_term(nm, mir, cs, sn);
+      __syncwarp();
+      if (lane == 0) cmi[ind_add] = t_ind;  // the reference's temporary marking
+      __syncwarp();
+    }
+    double itv[2];
+    for (int im = 0; im < ms; ++im) {
+      uint32_t ind_add = s.move_add[im];
+      int t_ind = (int)(signed char)cmi[ind_add];
+      int type = K.types[t_ind];
+      prepare_add(ind_add, type, itv, true);
+      add_term(nm, ind_add, t_ind, itv);
+      __syncwarp();
+      if (lane == 0) cmi[ind_add] = -1;
+      __syncwarp();
+    }
+    double log_r = nm->ll - cur->ll;
+    if (log_r >= 0 || log(u01()) <= log_r) {
+      accept_model();
+      for (int im = 0; im < ms; ++im) {
+        add_set_zero(s.move_rem[im], false);
+        add_set_zero(s.move_add[im], true);
+      }
+      return 2 * ms;
+    }
+    copy_model(nm, cur);
+    return 0;
+  }
+
+  /* src/sampler.hpp:1421-1669 (delayed rejection off) */
+  __device__ int do_statechange_move(double* cs, double* sn)
+  {
+    long long mms = min((long long)K.max_nbh * 2, min((long long)K.p - 1, (long long)K.max_move_size));
+    int ms = sample_naive(K.q_nbc + (size_t)c * 256, (int)mms) + 1;
+    if (lane == 0) ch->movesize = ms;
+    __syncwarp();
+    long long nbh = min((long long)K.max_nbh, (long long)K.p / 2);
+    int mic = (int)floor(u01() * nm->k);
+    long long ind_c = nm->loci[mic];
+    // the permutation of 2*nbh neighbours is kept in move_map
+    for (int i = lane; i < 2 * nbh && i <= BMG_MAX_MS; i += 32) s.move_map[i] = i;
+    __syncwarp();
+    long long wrap = ind_c + nbh;
+    if (ind_c < nbh) wrap += (nbh - ind_c);
+    else if (wrap > (long long)K.p - 1) wrap = (long long)K.p - 1;
+    for (int im = 0; im < ms; ++im) {
+      long long ind = (long long)floor(u01() * (double)(nbh * 2 - im)) + im;
+      __syncwarp();
+      if (lane == 0) {
+        long long t = s.move_map[im];
+        s.move_map[im] = s.move_map[ind];
+        s.move_map[ind] = t;
+      }
+      __syncwarp();
+    }
+    const int32_t* cmi = K.model_inds + (size_t)c * K.p;
+    int nadd = 0, nrem = 0;
+    for (int im = 0; im < ms; ++im) {
+      long long ind = s.move_map[im] + ind_c + 1;
+      if (ind > wrap) ind = ind_c - (ind - wrap);
+      // nm equals cur here, so cur's membership map answers nm's query
+      if (cmi[ind] < 0) { if (lane == 0) s.move_add[nadd] = (uint32_t)ind; ++nadd; }
+      else { if (lane == 0) s.move_rem[nrem] = (uint32_t)ind; ++nrem; }
+    }
+    __syncwarp();
+    double lmpc = 0;
+    for (int im = 0; im < nrem; ++im) {
+      int mir = find_locus(nm, s.move_rem[im]);
+      int type = K.types[nm->type_inds[mir]];
+      lmpc += lchange_rem(nm->Ns, nm->k, type);
+      remove_term(nm, mir, cs, sn);
+    }
+    double itv[2];
+    int t_ind = nm->type_inds[mic];
+    int type = K.types[t_ind];
+    for (int im = 0; im < nadd; ++im) {
+      uint32_t ind_add = s.move_add[im];
+      lmpc += lchange_add(nm->Ns, nm->k, type);
+      prepare_add(ind_add, type, itv, true);
+      add_term(nm, ind_add, t_ind, itv);
+    }
+    double log_r = lmpc + nm->ll - cur->ll;
+    log_r += log((double)cur->k) - log((double)nm->k);
+    if (log_r >= 0 || log(u01()) <= log_r) {
+      accept_model();
+      for (int im = 0; im < nadd; ++im) add_set_zero(s.move_add[im], true);
+      for (int im = 0; im < nrem; ++im) add_set_zero(s.move_rem[im], false);
+      return ms;
+    }
+    copy_model(nm, cur);
+    return 0;
+  }
+
+  /* src/sampler.hpp:1672-1713 */
+  __device__ int do_typeswitch_move(double* cs, double* sn)
+  {
+    if (lane == 0) ch->movesize = 1;
+    __syncwarp();
+    int mi = (int)round((cur->k - 1) * u01());
+    uint32_t ind = cur->loci[mi];
+    int tr = cur->type_inds[mi];
+    double qa[5], qc[5], tmp[5];
+    qtypes(ind, qa, qc);
+    int nt = K.n_types;
+    tmp[0] = (tr == 0) ? 0 : qa[0];
+    for (int i = 1; i < nt; ++i) tmp[i] = tmp[i - 1] + ((tr == i) ? 0 : qa[i]);
+    int ta = sample_naive(tmp, nt);
+    int type_add = K.types[ta], type_rem = K.types[tr];
+    double itv[2];
+    remove_term(nm, mi, cs, sn);
+    prepare_add(ind, type_add, itv, false);
+    add_term(nm, ind, ta, itv);
+    double r = lchange_swi(cur->Ns, type_add, type_rem) + nm->ll - cur->ll -
+               log(qa[ta] / tmp[nt - 1]) + log(qa[tr] / (qc[nt - 1] - qa[ta]));
+    if (r >= 0 || log(u01()) <= r) {
+      accept_model();
+      return 1;
+    }
+    copy_model(nm, cur);
+    return 0;
+  }
+
+  /* src/sampler.hpp:1715-1769 */
+  __device__ void adapt_move_size()
+  {
+    double* q_p0 = K.q_p0_ms + (size_t)c * 256;
+    const double* rs = K.r_ms_sum + (size_t)c * 256;
+    const double* rn = K.r_ms_n + (size_t)c * 256;
+    int mx = K.max_move_size;
+    double pms = ch->p_move_size;
+    if (K.acpt_goal > 0) {
+      double t = fmax(1.0, ch->k_move_size * (double)ch->p_proposal_n);
+      double ar = (double)ch->n_acpt[0] / (double)ch->n_moves[0];
+      pms = pms + (K.acpt_goal - ar) / (2.0 + t);
+      pms = fmax(fmin(pms, 0.99), 0.01);
+      if (lane == 0) { ch->n_acpt[0] = 1; ch->n_moves[0] = 2; }
+    } else {
+      double q = 1 - pms;
+      double zp = 1 - pow(q, (double)mx);
+      double q_p = pms / zp;
+      for (int i = 0; i < mx; ++i) {
+        double nv = q_p0[i] + q_p;
+        __syncwarp();
+        if (lane == 0) q_p0[i] = nv;
+        q_p *= q;
+      }
+      __syncwarp();
+      double p_best = 0.01, pp = 0.01, h_best = -INFINITY;
+      double step = 0.98 / 49.0;
+      for (int j = 0; j < 50; ++j) {
+        double h = 0.0, z = 0.0, qq = 1.0 - pp, qp = pp;
+        for (int i = 0; i < mx; ++i) {
+          double ratio = qp / q_p0[i];
+          h += (i + 1) * rs[i] * ratio;
+          z += rn[i] * ratio;
+          qp *= qq;
+        }
+        h /= z;
+        if (h > h_best) { h_best = h; p_best = pp; }
+        pp += step;
+      }
+      pms = p_best;
+    }
+    // Utils::geometric_dist_cdf
+    double* qms = K.q_ms + (size_t)c * 256;
+    double q = 1 - pms, qp = q;
+    for (int i = lane; i < mx; i += 32) {
+      double qi = q;
+      for (int t = 0; t < i; ++t) qi *= qp;
+      qms[i] = 1 - qi;
+    }
+    if (lane == 0) ch->p_move_size = pms;
+    __syncwarp();
+  }
+};
+
+// ------------------------------------------------------------ bulk phases
+// All 256 threads: fitted values of the current model's genotype columns in
+// fixed point (coefficients round(beta * 2^s)), the covariate part in FP64,
+// and the requested sums; optionally the residual limbs for the scan.
+#define BULK_PVE 1
+#define BULK_ALPHA 2
+#define BULK_RESID 4
+
+__device__ void bulk_phase(const DevConst& K, int c, MoveShared& s, BulkCols& bc)
+{
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const int mode = s.bulk_mode, nt = s.bulk_nterm, sh = s.bulk_s;
+  const int me = K.m_e;
+  const double sc = ldexp(1.0, -sh);
+  double s1g = 0, s2g = 0, s1e = 0, s2e = 0, s1t = 0, s2t = 0;
+  long long rsum = 0;
+  const uint32_t L = K.limbs_n;
+  for (uint64_t i = tid; i < K.n_pad; i += nth) {
+    long long yg = 0;
+    double ye = 0;
+    bool live = i < K.n;
+    if (live) {
+      for (int j = 0; j < nt; ++j) {
+        const uint8_t* row = K.geno + (size_t)bc.snp[j] * K.gs;
+        int code = (row[i >> 2] >> ((i & 3) * 2)) & 3;
+        int v = term_value(code, bc.term[j]);
+        if (v == 1) yg += bc.coef[j];
+        else if (v == 2) yg += 2 * bc.coef[j];
+      }
+      if (me > 1) {
+        for (int e = 0; e < me; ++e) ye += K.e[(size_t)e * K.n + i] * s.bulk_e[e];
+      } else {
+        ye = s.bulk_b0;
+      }
+    }
+    double ygd = (double)yg * sc;
+    if (live && (mode & (BULK_PVE | BULK_ALPHA))) {
+      s1g += ygd;
+      s2g += ygd * ygd;
+      if (mode & BULK_ALPHA) {
+        // eb = E beta_E - y, xb = fitted genotype part
+        s1e += (ye - K.y[i]) * ygd;
+      } else {
+        s1e += ye;
+        s2e += ye * ye;
+        double yt = ygd + ye;
+        s1t += yt;
+        s2t += yt * yt;
+      }
+    }
+    if (mode & BULK_RESID) {
+      long long R = 0;
+      if (live) {
+        long long Y = K.yint[i];
+        int d = K.sy - sh;
+        long long Ys = (d > 0) ? ((Y + (1ll << (d - 1))) >> d) : (Y << (-d));
+        long long E = (me > 1) ? __double2ll_rn(ye * ldexp(1.0, sh)) : s.bulk_b0i;
+        R = Ys - E - yg;
+        K.resid[(size_t)c * K.n_pad + i] = R;
+      }
+      rsum += R;
+      // balanced base-256 limbs, exact as bf16
+      long long rr = R;
+      for (uint32_t l = 0; l < L; ++l) {
+        int d8 = (int)(signed char)(rr & 0xff);
+        rr = (rr - d8) >> 8;
+        float f = (float)d8;
+        uint32_t bits = __float_as_uint(f);
+        K.limbs[((size_t)c * L + l) * K.n_pad + i] = (uint16_t)(bits >> 16);
+      }
+    }
+  }
+  // block reduction
+  double v6[6] = {s1g, s2g, s1e, s2e, s1t, s2t};
+  const int w = tid >> 5, ln = tid & 31;
+  for (int q = 0; q < 6; ++q) {
+    double r = warp_sum_d(v6[q]);
+    if (ln == 0) s.bd[w][q] = r;
+  }
+  long long rs = warp_sum_ll(rsum);
+  if (ln == 0) s.bl[w][0] = rs;
+  __syncthreads();
+  if (tid == 0) {
+    for (int q = 0; q < 6; ++q) {
+      double t = 0;
+      for (int ww = 0; ww < (nth >> 5); ++ww) t += s.bd[ww][q];
+      s.bsum[q] = t;
+    }
+    long long t = 0;
+    for (int ww = 0; ww < (nth >> 5); ++ww) t += s.bl[ww][0];
+    s.bsuml[0] = t;
+  }
+  __syncthreads();
+}
+
+// warp 0: fill the bulk column list and coefficients from the current model
+__device__ void bulk_setup(Warp& W, BulkCols& bc, int mode)
+{
+  DevModel* M = W.cur;
+  const DevConst& K = W.K;
+  int me = K.m_e, bl = M->blen, xc = M->xcols;
+  int nt = min(bl, xc) - me;
+  if (nt < 0) nt = 0;
+  double bound = 0;
+  for (int j = 0; j < nt; ++j) bound += 2.0 * fabs(M->beta[me + j]);
+  int sh;
+  if (mode & BULK_RESID) {
+    // |r_i| <= max|y| + sum_e max|E_e| |beta_e| + sum_j 2 |beta_j|; the limbs
+    // hold |R| < 2^(8L-1)
+    double eb = 0;
+    for (int e = 0; e < me && e < bl; ++e) eb += K.e_absmax[e] * fabs(M->beta[e]);
+    double tot = bound + K.y_absmax + eb + 1e-300;
+    int e2 = (int)ceil(log2(tot));
+    sh = (int)(8 * K.limbs_n - 3) - e2;
+  } else {
+    // fitted genotype values stay below 2^52 so they convert to double exactly
+    int e2 = (int)ceil(log2(bound + 1e-300));
+    sh = 51 - e2;
+  }
+  if (sh > 60) sh = 60;
+  double scl = ldexp(1.0, sh);
+  for (int j = W.lane; j < nt; j += 32) {
+    bc.snp[j] = M->xc_snp[me + j];
+    bc.term[j] = (int8_t)M->xc_type[me + j];
+    bc.coef[j] = __double2ll_rn(M->beta[me + j] * scl);
+  }
+  if (W.lane == 0) {
+    W.s.bulk_mode = mode;
+    W.s.bulk_nterm = nt;
+    W.s.bulk_s = sh;
+    W.s.bulk_b0 = (bl > 0) ? M->beta[0] : 0.0;
+    W.s.bulk_b0i = __double2ll_rn(W.s.bulk_b0 * scl);
+    for (int e = 0; e < 8; ++e) W.s.bulk_e[e] = (e < me && e < bl) ? M->beta[e] : 0.0;
+  }
+  __syncwarp();
+}
+
+// ------------------------------------------------------------- RB step
+/* src/sampler.cpp:731-811: everything of an RB step except the p-wide scan.
+   With scan_only the flags ask for p_r only and no counter moves. */
+__device__ void prep_rb(Warp& W, bool scan_only)
+{
+  const DevConst& K = W.K;
+  DevChain* ch = W.ch;
+  RbParams* rp = K.rb + W.c;
+  DevModel* M = W.cur;
+  bool do_scan, adapt;
+  int acc_rao = 0;
+  double rz1 = 0, rz2 = 0, pz1 = 0, pz2 = 0;
+  if (scan_only) {
+    do_scan = true;
+    adapt = false;
+  } else {
+    do_scan = !K.flat_proposal_dist || ch->n_rao_burnin == 0;
+    if (ch->n_rao_burnin == 0) {
+      rz1 = (double)(ch->p_rao_n + 1);
+      rz2 = (double)ch->p_rao_n / rz1;
+      acc_rao = 1;
+    }
+    uint64_t burn = ch->n_rao_burnin;
+    if (burn > 0) burn--;
+    adapt = K.adaptation || burn > 0;
+    pz1 = (double)(ch->p_proposal_n + 1);
+    pz2 = (double)ch->p_proposal_n / pz1;
+    __syncwarp();
+    if (W.lane == 0) {
+      if (acc_rao) ch->p_rao_n++;
+      ch->n_rao_burnin = burn;
+    }
+  }
+  if (W.lane == 0) {
+    rp->do_scan = do_scan;
+    rp->acc_rao = acc_rao;
+    rp->adapt = adapt && !K.flat_proposal_dist;
+    rp->rao_z1 = rz1;
+    rp->rao_z2 = rz2;
+    rp->prop_z1 = pz1;
+    rp->prop_z2 = pz2;
+    rp->inv_2s2 = 1.0 / (2 * M->sigma2);
+    rp->scale = ldexp(1.0, -W.s.bulk_s);
+    rp->mr = (double)W.s.bsuml[0] * ldexp(1.0, -W.s.bulk_s) / (double)K.n;
+    for (int t = 0; t < 4; ++t) rp->itv[t] = ch->inv_t2a2[t];
+  }
+  // log prior changes of the scan (src/sampler.cpp:51-76)
+  int Ns[5];
+  for (int t = 0; t < 5; ++t) Ns[t] = M->Ns[t];
+  int nl = M->k;
+  for (int t = 0; t < 5; ++t) {
+    if (!K.allow_types[t]) continue;
+    double la = 0;
+    if ((uint64_t)(Ns[t] + 1) <= K.p) la = W.lchange_add(Ns, nl, t);
+    if (W.lane == 0) rp->lmp_add[t] = la;
+    Ns[t]--;
+    nl--;
+    if (Ns[t] >= 0) {
+      for (int j = 0; j < 5; ++j) {
+        if (!K.allow_types[j]) continue;
+        double lr = W.lchange_add(Ns, nl, j);
+        if (W.lane == 0) rp->lmp_rem[t][j] = lr;
+      }
+    }
+    Ns[t]++;
+    nl++;
+  }
+  __syncwarp();
+  if (!scan_only && adapt) {
+    if (K.adapt_p_move_size) W.adapt_move_size();
+    if (W.lane == 0) {
+      ch->p_proposal_n++;
+      if (!K.flat_proposal_dist) ch->rebuild = 1;
+    }
+  }
+  if (W.lane == 0) ch->rb_pending = do_scan || adapt;
+  __syncwarp();
+}
+
+// ------------------------------------------------------------- kernels
+// Model of every chain at construction (src/model.hpp:49-113): the covariate
+// block is set by the host; here its likelihood, then new = current.
+extern "C" __global__ void __launch_bounds__(32)
+bmg_init_kernel(DevConst K)
+{
+  __shared__ MoveShared s;
+  if (threadIdx.x == 0) s.err = 0;
+  __syncwarp();
+  Warp W(K, blockIdx.x, s);
+  W.compute_log_likelihood(W.cur);
+  W.copy_model(W.nm, W.cur);
+  if (W.lane == 0 && s.err) W.ch->error = s.err;
+}
+
+// Residual limbs and RbParams of every chain at its current beta, for a scan
+// requested outside the MCMC loop (bmg_scan).
+extern "C" __global__ void __launch_bounds__(BMG_MOVE_THREADS, 1)
+bmg_rbprep_kernel(DevConst K)
+{
+  __shared__ MoveShared s;
+  __shared__ BulkCols bc;
+  const int c = blockIdx.x, tid = threadIdx.x;
+  if (tid == 0) s.err = 0;
+  __syncthreads();
+  Warp W(K, c, s);
+  if (tid < 32) bulk_setup(W, bc, BULK_RESID);
+  __syncthreads();
+  bulk_phase(K, c, s, bc);
+  if (tid < 32) prep_rb(W, true);
+}
+
+// Runs iterations of chain blockIdx.x until `max_iters` are done or an RB
+// step has been prepared (its residual limbs and RbParams written).
+extern "C" __global__ void __launch_bounds__(BMG_MOVE_THREADS, 1)
+bmg_move_kernel(DevConst K, int max_iters)
+{
+  __shared__ MoveShared s;
+  __shared__ BulkCols bc;
+  __shared__ long long part[BMG_MOVE_THREADS];
+  const int c = blockIdx.x;
+  const int tid = threadIdx.x;
+  DevChain* ch = K.ch + c;
+  if (tid == 0) {
+    s.err = ch->error;
+    s.n_pend = ch->n_pend;
+    s.iter_stop = 0;
+  }
+  __syncthreads();
+  if (s.err) return;
+  for (int i = tid; i < s.n_pend; i += blockDim.x) {
+    int sn = ch->pend_snp[i];
+    s.pend_snp[i] = sn;
+    s.pend_pos[i] = K.pos[sn];
+    double pp = K.p_prop[(size_t)c * K.p + K.pos[sn]];
+    long long w = __double2ll_rn(fmax(pp, K.q_add_min) * ldexp(1.0, K.qs));
+    bool bz = (K.basebits[(size_t)c * ((K.p + 31) / 32) + (sn >> 5)] >> (sn & 31)) & 1u;
+    s.pend_d[i] = bz ? w : -w;
+  }
+  __syncthreads();
+
+  // warp 0 keeps the sampler context (and its random stream) in registers
+  Warp W(K, c, s);
+  double* cs_buf = K.scratch + (size_t)c * 2 * K.km;
+  double* sn_buf = cs_buf + K.km;
+
+  if (tid < 32 && !ch->started) {
+    /* src/sampler.cpp:551-620: the model is still empty here, so alpha is
+       drawn from its prior and needs no data pass */
+    if (!isfinite(W.cur->ll)) W.fail(BMG_DERR_START);
+    W.copy_model(W.nm, W.cur);
+    W.sample_beta_sigma2(W.cur);
+    W.sample_tau2(W.cur);
+    double a = W.sample_alpha(W.cur, 0.0, 0.0);
+    W.set_alpha(a, W.cur);
+    W.compute_log_likelihood(W.cur);
+    W.copy_model(W.nm, W.cur);
+    if (W.lane == 0) ch->started = 1;
+  }
+  __syncthreads();
+
+  for (int it = 0; it < max_iters; ++it) {
+    __syncthreads();
+    if (s.err || s.iter_stop) break;
+    // room for one more move's flips of dd_add, else rebuild its prefix here
+    if (s.n_pend > BMG_PEND_MAX - 2 * (int)K.max_move_size - 2) {
+      if (tid == 0) ch->n_pend = 0;
+      rebuild_chain(K, c, part);
+      if (tid == 0) s.n_pend = 0;
+      __syncthreads();
+    }
+    const uint64_t iter = ch->n_iter;
+    const bool ns_step = ((iter + 1) % K.n_sample_tau2) == 0;
+    const bool thin_step = ((iter + 1) % K.thin) == 0;
+    const bool rb_step = ((iter + 1) % K.n_rao) == 0;
+    if (ns_step) {
+      /* src/sampler.cpp:628-635 */
+      if (tid < 32) bulk_setup(W, bc, BULK_ALPHA);
+      __syncthreads();
+      bulk_phase(K, c, s, bc);
+      if (tid < 32) {
+        W.sample_tau2(W.cur);
+        double a = W.sample_alpha(W.cur, s.bsum[1], s.bsum[2]);
+        W.set_alpha(a, W.cur);
+        W.compute_log_likelihood(W.cur);
+        W.copy_model(W.nm, W.cur);
+      }
+      __syncthreads();
+    }
+    if (tid < 32) {
+      /* src/sampler.cpp:637-684; move mix of compute_p_moves (:455-515) */
+      double pm[7], pcs[7];
+      if (K.n_types > 1) { pm[0] = 0.8; pm[1] = 0.1; pm[2] = 0.0; pm[3] = 0.1; }
+      else { pm[0] = 0.7; pm[1] = 0.15; pm[2] = 0.15; pm[3] = 0.0; }
+      pm[4] = pm[5] = pm[6] = 0.0;
+      pcs[0] = pm[0];
+      for (int i = 1; i < 7; ++i) pcs[i] = pcs[i - 1] + pm[i];
+      int move = W.sample_naive(pcs, 7);
+      int jd = 0;
+      switch (move) {
+        case 0: jd = W.do_addrem_move(cs_buf, sn_buf); break;
+        case 1:
+          if (W.cur->k > 0 && (long long)W.cur->k < (long long)K.p - 1) jd = W.do_swap_move(cs_buf, sn_buf);
+          break;
+        case 2:
+          if (W.cur->k > 0 && K.p > 2) jd = W.do_statechange_move(cs_buf, sn_buf);
+          break;
+        case 3:
+          if (W.cur->k > 0) jd = W.do_typeswitch_move(cs_buf, sn_buf);
+          break;
+        default: W.fail(BMG_DERR_NAN); break;
+      }
+      if (W.lane == 0) {
+        ch->n_moves[move]++;
+        ch->n_acpt[move] += (jd > 0);
+        ch->n_accepted += (jd > 0);
+      }
+      __syncwarp();
+      const bool pre_ns = ((iter + 2) % K.n_sample_tau2) == 0;
+      if (thin_step || pre_ns) W.sample_beta_sigma2(W.cur);
+      if (W.lane == 0) {
+        uint32_t ti = ch->tr_iter;
+        if (ti < K.tr.iter_cap) {
+          size_t o = (size_t)c * K.tr.iter_cap + ti;
+          K.tr.jump[o] = (uint8_t)jd;
+          K.tr.mtype[o] = (uint8_t)move;
+          K.tr.msize[o] = (uint8_t)ch->movesize;
+          ch->tr_iter = ti + 1;
+        } else if (s.err == 0) {
+          s.err = BMG_DERR_TRACE;
+        }
+      }
+      __syncwarp();
+      if (thin_step) bulk_setup(W, bc, BULK_PVE | (rb_step ? BULK_RESID : 0));
+    }
+    __syncthreads();
+    if (thin_step) {
+      bulk_phase(K, c, s, bc);
+      if (tid < 32) {
+        /* src/sampler.cpp:691-727, src/model.hpp:345-392 */
+        DevModel* M = W.cur;
+        const double n = (double)K.n;
+        const bool ce = K.m_e > 1, cg = M->k > 0;
+        double pv[3];
+        double vg = (s.bsum[1] - s.bsum[0] * s.bsum[0] / n) / (n - 1);
+        double ve = (s.bsum[3] - s.bsum[2] * s.bsum[2] / n) / (n - 1);
+        double vt = (s.bsum[5] - s.bsum[4] * s.bsum[4] / n) / (n - 1);
+        pv[2] = ce ? ve : 0.0;
+        pv[1] = cg ? vg : 0.0;
+        if (ce || cg) {
+          pv[0] = !ce ? pv[1] : (!cg ? pv[2] : vt);
+          double z = pv[0] + M->sigma2;
+          pv[0] /= z; pv[1] /= z; pv[2] /= z;
+        } else {
+          pv[0] = pv[1] = pv[2] = 0;
+        }
+        double lp = W.log_model(M->Ns);
+        uint32_t tt = ch->tr_thin, tl = ch->tr_loci;
+        bool room = tt < K.tr.thin_cap && tl + M->k <= K.tr.loci_cap;
+        if (W.lane == 0) {
+          ch->pves[0] = pv[0]; ch->pves[1] = pv[1]; ch->pves[2] = pv[2];
+          if (room) {
+            size_t o = (size_t)c * K.tr.thin_cap + tt;
+            K.tr.msz[o] = M->k;
+            K.tr.ll[o] = M->ll;
+            K.tr.lp[o] = lp;
+            K.tr.s2[o] = M->sigma2;
+            K.tr.alpha[o] = ch->alpha;
+            K.tr.pve[3 * o] = pv[0];
+            K.tr.pve[3 * o + 1] = pv[1];
+            K.tr.pve[3 * o + 2] = pv[2];
+            ch->tr_thin = tt + 1;
+            ch->tr_loci = tl + M->k;
+          } else if (s.err == 0) {
+            s.err = BMG_DERR_TRACE;
+          }
+        }
+        if (room) {
+          for (int i = W.lane; i < M->k; i += 32) {
+            K.tr.loci[(size_t)c * K.tr.loci_cap + tl + i] = M->loci[i];
+            K.tr.types[(size_t)c * K.tr.loci_cap + tl + i] = M->type_inds[i];
+          }
+        }
+        if (K.save_beta) {
+          uint32_t tb = ch->tr_beta;
+          if (tb + M->blen <= K.tr.beta_cap) {
+            for (int i = W.lane; i < M->blen; i += 32) K.tr.beta[(size_t)c * K.tr.beta_cap + tb + i] = M->beta[i];
+            __syncwarp();
+            if (W.lane == 0) ch->tr_beta = tb + M->blen;
+          } else if (W.lane == 0 && s.err == 0) {
+            s.err = BMG_DERR_TRACE;
+          }
+        }
+        __syncwarp();
+      }
+    }
+    __syncthreads();
+    if (tid < 32) {
+      if (rb_step) {
+        prep_rb(W, false);
+        if (W.lane == 0) s.iter_stop = 1;
+      }
+      if (K.verbosity > 0 && ((iter + 1) % K.verbosity) == 0) {
+        /* src/sampler.cpp:813-833 */
+        double lp = W.log_model(W.cur->Ns);
+        if (W.lane == 0) {
+          uint32_t tg = ch->tr_log;
+          if (tg < K.tr.log_cap) {
+            double* r = K.tr.logrec + ((size_t)c * K.tr.log_cap + tg) * BMG_LOGREC;
+            r[0] = (double)(iter + 1);
+            r[1] = (double)ch->n_accepted;
+            r[2] = (double)ch->n_acpt[1];
+            r[3] = (double)ch->n_moves[1];
+            r[4] = (double)ch->n_acpt[2];
+            r[5] = (double)ch->n_moves[2];
+            r[6] = ch->p_move_size;
+            r[7] = (double)W.cur->k;
+            r[8] = W.cur->ll + lp;
+            r[9] = ch->pves[0];
+            r[10] = ch->pves[1];
+            r[11] = ch->pves[2];
+            r[12] = W.cur->sigma2;
+            ch->tr_log = tg + 1;
+          }
+        }
+      }
+      if (W.lane == 0) {
+        ch->n_iter = iter + 1;
+        if (s.err) ch->error = s.err;
+      }
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  if (tid == 0) {
+    ch->rng = W.rng;
+    ch->n_pend = s.n_pend;
+    for (int i = 0; i < s.n_pend; ++i) ch->pend_snp[i] = s.pend_snp[i];
+    if (s.err) ch->error = s.err;
+  }
+}

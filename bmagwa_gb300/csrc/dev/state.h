@@ -1,0 +1,232 @@
+// Device-resident data layout of libbmg (shared by host and device code).
+//
+// HBM layout (one context):
+//   geno      m_g rows of `gs` bytes: PLINK 2-bit codes, 4 individuals per
+//             byte, rows padded to a multiple of 16 bytes (64 individuals);
+//             padding codes are 00 and every padded individual carries a zero
+//             residual, so it adds nothing to any product.
+//   cnt       per SNP: counts of genotype 1 and 2 (missing codes rejected).
+//   pre       per SNP: the reference's precomputed sums and centred second
+//             moments (src/precomputed_snp_covariances.hpp:42-84 layout).
+//   inorder   heap node -> in-order rank of the reference's proposal tree
+//             (src/discrete_distribution.hpp:217-261) and its inverse.
+//   per chain: two models (current, proposed), the dynamic sampler state,
+//             proposal arrays of m_g doubles, a prefix array of m_g+1
+//             doubles, a model-membership bitmap and model index map.
+#ifndef BMG_DEV_STATE_H_
+#define BMG_DEV_STATE_H_
+
+#include <stdint.h>
+
+#include "bmg_rng.h"
+
+#define BMG_MOVE_THREADS 256
+#define BMG_PEND_MAX 64          /* pending zero/unzero flips of dd_add */
+#define BMG_MAX_MS 255
+#define BMG_REMSET_MAX 1280      /* in-model SNPs + moved SNPs for dd_rem */
+
+// One model (bmagwa::Model, src/model.hpp:394-423) of one chain.
+// Matrices are column-major with leading dimension km (max_model_size).
+struct DevModel {
+  int k;          // loci in the model
+  int xcols;      // columns of X (covariates incl. constant + terms)
+  int llen;       // active order of l
+  int vlen;       // active length of v
+  int blen;       // active length of beta
+  int Ns[5];
+  int mu_beta_computed;
+  int pad_;
+  double sigma2, syx, ldq, ldqx, ll;
+  // arrays (device pointers into the chain's arena)
+  double* xx;     // km x km upper
+  double* l;      // km x km upper Cholesky factor
+  double* xy;     // km
+  double* v;
+  double* inv;    // inv_tau2_alpha2 per column
+  double* beta;
+  double* mu_beta;
+  uint32_t* loci;       // km
+  uint8_t* type_inds;   // km
+  uint32_t* x_ind1;
+  uint32_t* x_ind2;
+  uint32_t* xc_snp;     // x_ind_to_g_ind
+  int32_t* xc_type;     // x_types (4 = covariate)
+};
+
+// Dynamic per-chain sampler state (bmagwa::Sampler members that change).
+struct DevChain {
+  bmg_rng_t rng;
+  uint64_t n_iter;
+  uint64_t n_accepted;
+  uint64_t n_rao_burnin;     // remaining
+  uint64_t p_proposal_n;
+  int64_t p_rao_n;
+  uint64_t n_moves[7];
+  uint64_t n_acpt[7];
+  uint64_t n_lik_add, n_lik_rem, n_lik_full;
+  double alpha, alpha2;       // Prior::alpha_ / alpha2_
+  double inv_t2a2[4];         // Prior::inv_tau2_alpha2
+  double p_move_size;
+  double k_move_size;
+  double pves[3];
+  int started;
+  int movesize;
+  int error;                  // 0 = fine; see BMG_DERR_*
+  int rb_pending;             // an RB scan must follow this launch
+  // dd_add prefix bookkeeping
+  int64_t cadd_total;         // prefix[m_g] at the last rebuild
+  int n_pend;
+  int rebuild;                // proposal weights changed: rebuild prefix
+  int pend_snp[BMG_PEND_MAX];
+  // trace cursor (reset by the host per chunk)
+  uint32_t tr_iter;
+  uint32_t tr_thin;
+  uint32_t tr_loci;
+  uint32_t tr_beta;
+  uint32_t tr_log;
+};
+
+// one _log.txt line (src/sampler.cpp:813-833): iter, n_accepted, n_acpt[1],
+// n_moves[1], n_acpt[2], n_moves[2], p_move_size, model size, log p, pve[3], sigma2
+#define BMG_LOGREC 13
+
+// Device error codes (DevChain::error)
+#define BMG_DERR_NONE 0
+#define BMG_DERR_CAPACITY 1      // model larger than max_model_size
+#define BMG_DERR_NAN 2           // NaN where the reference throws
+#define BMG_DERR_RNG 3           // gamma sampler ran out of attempts
+#define BMG_DERR_PEND 4          // pending proposal list overflow
+#define BMG_DERR_TRACE 5         // trace buffer overflow
+#define BMG_DERR_REMSET 6
+#define BMG_DERR_START 7         // non-finite likelihood at start
+
+// Parameters the move kernel hands to the RB scan epilogue, per chain.
+struct RbParams {
+  double inv_2s2;           // 1 / (2 sigma2)
+  double mr;                // mean residual
+  double scale;             // 2^-s of the fixed-point residual
+  double itv[4];            // inv_tau2_alpha2 per term (shared tau2)
+  double lmp_add[5];
+  double lmp_rem[5][5];
+  double rao_z1, rao_z2;    // running-mean weights of p_rao
+  double prop_z1, prop_z2;  // running-mean weights of p_proposal
+  int do_scan;              // compute p_r at all this step
+  int acc_rao;              // n_rao_burnin <= 0: accumulate p_rao
+  int adapt;                // update p_proposal and the proposal weights
+};
+
+// Trace buffers of one chunk (device), per chain.
+struct DevTrace {
+  uint8_t* jump;      // chains x iters
+  uint8_t* mtype;
+  uint8_t* msize;
+  uint32_t* msz;      // chains x thin_cap
+  uint32_t* loci;     // chains x loci_cap
+  uint8_t* types;     // chains x loci_cap
+  double* ll;         // chains x thin_cap
+  double* lp;
+  double* s2;
+  double* alpha;
+  double* pve;        // chains x thin_cap x 3
+  double* beta;       // chains x beta_cap
+  double* logrec;     // chains x log_cap x BMG_LOGREC doubles (the _log.txt lines)
+  uint32_t iter_cap, thin_cap, loci_cap, beta_cap, log_cap;
+};
+
+// Read-only context constants.
+struct DevConst {
+  // sizes
+  uint64_t n;           // individuals
+  uint64_t p;           // SNPs (m_g)
+  uint32_t gs;          // bytes per genotype row (multiple of 16)
+  uint32_t nw;          // 32-bit words per genotype row (gs / 4)
+  uint32_t m_e;         // covariate columns incl. the constant
+  uint32_t km;          // max_model_size
+  uint32_t n_chains;
+  uint32_t n_types;
+  int32_t types[5];
+  int32_t allow_types[5];
+  int32_t allow_terms[4];
+  int32_t offset;       // per-SNP doubles of `pre`
+  int32_t offset_type[4];
+  uint32_t n_terms;     // allowed terms (rows per SNP in the scan)
+  int32_t term_of[4];   // scan row r -> term type
+  // sampler options
+  uint64_t n_rao, thin, n_sample_tau2, verbosity;
+  uint32_t max_move_size;       // already min(m_g, 255, option)
+  uint32_t max_nbh;
+  double p_move_size_nbs, p_move_size_nbc;
+  int32_t adapt_p_move_size;
+  double acpt_goal;
+  int32_t adaptation, flat_proposal_dist, save_beta;
+  double q_add_min, q_rem_min;
+  // prior constants (per context; sigma2 terms per phenotype below)
+  double n_plus_nu, minus_n_plus_nu_2, nus2_plus_yy;
+  double mu_alpha;
+  int32_t use_individual_tau2;
+  double g_a, g_b;
+  double types_prior[5], types_prior_sum;
+  double nu_tau2[4], s2_tau2[4], nus2_tau2[4];
+  double rng_nu;        // n + nu_sigma2 (src/sampler.hpp:127)
+  // Host-computed prior tables (index = a count 0..km+1), evaluated with the
+  // reference's own expressions (src/prior.hpp:144-183) by the host libm:
+  //   add_a[nl] = log(g_a + nl) - log(g_b + m_g - nl - 1)
+  //   rem_a[nl] = log(g_b + m_g - nl) - log(g_a + nl - 1)
+  //   lt[t][k] = log(tp[t] + k),   ltm1[t][k] = log(tp[t] + k - 1)
+  //   ls[k] = log(tps + k),        lsm1[k] = log(tps + k - 1)
+  //   lgt[t][k] = lgamma(tp[t] + k), lga[k] = lgamma(g_a + k),
+  //   lgb[k] = lgamma(g_b + m_g - k), lgs[k] = lgamma(tps + k)
+  // Layout: one array `tab`, each table tw = km + 2 entries; typed tables
+  // hold 5 rows.
+  const double* tab;
+  uint32_t tw;
+  int32_t qs;           // fixed-point exponent of the dd_add weights
+  // data
+  const uint8_t* geno;
+  const int32_t* cnt;   // p x 2
+  const double* pre;    // p x offset
+  const double* lvar;   // p x n_terms: log of the centred second moment
+  const int32_t* pos;   // heap node -> in-order rank
+  const int32_t* inv;   // in-order rank -> heap node
+  const double* y;      // n
+  const int64_t* yint;  // n, y * 2^sy rounded
+  int32_t sy;
+  const double* e;      // n x m_e column-major (column 0 = 1)
+  const int64_t* eint;  // m_e x n fixed point covariates (column 0 unused)
+  const int32_t* se;    // per covariate scale exponent
+  const double* ee;     // m_e x m_e upper: E'E (host, FP64)
+  const double* ey;     // m_e: E'y
+  const double* inv_tau2_e;  // m_e
+  double y_absmax;      // max |y|
+  const double* e_absmax;    // m_e: max |E column| (1 for the constant)
+  double* scratch;      // chains x 2 km: Givens cosines and sines
+  double yy;
+  // per-chain arrays
+  DevModel* cur;        // chains
+  DevModel* nm;         // chains
+  DevChain* ch;         // chains
+  RbParams* rb;         // chains
+  double* p_prop;       // chains x p
+  double* p_prop_types; // chains x p x n_types
+  double* p_rao;        // chains x p
+  double* p_rao_types;  // chains x p x n_types
+  double* p_r;          // chains x p (last scan; optional output)
+  double* p_r_types;    // chains x p x n_types
+  double* q_ms;         // chains x 256: q_p_move_size
+  double* q_nbs;        // chains x 128
+  double* q_nbc;        // chains x 256
+  double* r_ms_sum;     // chains x 256
+  double* r_ms_n;       // chains x 256
+  double* q_p0_ms;      // chains x 256
+  int64_t* cadd;        // chains x (p + 1) prefix of dd_add weights (x 2^qs) in in-order
+  uint32_t* inbits;     // chains x ceil(p/32): SNP in current model
+  uint32_t* basebits;   // chains x ceil(p/32): zeroed in the cadd base
+  int32_t* model_inds;  // chains x p: current model's index or -1
+  int64_t* resid;       // chains x n_pad: fixed-point residual of the last RB step
+  uint16_t* limbs;      // (chains * L) x n_pad bf16 residual limbs (scan B operand)
+  uint32_t n_pad;       // individuals padded to the scan's K multiple
+  uint32_t limbs_n;     // L
+  DevTrace tr;
+};
+
+#endif

@@ -235,6 +235,10 @@ bmg_status bmg_finish(bmg_ctx* ctx);
  * [0] move kernel, [1] scan, [2] proposal rebuild, [3] total. */
 bmg_status bmg_get_timings(bmg_ctx* ctx, double* ms4);
 
+/* var_x, mean_x, var_y, y'y of the loaded data (src/data.hpp:66-71; the
+ * reference prints the first three at start, src/main.cpp:58-62). */
+bmg_status bmg_get_data_stats(bmg_ctx* ctx, double* out4);
+
 const char* bmg_last_error(const bmg_ctx* ctx);
 const char* bmg_status_string(bmg_status s);
 void bmg_destroy(bmg_ctx* ctx);
