@@ -60,6 +60,8 @@ def lib():
         L.bmg_get_rao.argtypes = [vp, u32, vp, vp]
         L.bmg_finish.argtypes = [vp]
         L.bmg_get_timings.argtypes = [vp, vp]
+        L.bmg_get_proposal.argtypes = [vp, u32, vp, vp]
+        L.bmg_get_last_scan.argtypes = [vp, u32, vp, vp]
         L.bmg_get_data_stats.argtypes = [vp, vp]
         L.bmg_last_error.argtypes = [vp]
         L.bmg_last_error.restype = C.c_char_p
@@ -69,7 +71,8 @@ def lib():
         L.bmg_destroy.restype = None
         for name in ("bmg_create", "bmg_load_bed", "bmg_set_phenotypes", "bmg_set_covariates",
                      "bmg_precompute", "bmg_get_precomputed", "bmg_scan", "bmg_run", "bmg_get_state",
-                     "bmg_get_rao", "bmg_finish", "bmg_get_timings", "bmg_get_data_stats"):
+                     "bmg_get_rao", "bmg_finish", "bmg_get_timings", "bmg_get_data_stats",
+                     "bmg_get_proposal", "bmg_get_last_scan"):
             getattr(L, name).restype = C.c_int
         _lib = L
     return _lib
@@ -202,6 +205,18 @@ class Context:
         p = np.zeros(self.m_g)
         pt = np.zeros(self.m_g * self.n_types) if self.n_types > 1 else None
         self._check(lib().bmg_get_rao(self.h, chain, _ptr(p), _ptr(pt)))
+        return p, (pt.reshape(self.m_g, self.n_types) if pt is not None else None)
+
+    def proposal(self, chain=0):
+        p = np.zeros(self.m_g)
+        pt = np.zeros(self.m_g * self.n_types) if self.n_types > 1 else None
+        self._check(lib().bmg_get_proposal(self.h, chain, _ptr(p), _ptr(pt)))
+        return p, (pt.reshape(self.m_g, self.n_types) if pt is not None else None)
+
+    def last_scan(self, chain=0):
+        p = np.zeros(self.m_g)
+        pt = np.zeros(self.m_g * self.n_types) if self.n_types > 1 else None
+        self._check(lib().bmg_get_last_scan(self.h, chain, _ptr(p), _ptr(pt)))
         return p, (pt.reshape(self.m_g, self.n_types) if pt is not None else None)
 
     def data_stats(self):

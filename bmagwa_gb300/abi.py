@@ -117,6 +117,7 @@ class ChainState(C.Structure):
         ("n_iter", C.c_uint64),
         ("n_accepted", C.c_uint64),
         ("p_move_size", C.c_double),
+        ("rng_draws", C.c_uint64),
     ]
 
 

@@ -584,6 +584,23 @@ extern "C" bmg_status bmg_precompute(bmg_ctx* ctx)
   double* dtab = ctx->dalloc<double>(tab.size(), false);
   CK(cudaMemcpyAsync(dtab, tab.data(), 8 * tab.size(), cudaMemcpyHostToDevice, ctx->stream));
   K.tab = dtab;
+  {  // the move-size grid of Sampler::adapt_p_move_size_jd_mb (src/sampler.hpp:1739-1766)
+    std::vector<double> grid(50), pw(51);
+    double pp = 0.01, step = 0.98 / 49.0;
+    for (int j = 0; j < 50; ++j) {
+      grid[j] = pp;
+      pw[j] = std::pow(1 - pp, (double)ctx->max_ms);
+      pp += step;
+    }
+    pw[50] = std::pow(1 - o.p_move_size, (double)ctx->max_ms);
+    double* dg = ctx->dalloc<double>(50, false);
+    double* dp = ctx->dalloc<double>(51, false);
+    CK(cudaMemcpyAsync(dg, grid.data(), 8 * 50, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(dp, pw.data(), 8 * 51, cudaMemcpyHostToDevice, ctx->stream));
+    K.ms_grid = dg;
+    K.ms_pow = dp;
+    K.ms_init = o.p_move_size;
+  }
   int qbits = 0;
   while ((1ull << qbits) < p + 1) ++qbits;
   K.qs = 61 - qbits;
@@ -614,6 +631,7 @@ extern "C" bmg_status bmg_precompute(bmg_ctx* ctx)
   K.n_pad = ctx->n_pad;
   K.limbs_n = ctx->L;
   K.resid = ctx->dalloc<int64_t>((size_t)C * ctx->n_pad);
+  K.yhat = ctx->dalloc<double>((size_t)C * n);
   K.limbs = ctx->dalloc<uint16_t>((size_t)C * ctx->L * ctx->n_pad);
   ctx->resid_t = ctx->dalloc<int64_t>((size_t)C * ctx->n_pad);
   K.scratch = ctx->dalloc<double>((size_t)C * 2 * km);
@@ -977,6 +995,7 @@ extern "C" bmg_status bmg_get_state(bmg_ctx* ctx, uint32_t chain, bmg_chain_stat
   st->n_iter = h.n_iter;
   st->n_accepted = h.n_accepted;
   st->p_move_size = h.p_move_size;
+  st->rng_draws = h.rng.slot;
   for (int i = 0; i < M.k && (uint32_t)i < loci_cap; ++i) {
     if (loci) loci[i] = lc[i];
     if (type_inds) type_inds[i] = ti[i];
@@ -995,6 +1014,46 @@ extern "C" bmg_status bmg_get_rao(bmg_ctx* ctx, uint32_t chain, double* p_rao, d
   if (p_rao) CK(cudaMemcpyAsync(p_rao, ctx->K.p_rao + chain * p, 8 * p, cudaMemcpyDeviceToHost, ctx->stream));
   if (p_rao_types && ctx->opt.n_types > 1)
     CK(cudaMemcpyAsync(p_rao_types, ctx->K.p_rao_types + chain * p * ctx->opt.n_types, 8 * p * ctx->opt.n_types,
+                       cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return BMG_OK;
+  API_END
+}
+
+extern "C" bmg_status bmg_get_proposal(bmg_ctx* ctx, uint32_t chain, double* p_prop, double* p_prop_types)
+{
+  if (!ctx) return BMG_EINVAL;
+  API_BEGIN
+  check_ready(ctx);
+  if (chain >= ctx->C) throw bmg_error(BMG_EINVAL, "chain index");
+  const size_t p = ctx->p;
+  if (p_prop) {
+    // stored in the proposal tree's in-order position order
+    std::vector<double> byq(p);
+    std::vector<int32_t> pos, inv;
+    inorder_ranks(p, pos, inv);
+    CK(cudaMemcpyAsync(byq.data(), ctx->K.p_prop + chain * p, 8 * p, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    for (size_t j = 0; j < p; ++j) p_prop[j] = byq[pos[j]];
+  }
+  if (p_prop_types && ctx->opt.n_types > 1)
+    CK(cudaMemcpyAsync(p_prop_types, ctx->K.p_prop_types + chain * p * ctx->opt.n_types,
+                       8 * p * ctx->opt.n_types, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return BMG_OK;
+  API_END
+}
+
+extern "C" bmg_status bmg_get_last_scan(bmg_ctx* ctx, uint32_t chain, double* p_r, double* p_r_types)
+{
+  if (!ctx) return BMG_EINVAL;
+  API_BEGIN
+  check_ready(ctx);
+  if (chain >= ctx->C) throw bmg_error(BMG_EINVAL, "chain index");
+  const size_t p = ctx->p;
+  if (p_r) CK(cudaMemcpyAsync(p_r, ctx->K.p_r + chain * p, 8 * p, cudaMemcpyDeviceToHost, ctx->stream));
+  if (p_r_types && ctx->opt.n_types > 1)
+    CK(cudaMemcpyAsync(p_r_types, ctx->K.p_r_types + chain * p * ctx->opt.n_types, 8 * p * ctx->opt.n_types,
                        cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   return BMG_OK;

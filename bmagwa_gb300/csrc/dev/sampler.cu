@@ -53,6 +53,7 @@ struct MoveShared {
   double bd[8][6];
   double bsum[6];
   long long bsuml[2];
+  double bmax[8];
   int bulk_mode;
   int bulk_s;           // fixed-point exponent of the bulk phase
   int bulk_nterm;       // genotype columns in the bulk phase
@@ -1308,14 +1309,25 @@ struct Warp {
       pms = fmax(fmin(pms, 0.99), 0.01);
       if (lane == 0) { ch->n_acpt[0] = 1; ch->n_moves[0] = 2; }
     } else {
+      // Evaluated without FMA contraction, with pow() from the host table, so
+      // that equal inputs give the reference's rounding: when one move size
+      // has data the criterion is flat in p and rounding picks the grid point.
       double q = 1 - pms;
-      double zp = 1 - pow(q, (double)mx);
+      double pw = K.ms_pow[50];
+      for (int j = 0; j < 50; ++j)
+        if (K.ms_grid[j] == pms) { pw = K.ms_pow[j]; break; }
+      if (pms != K.ms_init && pw == K.ms_pow[50]) {
+        bool found = false;
+        for (int j = 0; j < 50; ++j) found = found || (K.ms_grid[j] == pms);
+        if (!found) pw = pow(q, (double)mx);
+      }
+      double zp = 1 - pw;
       double q_p = pms / zp;
       for (int i = 0; i < mx; ++i) {
-        double nv = q_p0[i] + q_p;
+        double nv = __dadd_rn(q_p0[i], q_p);
         __syncwarp();
         if (lane == 0) q_p0[i] = nv;
-        q_p *= q;
+        q_p = __dmul_rn(q_p, q);
       }
       __syncwarp();
       double p_best = 0.01, pp = 0.01, h_best = -INFINITY;
@@ -1323,14 +1335,14 @@ struct Warp {
       for (int j = 0; j < 50; ++j) {
         double h = 0.0, z = 0.0, qq = 1.0 - pp, qp = pp;
         for (int i = 0; i < mx; ++i) {
-          double ratio = qp / q_p0[i];
-          h += (i + 1) * rs[i] * ratio;
-          z += rn[i] * ratio;
-          qp *= qq;
+          double ratio = __ddiv_rn(qp, q_p0[i]);
+          h = __dadd_rn(h, __dmul_rn(__dmul_rn((double)(i + 1), rs[i]), ratio));
+          z = __dadd_rn(z, __dmul_rn(rn[i], ratio));
+          qp = __dmul_rn(qp, qq);
         }
-        h /= z;
+        h = __ddiv_rn(h, z);
         if (h > h_best) { h_best = h; p_best = pp; }
-        pp += step;
+        pp = __dadd_rn(pp, step);
       }
       pms = p_best;
     }
@@ -1361,9 +1373,15 @@ __device__ void bulk_phase(const DevConst& K, int c, MoveShared& s, BulkCols& bc
   const int mode = s.bulk_mode, nt = s.bulk_nterm, sh = s.bulk_s;
   const int me = K.m_e;
   const double sc = ldexp(1.0, -sh);
-  double s1g = 0, s2g = 0, s1e = 0, s2e = 0, s1t = 0, s2t = 0;
+  double s1g = 0, s2g = 0, s1e = 0, s2e = 0, s1t = 0, s2t = 0, ymax = 0;
   long long rsum = 0;
   const uint32_t L = K.limbs_n;
+  // Model::compute_pve (src/model.hpp:359-371) leaves y_hat untouched before
+  // adding E beta_E when the model has no genotype term and there are
+  // covariates, so y_hat then accumulates; the scan reads that y_hat
+  // (src/sampler.cpp:735).  The same update is reproduced here.
+  const bool stale = (nt == 0) && (me > 1);
+  double* yhat = K.yhat + (size_t)c * K.n;
   for (uint64_t i = tid; i < K.n_pad; i += nth) {
     long long yg = 0;
     double ye = 0;
@@ -1383,6 +1401,12 @@ __device__ void bulk_phase(const DevConst& K, int c, MoveShared& s, BulkCols& bc
       }
     }
     double ygd = (double)yg * sc;
+    double yh = 0;
+    if (live && (mode & BULK_PVE)) {
+      yh = stale ? yhat[i] + ye : ygd + ye;
+      yhat[i] = yh;
+      ymax = fmax(ymax, fabs(yh));
+    }
     if (live && (mode & (BULK_PVE | BULK_ALPHA))) {
       s1g += ygd;
       s2g += ygd * ygd;
@@ -1403,8 +1427,13 @@ __device__ void bulk_phase(const DevConst& K, int c, MoveShared& s, BulkCols& bc
         long long Y = K.yint[i];
         int d = K.sy - sh;
         long long Ys = (d > 0) ? ((Y + (1ll << (d - 1))) >> d) : (Y << (-d));
-        long long E = (me > 1) ? __double2ll_rn(ye * ldexp(1.0, sh)) : s.bulk_b0i;
-        R = Ys - E - yg;
+        if (stale) {
+          double yv = (mode & BULK_PVE) ? yh : yhat[i];
+          R = Ys - __double2ll_rn(yv * ldexp(1.0, sh));
+        } else {
+          long long E = (me > 1) ? __double2ll_rn(ye * ldexp(1.0, sh)) : s.bulk_b0i;
+          R = Ys - E - yg;
+        }
         K.resid[(size_t)c * K.n_pad + i] = R;
       }
       rsum += R;
@@ -1428,6 +1457,8 @@ __device__ void bulk_phase(const DevConst& K, int c, MoveShared& s, BulkCols& bc
   }
   long long rs = warp_sum_ll(rsum);
   if (ln == 0) s.bl[w][0] = rs;
+  for (int o = 16; o > 0; o >>= 1) ymax = fmax(ymax, __shfl_xor_sync(FULL_MASK, ymax, o));
+  if (ln == 0) s.bmax[w] = ymax;
   __syncthreads();
   if (tid == 0) {
     for (int q = 0; q < 6; ++q) {
@@ -1438,6 +1469,11 @@ __device__ void bulk_phase(const DevConst& K, int c, MoveShared& s, BulkCols& bc
     long long t = 0;
     for (int ww = 0; ww < (nth >> 5); ++ww) t += s.bl[ww][0];
     s.bsuml[0] = t;
+    if (mode & BULK_PVE) {
+      double m = 0;
+      for (int ww = 0; ww < (nth >> 5); ++ww) m = fmax(m, s.bmax[ww]);
+      K.ch[c].yhat_absmax = m;
+    }
   }
   __syncthreads();
 }
@@ -1459,6 +1495,7 @@ __device__ void bulk_setup(Warp& W, BulkCols& bc, int mode)
     double eb = 0;
     for (int e = 0; e < me && e < bl; ++e) eb += K.e_absmax[e] * fabs(M->beta[e]);
     double tot = bound + K.y_absmax + eb + 1e-300;
+    if (nt == 0 && me > 1) tot += W.ch->yhat_absmax;  // the accumulated y_hat
     int e2 = (int)ceil(log2(tot));
     sh = (int)(8 * K.limbs_n - 3) - e2;
   } else {
@@ -1517,7 +1554,15 @@ __device__ void prep_rb(Warp& W, bool scan_only)
       ch->n_rao_burnin = burn;
     }
   }
+  // per-SNP tau2 draws of the scan (src/sampler.cpp:99-106) take p * terms
+  // consecutive slots, one per (SNP, allowed term) in the reference's order
+  uint64_t slot0 = W.rng.slot;
+  if (do_scan && K.use_individual_tau2) W.rng.slot += K.p * (uint64_t)K.n_terms;
   if (W.lane == 0) {
+    rp->alpha2 = ch->alpha2;
+    rp->rng_slot = slot0;
+    rp->key0 = W.rng.key0;
+    rp->key1 = W.rng.key1;
     rp->do_scan = do_scan;
     rp->acc_rao = acc_rao;
     rp->adapt = adapt && !K.flat_proposal_dist;
@@ -1592,7 +1637,10 @@ bmg_rbprep_kernel(DevConst K)
   if (tid < 32) bulk_setup(W, bc, BULK_RESID);
   __syncthreads();
   bulk_phase(K, c, s, bc);
-  if (tid < 32) prep_rb(W, true);
+  if (tid < 32) {
+    prep_rb(W, true);
+    if (W.lane == 0) K.ch[c].rng = W.rng;
+  }
 }
 
 // Runs iterations of chain blockIdx.x until `max_iters` are done or an RB

@@ -24,6 +24,18 @@ __device__ void rb_epilogue(const DevConst& K, int c, uint64_t j, const long lon
   for (int t = 0; t < 4; ++t) xr[t] = (double)xr_by_type[t] * rp.scale;
   double mr = rp.mr;
   double itv[4] = {rp.itv[0], rp.itv[1], rp.itv[2], rp.itv[3]};
+  if (K.use_individual_tau2) {
+    // Prior::sample_single_inv_tau2_from_prior_times_alpha2 (src/prior.hpp:192-199)
+    // with Rand::rand_sinvchi2(nu, s2) (src/rand.hpp:85-97); slot of (j, term u)
+    uint64_t slot = rp.rng_slot + j * (uint64_t)K.n_terms;
+    for (int t = 0; t < 4; ++t) {
+      if (!K.allow_terms[t]) continue;
+      double nu = K.nu_tau2[t];
+      double g = bmg_gamma_at(rp.key0, rp.key1, slot++, 0.5 * nu);
+      double val = nu * K.s2_tau2[t] / (2.0 * g);
+      itv[t] = 1.0 / (rp.alpha2 * val);
+    }
+  }
   const double* lmp = rp.lmp_add;
   if (in_model(K, c, j)) {
     const DevModel& M = K.cur[c];

@@ -69,6 +69,7 @@ struct DevChain {
   double p_move_size;
   double k_move_size;
   double pves[3];
+  double yhat_absmax;         // max |y_hat| after the last PVE pass
   int started;
   int movesize;
   int error;                  // 0 = fine; see BMG_DERR_*
@@ -110,6 +111,9 @@ struct RbParams {
   double lmp_rem[5][5];
   double rao_z1, rao_z2;    // running-mean weights of p_rao
   double prop_z1, prop_z2;  // running-mean weights of p_proposal
+  double alpha2;            // Prior::alpha2_ for per-SNP tau2 draws
+  uint64_t rng_slot;        // first stream slot of the per-SNP tau2 draws
+  uint32_t key0, key1;      // chain stream key
   int do_scan;              // compute p_r at all this step
   int acc_rao;              // n_rao_burnin <= 0: accumulate p_rao
   int adapt;                // update p_proposal and the proposal weights
@@ -181,6 +185,12 @@ struct DevConst {
   const double* tab;
   uint32_t tw;
   int32_t qs;           // fixed-point exponent of the dd_add weights
+  // move-size adaptation (src/sampler.hpp:1728-1769): the 50 grid values of p
+  // the reference visits (p = 0.01; p += 0.98 / 49) and pow(1 - p, max_ms) for
+  // each grid value [0..49] and for the initial p_move_size [50], by the host libm
+  const double* ms_grid;
+  const double* ms_pow;
+  double ms_init;
   // data
   const uint8_t* geno;
   const int32_t* cnt;   // p x 2
@@ -223,6 +233,7 @@ struct DevConst {
   uint32_t* basebits;   // chains x ceil(p/32): zeroed in the cadd base
   int32_t* model_inds;  // chains x p: current model's index or -1
   int64_t* resid;       // chains x n_pad: fixed-point residual of the last RB step
+  double* yhat;         // chains x n: Model::y_hat as compute_pve leaves it
   uint16_t* limbs;      // (chains * L) x n_pad bf16 residual limbs (scan B operand)
   uint32_t n_pad;       // individuals padded to the scan's K multiple
   uint32_t limbs_n;     // L

@@ -217,6 +217,7 @@ typedef struct bmg_chain_state {
   uint64_t n_iter;
   uint64_t n_accepted;
   double p_move_size;
+  uint64_t rng_draws;     /* logical random draws so far (the stream position) */
 } bmg_chain_state;
 
 /* loci (capacity loci_cap) receives the model's SNPs in model order. */
@@ -226,6 +227,15 @@ bmg_status bmg_get_state(bmg_ctx* ctx, uint32_t chain, bmg_chain_state* st,
 /* Rao-Blackwellised posterior of a chain (the _rao.dat / _rao_types.dat
  * payloads, src/sampler.cpp:846-858).  p_rao_types may be NULL. */
 bmg_status bmg_get_rao(bmg_ctx* ctx, uint32_t chain, double* p_rao, double* p_rao_types);
+
+/* Adaptive proposal of a chain: the running mean p_proposal of the
+ * Rao-Blackwellised probabilities that sets the add/remove weights
+ * (Sampler::save_p_proposal, src/sampler.hpp:363-383).  p_prop_types may be NULL. */
+bmg_status bmg_get_proposal(bmg_ctx* ctx, uint32_t chain, double* p_prop, double* p_prop_types);
+
+/* Rao-Blackwellised probabilities of the last scan inside bmg_run (the
+ * p_r_ the reference averages, src/sampler.cpp:731-757).  p_r_types may be NULL. */
+bmg_status bmg_get_last_scan(bmg_ctx* ctx, uint32_t chain, double* p_r, double* p_r_types);
 
 /* Write a chain's _rao.dat, _rao_types.dat, _samplerstats.txt and _prior.txt
  * under opt.basename (src/sampler.cpp:838-858, src/sampler.hpp:384-390). */

@@ -39,16 +39,24 @@ def build_reference():
 def lib():
     global _lib
     if _lib is None:
-        if not os.path.exists(PORT_LIB):
+        srcs = [os.path.join(HERE, "port", "port.cpp"), os.path.join(HERE, "port", "port.h"),
+                os.path.join(HERE, "linalg.c"), os.path.join(HERE, "..", "include", "bmg_rng.h"),
+                os.path.join(HERE, "..", "include", "bmg.h")]
+        if not os.path.exists(PORT_LIB) or any(os.path.getmtime(s) > os.path.getmtime(PORT_LIB)
+                                               for s in srcs):
             build()
         L = C.CDLL(PORT_LIB)
         L.bmgport_create.argtypes = [C.POINTER(abi.Options), C.c_void_p, C.c_void_p, C.c_void_p,
                                      C.POINTER(C.c_void_p), C.c_char_p, C.c_size_t]
         L.bmgport_run.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32, C.POINTER(abi.TraceSink)]
         L.bmgport_scan.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]
+        L.bmgport_scan_yhat.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_double, C.c_void_p,
+                                        C.c_void_p]
         L.bmgport_get_state.argtypes = [C.c_void_p, C.c_uint32, C.POINTER(abi.ChainState),
                                         C.c_void_p, C.c_void_p, C.c_uint32]
         L.bmgport_get_rao.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]
+        L.bmgport_get_last_scan.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]
+        L.bmgport_get_proposal.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]
         L.bmgport_get_precomputed.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(C.c_uint32)]
         L.bmgport_get_data_stats.argtypes = [C.c_void_p, C.c_void_p]
         L.bmgport_get_genotypes.argtypes = [C.c_void_p, C.c_uint32, C.c_uint64, C.c_void_p]
@@ -100,6 +108,14 @@ class Port:
             raise RuntimeError("oracle scan failed")
         return pr, (prt.reshape(self.m_g, self.n_types) if prt is not None else None)
 
+    def scan_yhat(self, y_hat, sigma2, chain=0):
+        pr = np.zeros(self.m_g)
+        prt = np.zeros(self.m_g * self.n_types) if self.n_types > 1 else None
+        yh = np.ascontiguousarray(y_hat, dtype=np.float64)
+        if lib().bmgport_scan_yhat(self.h, chain, _ptr(yh), float(sigma2), _ptr(pr), _ptr(prt)) != 0:
+            raise RuntimeError("oracle scan failed")
+        return pr, (prt.reshape(self.m_g, self.n_types) if prt is not None else None)
+
     def state(self, chain=0, cap=4096):
         st = abi.ChainState()
         loci = np.zeros(cap, dtype=np.uint32)
@@ -112,6 +128,18 @@ class Port:
         p = np.zeros(self.m_g)
         pt = np.zeros(self.m_g * self.n_types) if self.n_types > 1 else None
         lib().bmgport_get_rao(self.h, chain, _ptr(p), _ptr(pt))
+        return p, (pt.reshape(self.m_g, self.n_types) if pt is not None else None)
+
+    def last_scan(self, chain=0):
+        p = np.zeros(self.m_g)
+        pt = np.zeros(self.m_g * self.n_types) if self.n_types > 1 else None
+        lib().bmgport_get_last_scan(self.h, chain, _ptr(p), _ptr(pt))
+        return p, (pt.reshape(self.m_g, self.n_types) if pt is not None else None)
+
+    def proposal(self, chain=0):
+        p = np.zeros(self.m_g)
+        pt = np.zeros(self.m_g * self.n_types) if self.n_types > 1 else None
+        lib().bmgport_get_proposal(self.h, chain, _ptr(p), _ptr(pt))
         return p, (pt.reshape(self.m_g, self.n_types) if pt is not None else None)
 
     def precomputed(self):

@@ -1971,6 +1971,22 @@ extern "C" int bmgport_scan(bmgport* P, uint32_t chain, double* p_r, double* p_r
   }
 }
 
+extern "C" int bmgport_scan_yhat(bmgport* P, uint32_t chain, const double* y_hat, double sigma2,
+                                 double* p_r, double* p_r_types)
+{
+  try {
+    Sampler* s = P->p.chains.at(chain);
+    std::vector<double> yh(y_hat, y_hat + s->data->n);
+    s->cur->sigma2 = sigma2;
+    std::vector<double> prt(s->use_types ? s->m_g * s->n_types : 1);
+    s->p_raoblackwell(yh, p_r, prt.data());
+    if (p_r_types && s->use_types) std::memcpy(p_r_types, prt.data(), prt.size() * sizeof(double));
+    return 0;
+  } catch (...) {
+    return 1;
+  }
+}
+
 extern "C" int bmgport_get_state(bmgport* P, uint32_t chain, bmg_chain_state* st, uint32_t* loci,
                                  uint8_t* type_inds, uint32_t cap)
 {
@@ -1984,6 +2000,7 @@ extern "C" int bmgport_get_state(bmgport* P, uint32_t chain, bmg_chain_state* st
   st->n_iter = s->n_iter;
   st->n_accepted = s->n_accepted;
   st->p_move_size = s->p_move_size;
+  st->rng_draws = s->rng.st.slot;
   for (uint32_t i = 0; i < st->model_size && i < cap; ++i) {
     if (loci) loci[i] = s->cur->loci[i];
     if (type_inds) type_inds[i] = s->cur->type_inds[i];
@@ -1998,6 +2015,25 @@ extern "C" int bmgport_get_rao(bmgport* P, uint32_t chain, double* p_rao, double
   std::memcpy(p_rao, s->p_rao.data(), s->m_g * sizeof(double));
   if (p_rao_types && s->use_types)
     std::memcpy(p_rao_types, s->p_rao_types.data(), s->p_rao_types.size() * sizeof(double));
+  return 0;
+}
+
+extern "C" int bmgport_get_proposal(bmgport* P, uint32_t chain, double* p_prop, double* p_prop_types)
+{
+  if (chain >= P->p.chains.size()) return 1;
+  Sampler* s = P->p.chains[chain];
+  std::memcpy(p_prop, s->p_proposal.data(), s->m_g * sizeof(double));
+  if (p_prop_types && s->use_types)
+    std::memcpy(p_prop_types, s->p_proposal_types.data(), s->p_proposal_types.size() * sizeof(double));
+  return 0;
+}
+
+extern "C" int bmgport_get_last_scan(bmgport* P, uint32_t chain, double* p_r, double* p_r_types)
+{
+  if (chain >= P->p.chains.size()) return 1;
+  Sampler* s = P->p.chains[chain];
+  std::memcpy(p_r, s->p_r.data(), s->m_g * sizeof(double));
+  if (p_r_types && s->use_types) std::memcpy(p_r_types, s->p_r_types.data(), s->p_r_types.size() * sizeof(double));
   return 0;
 }
 

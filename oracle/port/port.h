@@ -33,9 +33,16 @@ int bmgport_run(bmgport* P, uint64_t n_iter, uint32_t n_threads,
                 const bmg_trace_sink* sink);
 /* RB scan of one chain against y - y_hat of its current model */
 int bmgport_scan(bmgport* P, uint32_t chain, double* p_r, double* p_r_types);
+/* RB scan of one chain against y - y_hat with sigma2 replaced (known-answer tests) */
+int bmgport_scan_yhat(bmgport* P, uint32_t chain, const double* y_hat, double sigma2,
+                      double* p_r, double* p_r_types);
 int bmgport_get_state(bmgport* P, uint32_t chain, bmg_chain_state* st,
                       uint32_t* loci, uint8_t* type_inds, uint32_t cap);
 int bmgport_get_rao(bmgport* P, uint32_t chain, double* p_rao, double* p_rao_types);
+/* the adaptive proposal p_proposal (src/sampler.hpp:363-383) */
+int bmgport_get_proposal(bmgport* P, uint32_t chain, double* p_prop, double* p_prop_types);
+/* p_r of the last in-loop RB scan (src/sampler.cpp:731-757) */
+int bmgport_get_last_scan(bmgport* P, uint32_t chain, double* p_r, double* p_r_types);
 int bmgport_get_precomputed(bmgport* P, double* xx, uint32_t* offset);
 /* var_x, mean_x, var_y, yy of the loaded data (src/data.hpp:66-71) */
 int bmgport_get_data_stats(bmgport* P, double* out4);

@@ -1,0 +1,186 @@
+"""Generate the golden fixtures of tests/golden/ from the reference itself.
+
+Runs only where the reference tree and its oracle build (oracle/_ref) exist:
+
+  1. known-answer vectors the reference's own tests hold, read as text from
+     src/tests/data_tests.hpp (genotype matrices and phenotypes of the two test
+     PLINK files), with the PLINK files themselves as byte arrays;
+  2. traces of the compiled reference (oracle/_ref/bmagwa_ref, the reference
+     sources built against oracle/shim) on small runs derived from the
+     reference's test configurations and its example dataset, with every
+     input file stored in the fixture.
+
+Usage:  python tests/golden/make_golden.py [REFERENCE_DIR]
+"""
+import os
+import re
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF_BIN = os.path.join(ROOT, "oracle", "_ref", "bmagwa_ref")
+
+TRACE_FILES = {
+    "jumpdistance": np.uint8, "move_type": np.uint8, "move_size": np.uint8,
+    "modelsize": np.uint32, "loci": np.uint32, "log_likelihood": np.float64,
+    "log_prior": np.float64, "sigma2": np.float64, "alpha": np.float64, "pve": np.float64,
+    "rao": np.float64, "types": np.uint8, "rao_types": np.float64,
+}
+
+
+def parse_matrix(text, name):
+    """Values of `const char name[..][..] = {{...},...};` in a C++ test file."""
+    m = re.search(r"%s\[(\d+)\]\[(\d+)\]\s*=\s*\{(.*?)\};" % name, text, re.S)
+    rows, cols = int(m.group(1)), int(m.group(2))
+    vals = [int(v) for v in re.findall(r"-?\d+", m.group(3))]
+    return np.array(vals, dtype=np.int8).reshape(rows, cols)
+
+
+def known_answers():
+    text = open(os.path.join(REF, "src/tests/data_tests.hpp")).read()
+    first, second = text.split("LoadAndHandlePlinkDataWithMissing")
+    g7 = parse_matrix(first, "genotypes")
+    ym = re.search(r"const double y\[30\]\s*=\s*\{(.*?)\};", first, re.S)
+    y30 = np.array([float(v) for v in ym.group(1).replace("\n", " ").split(",")])
+    g10 = parse_matrix(second, "genotypes")
+    tdir = os.path.join(REF, "src/tests/testdata")
+    rd = lambda f: np.frombuffer(open(os.path.join(tdir, f), "rb").read(), dtype=np.uint8)
+    np.savez_compressed(os.path.join(HERE, "data_tests.npz"),
+                        small_bed=rd("small_modelspace.bed"), small_fam=rd("small_modelspace.fam"),
+                        small_genotypes=g7, small_y=y30,
+                        plink_bed=rd("plinktest.bed"), plink_fam=rd("plinktest.fam"),
+                        plink_genotypes=g10)
+
+
+INI = """[datafiles]
+file_fam = {{DIR}}/data.fam
+file_g = {{DIR}}/data.bed
+{efile}{yfile}recode_g_to_minor_allele_count = {recode}
+[sizes]
+n = {n}
+m_g = {p}
+m_e = {m_e}
+[sampler]
+type = PMV
+do_n_iter = {iters}
+n_rao = {n_rao}
+n_rao_burnin = {burnin}
+adaptation = {adaptation}
+verbosity = {verbosity}
+thin = {thin}
+n_sample_tau2_and_missing = {nst}
+delay_rejection = 0
+p_move_size = 0.2
+p_move_size_nbc = 0.25
+p_move_size_nbs = 0.7
+max_SNP_neighborhood_size = {nbh}
+adapt_p_move_size = 1
+p_move_size_acpt_goal = {acpt}
+max_move_size = {maxms}
+flat_proposal_dist = 0
+[thread]
+n_threads = {chains}
+basename = {{DIR}}/out/chain
+seeds = {seeds}
+[model]
+types = {types}
+[prior]
+use_individual_tau2 = {indiv}
+type_A = 1
+type_H = 1
+type_D = 1
+type_R = 1
+type_AH = 1
+e_qg = {e_qg}
+var_qg = {var_qg}
+R2mode_sigma2 = 0.2
+nu_sigma2 = 1
+nu_tau2_A = 5
+s2_tau2_A = 0.05
+nu_tau2_H = 5
+s2_tau2_H = 0.05
+nu_tau2_D = 5
+eh_tau2_D = 0.1
+nu_tau2_R = 5
+eh_tau2_R = 0.1
+mu_alpha = 1
+inv_tau2_e_const_val = 0
+inv_tau2_e_val = 0.001
+"""
+
+
+def run_case(name, files, **kw):
+    kw.setdefault("efile", "")
+    kw.setdefault("yfile", "")
+    kw.setdefault("m_e", 0)
+    kw.setdefault("recode", 1)
+    kw.setdefault("adaptation", 0)
+    kw.setdefault("verbosity", 0)
+    kw.setdefault("acpt", 0)
+    kw.setdefault("nbh", 20)
+    kw.setdefault("maxms", 20)
+    kw.setdefault("indiv", 0)
+    ini = INI.format(**kw)
+    with tempfile.TemporaryDirectory() as d:
+        for fn, data in files.items():
+            with open(os.path.join(d, fn), "wb") as f:
+                f.write(bytes(data))
+        os.makedirs(os.path.join(d, "out"))
+        ipath = os.path.join(d, "run.ini")
+        with open(ipath, "w") as f:
+            f.write(ini.replace("{DIR}", d))
+        subprocess.run([REF_BIN, ipath], check=True, capture_output=True)
+        out = {"ini": np.frombuffer(ini.encode(), dtype=np.uint8)}
+        for fn, data in files.items():
+            out["file_" + fn.replace(".", "_")] = np.asarray(data, dtype=np.uint8)
+        for c in range(kw["chains"]):
+            for key, dt in TRACE_FILES.items():
+                path = os.path.join(d, "out", "chain%d_%s.dat" % (c, key))
+                if os.path.exists(path):
+                    out["c%d_%s" % (c, key)] = np.fromfile(path, dtype=dt)
+    np.savez_compressed(os.path.join(HERE, "ref_%s.npz" % name), **out)
+
+
+def main():
+    if not os.path.exists(REF_BIN):
+        raise SystemExit("build oracle/_ref first (make -C oracle)")
+    known_answers()
+    tdir = os.path.join(REF, "src/tests/testdata")
+    rd = lambda path: np.frombuffer(open(path, "rb").read(), dtype=np.uint8)
+    small = {"data.bed": rd(os.path.join(tdir, "small_modelspace.bed")),
+             "data.fam": rd(os.path.join(tdir, "small_modelspace.fam"))}
+    # the exhaustive-posterior test setting (src/tests/testdata/small_modelspace_tau2.ini),
+    # shortened and with delayed rejection off
+    run_case("small", small, n=30, p=7, iters=3000, n_rao=10, burnin=50, thin=5, nst=10,
+             chains=2, seeds="1245,77", types="A", e_qg=2, var_qg=2)
+    run_case("small_types", small, n=30, p=7, iters=2000, n_rao=10, burnin=20, thin=2, nst=6,
+             chains=1, seeds="99", types="A,AH", e_qg=2, var_qg=2, indiv=1, maxms=5, nbh=3)
+    # the example dataset (testdata/testdata.ini): first 1500 SNPs, its covariate
+    # and alternate phenotype files, individual tau2, n_rao 10
+    ex = os.path.join(REF, "testdata")
+    bed = rd(os.path.join(ex, "testdata.bed"))
+    n = 1000
+    stride = (n + 3) // 4
+    p = 1500
+    sub = np.concatenate([bed[:3], bed[3:3 + p * stride]])
+    files = {"data.bed": sub, "data.fam": rd(os.path.join(ex, "testdata.fam")),
+             "data.e": rd(os.path.join(ex, "testdata.e")), "data.y": rd(os.path.join(ex, "testdata.y"))}
+    run_case("example", files, n=n, p=p, iters=600, n_rao=10, burnin=20, thin=10, nst=10,
+             chains=2, seeds="1234,2345", types="A", e_qg=20, var_qg=300, m_e=2,
+             efile="file_e = {DIR}/data.e\n", yfile="file_y = {DIR}/data.y\n", indiv=1,
+             verbosity=100)
+    run_case("example_types", files, n=n, p=p, iters=400, n_rao=20, burnin=5, thin=4, nst=8,
+             chains=1, seeds="4321", types="A,H,D,R,AH", e_qg=20, var_qg=300, m_e=2,
+             efile="file_e = {DIR}/data.e\n", yfile="file_y = {DIR}/data.y\n", adaptation=1, acpt=0.3)
+    for f in sorted(os.listdir(HERE)):
+        if f.endswith(".npz"):
+            print(f, os.path.getsize(os.path.join(HERE, f)))
+
+
+if __name__ == "__main__":
+    main()

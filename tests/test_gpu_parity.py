@@ -1,0 +1,119 @@
+"""GPU sampler parity: against traces of the reference itself (tests/golden)
+and against the CPU oracle on synthetic data, same seeds, same random stream.
+
+Integer traces (moves, sizes, model sizes, loci, types) must be identical;
+floating-point traces and the Rao-Blackwellised posteriors agree to 1e-9
+relative (the spec LML tolerance)."""
+import numpy as np
+import pytest
+
+import helpers as H
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-9
+
+
+def run_gpu(bg, opt, packed, y, e, n_iter):
+    ctx = bg.Context(opt)
+    ctx.load_bed(packed)
+    ctx.set_phenotypes(y)
+    ctx.set_covariates(e)
+    ctx.precompute()
+    col = ctx.run(n_iter)
+    return ctx, col
+
+
+@pytest.mark.parametrize("scan", [1, 0], ids=["simt", "tcgen05"])
+@pytest.mark.parametrize("name", ["small", "small_types", "example", "example_types"])
+def test_gpu_matches_reference(bmg, tmp_path, name, scan):
+    z = H.golden("ref_" + name)
+    ini = H.materialize(z, tmp_path)
+    opt = bmg.options_from_ini(ini)
+    opt.scan_impl = scan
+    packed, y, e = bmg.read_plink(opt)
+    ctx, col = run_gpu(bmg, opt, packed, y, e, opt.do_n_iter)
+    for c in range(opt.n_chains):
+        ref = H.ref_chain(z, c)
+        H.compare(ref, col.chain(c), rtol=RTOL, label="%s chain %d" % (name, c))
+        rao, raot = ctx.rao(c)
+        np.testing.assert_allclose(rao, ref["rao"], rtol=RTOL, atol=1e-12)
+        if raot is not None:
+            np.testing.assert_allclose(raot.reshape(-1), ref["rao_types"], rtol=RTOL, atol=1e-12)
+
+
+def synth_case(bg, tmp_path, name, **kw):
+    from bmagwa_gb300 import synth
+    ini = synth.make_dataset(name, str(tmp_path), **kw)
+    opt = bg.options_from_ini(ini)
+    packed, y, e = bg.read_plink(opt)
+    return opt, packed, y, e
+
+
+@pytest.mark.parametrize("case", [
+    dict(name="plain", n=700, p=3000, chains=2, iters=300, n_rao=1),
+    dict(name="batched", n=900, p=4000, chains=3, iters=300, n_rao=5),
+    dict(name="plain", n=1500, p=2500, chains=1, iters=500, n_rao=25),
+], ids=["rb_every_iter", "ld_types", "sparse_rb"])
+def test_gpu_matches_oracle_synthetic(bmg, oracle, tmp_path, case):
+    case = dict(case)
+    iters = case.pop("iters")
+    opt, packed, y, e = synth_case(bmg, tmp_path, iters=iters, **case)
+    port = oracle.Port(opt, packed, y, e)
+    colp = port.run(iters)
+    ctx, colg = run_gpu(bmg, opt, packed, y, e, iters)
+    for c in range(opt.n_chains):
+        H.compare(colp.chain(c), colg.chain(c), rtol=RTOL, label="chain %d" % c)
+        np.testing.assert_allclose(ctx.rao(c)[0], port.rao(c)[0], rtol=RTOL, atol=1e-12)
+
+
+def test_gpu_chunked_run_equals_single_run(bmg, tmp_path):
+    """bmg_run(a) + bmg_run(b) is one sample() of a + b iterations."""
+    opt, packed, y, e = synth_case(bmg, tmp_path, name="plain", n=500, p=1500, chains=2, iters=200,
+                                   n_rao=7)
+    opt.graph_iters = 16
+    _, whole = run_gpu(bmg, opt, packed, y, e, 200)
+    ctx = bmg.Context(opt)
+    ctx.load_bed(packed)
+    ctx.set_phenotypes(y)
+    ctx.set_covariates(e)
+    ctx.precompute()
+    parts = [ctx.run(k) for k in (33, 100, 67)]
+    for c in range(2):
+        merged = {k: np.concatenate([p.chain(c)[k] for p in parts]) for k in whole.chain(c)}
+        H.compare(whole.chain(c), merged, rtol=0.0, label="chain %d" % c)
+
+
+def test_gpu_scan_matches_oracle(bmg, oracle, tmp_path):
+    """bmg_scan (RaoBlackwellizer::p_raoblackwell) at the state after a run."""
+    opt, packed, y, e = synth_case(bmg, tmp_path, name="batched", n=800, p=3000, chains=2, iters=120,
+                                   n_rao=10)
+    port = oracle.Port(opt, packed, y, e)
+    port.run(120)
+    for scan in (1, 0):
+        opt.scan_impl = scan
+        ctx, _ = run_gpu(bmg, opt, packed, y, e, 120)
+        pr, prt = ctx.scan()
+        for c in range(opt.n_chains):
+            ppr, pprt = port.scan(c)
+            np.testing.assert_allclose(pr[c], ppr, rtol=RTOL, atol=1e-13)
+            np.testing.assert_allclose(prt[c], pprt, rtol=RTOL, atol=1e-13)
+        port2 = oracle.Port(opt, packed, y, e)  # the oracle's scan consumed nothing here
+        port2.run(120)
+        port = port2
+
+
+def test_gpu_writes_reference_files(bmg, tmp_path):
+    """run_ini writes the reference's binary trace files, byte-compatible in layout."""
+    z = H.golden("ref_small")
+    ini = H.materialize(z, tmp_path)
+    bmg.run_ini(ini)
+    import oracle.port as op
+    for c in range(2):
+        out = op.read_ref_outputs(str(tmp_path / "out" / "chain"), c, 7)
+        ref = H.ref_chain(z, c)
+        H.compare(ref, out, rtol=RTOL, label="files chain %d" % c)
+        np.testing.assert_allclose(out["rao"], ref["rao"], rtol=RTOL, atol=1e-12)
+    assert (tmp_path / "out" / "chain0_log.txt").exists()
+    assert (tmp_path / "out" / "chain_prior.txt").exists()
+    assert (tmp_path / "out" / "chain1_samplerstats.txt").exists()

@@ -1,0 +1,183 @@
+"""The CPU oracle against the reference's known answers and traces.
+
+The oracle (oracle/port) is the checker of every GPU parity test, so it is
+pinned first: against the golden vectors of the reference's own tests
+(src/tests/*_tests.hpp) and against traces of the reference itself (the
+fixtures of tests/golden, made by tests/golden/make_golden.py)."""
+import ctypes as C
+import math
+
+import numpy as np
+import pytest
+
+import helpers as H
+
+
+def small_opts(bg, n, p, types, **kw):
+    o = bg.default_options()
+    o.n, o.m_g, o.m_e = n, p, 0
+    o.n_types = len(types)
+    for i, t in enumerate(sorted(types)):
+        o.types[i] = t
+    o.do_n_iter, o.n_rao, o.n_rao_burnin, o.thin, o.n_sample_tau2_and_missing = 100, 10, 1, 10, 10
+    o.e_qg, o.var_qg, o.nu_sigma2, o.s2_sigma2 = 2, 2, 1, 1
+    for t in range(4):
+        o.nu_tau2[t], o.s2_tau2[t] = 4, 1
+    o.mu_alpha = 1
+    for k, v in kw.items():
+        setattr(o, k, v)
+    bg.set_seeds(o, [1245])
+    return o
+
+
+def test_decode_known_answers(bmg, oracle):
+    """DataTests.LoadAndHandlePlinkData{NoMissing,WithMissing} (src/tests/data_tests.hpp:30-194)."""
+    z = H.golden("data_tests")
+    for bed, fam, gold, n, p in (("small_bed", "small_fam", "small_genotypes", 30, 7),
+                                 ("plink_bed", "plink_fam", "plink_genotypes", 5, 10)):
+        packed = z[bed][3:]
+        g = z[gold]
+        o = small_opts(bmg, n, p, [0])
+        port = oracle.Port(o, packed, np.zeros(n) + np.arange(n) * 0.1)
+        for j in range(p):
+            for term in range(4):
+                assert np.array_equal(port.genotypes(term, j), H.coding(g[j], term)), (bed, j, term)
+        assert np.array_equal(H.decode(packed, n, p), g)
+
+
+def test_phenotypes_known_answer(bmg, tmp_path):
+    """The .fam phenotypes of small_modelspace (src/tests/data_tests.hpp:44-75) via the product reader."""
+    z = H.golden("data_tests")
+    (tmp_path / "d.bed").write_bytes(z["small_bed"].tobytes())
+    (tmp_path / "d.fam").write_bytes(z["small_fam"].tobytes())
+    o = small_opts(bmg, 30, 7, [0])
+    bmg.abi.set_path(o, "file_fam", str(tmp_path / "d.fam"))
+    bmg.abi.set_path(o, "file_g", str(tmp_path / "d.bed"))
+    packed, y, _ = bmg.read_plink(o)
+    assert np.array_equal(y, z["small_y"])
+    assert np.array_equal(packed, z["small_bed"][3:])
+
+
+@pytest.mark.parametrize("types", [[0], [0, 4], [0, 1, 2, 3, 4]])
+def test_precomputed_covariances(bmg, oracle, types):
+    """PrecomputedSNPCovariancesTests (src/tests/precomputed_snp_covariances_tests.hpp:30-150)."""
+    z = H.golden("data_tests")
+    packed, n, p = z["plink_bed"][3:], 5, 10
+    o = small_opts(bmg, n, p, types)
+    port = oracle.Port(o, packed, np.linspace(-1, 1, n))
+    xx = port.precomputed()
+    g = H.decode(packed, n, p).astype(float)
+    g[g < 0] = 0  # missing values enter the precomputation as 0
+    terms = sorted({t for ty in types for t in ((0, 1) if ty == 4 else (ty,))})
+    for j in range(p):
+        col = 0
+        for t in terms:
+            x = H.coding(g[j], t)
+            assert xx[j, col] == pytest.approx(x.sum(), abs=1e-12)
+            assert xx[j, col + 1] == pytest.approx(x @ x - x.sum() ** 2 / n, abs=1e-10)
+            col += 2
+        if 4 in types:
+            a, h = H.coding(g[j], 0), H.coding(g[j], 1)
+            assert xx[j, -1] == pytest.approx(a @ h - a.sum() * h.sum() / n, abs=1e-10)
+
+
+def test_lml_known_answer(bmg, oracle):
+    """ModelTests.LikelihoodComputation (src/tests/model_tests.hpp:36-90): hand-computed LMLs."""
+    z = H.golden("data_tests")
+    packed, n = z["plink_bed"][3:], 5
+    fam = z["plink_fam"].tobytes().decode().split()
+    y = np.array([float(fam[6 * i + 5]) for i in range(n)])
+    o = small_opts(bmg, n, 10, [0, 4], e_qg=2, var_qg=4, nu_sigma2=4, s2_sigma2=1, mu_alpha=2,
+                   inv_tau2_e_const_val=0)
+    port = oracle.Port(o, packed, y)
+    tau2 = 4.0 * 1.0 / (4.0 - 2.0)
+    inv = 1.0 / (2.0 * 2.0 * tau2)
+    lml = port.model_lml([1, 5], [0, 1], [[inv, inv], [inv, inv]])
+    nu_s, s2_s = 4.0, 1.0
+    syy1 = 0.58 - 0.51670588235294123702
+    exp1 = -0.5 * math.log(tau2) - 0.5 * math.log(4.0 * 10.0 + 5.0 / tau2) \
+        - 0.5 * (nu_s + n) * math.log(nu_s * s2_s + syy1)
+    syy2 = 0.58 - 0.56537856592135671274
+    exp2 = -0.5 * 3.0 * math.log(tau2) - 0.5 * math.log(810.62499999999954525265) \
+        - 0.5 * (nu_s + n) * math.log(nu_s * s2_s + syy2)
+    assert lml[0] == pytest.approx(exp1, abs=1e-8)
+    assert lml[1] == pytest.approx(exp2, abs=1e-8)
+
+
+def test_lml_matches_numpy(bmg, oracle):
+    """Incremental Cholesky LML (src/model.hpp:432-506) equals a direct dense computation."""
+    rng = np.random.default_rng(3)
+    n, p = 80, 40
+    g = rng.integers(0, 3, size=(p, n))
+    code = np.where(g == 0, 0, np.where(g == 1, 2, 3)).astype(np.uint8)
+    pad = np.zeros((p, (n + 3) // 4 * 4), dtype=np.uint8)
+    pad[:, :n] = code
+    pad = pad.reshape(p, -1, 4)
+    packed = (pad[..., 0] | pad[..., 1] << 2 | pad[..., 2] << 4 | pad[..., 3] << 6).astype(np.uint8)
+    y = rng.normal(size=n)
+    o = small_opts(bmg, n, p, [0, 4], nu_sigma2=2, s2_sigma2=0.7, inv_tau2_e_const_val=0.01)
+    port = oracle.Port(o, packed.reshape(-1), y)
+    snps = [3, 17, 5, 30, 22]
+    tinds = [0, 1, 0, 1, 0]
+    invs = [[0.5, 0.25], [0.3, 0.4], [0.7, 0.7], [0.2, 0.9], [1.1, 1.1]]
+    lml = port.model_lml(snps, tinds, invs)
+    cols, precs = [np.ones(n)], [0.01]
+    for step, (s, t, iv) in enumerate(zip(snps, tinds, invs)):
+        cols.append(H.coding(g[s], 0))
+        precs.append(iv[0])
+        if t == 1:
+            cols.append(H.coding(g[s], 1))
+            precs.append(iv[1])
+        X = np.stack(cols, 1)
+        exp = H.lml_numpy(X, y, np.array(precs), 2 * 0.7 + y @ y, n + 2)
+        assert lml[step] == pytest.approx(exp, rel=1e-11)
+
+
+def test_rb_closed_form(bmg, oracle):
+    """RaoBlackwellizerTests.EmptyCurrentModel (src/tests/raoblackwellizer_tests.hpp:31-93)."""
+    z = H.golden("data_tests")
+    packed, n, p = z["small_bed"][3:], 30, 7
+    y = z["small_y"]
+    o = small_opts(bmg, n, p, [0], e_qg=2, var_qg=2, nu_sigma2=1, s2_sigma2=0, R2mode_sigma2=0.2,
+                   recode_g_to_minor_allele_count=1, inv_tau2_e_const_val=0)
+    o.nu_tau2[0], o.s2_tau2[0] = 3, 0.02
+    port = oracle.Port(o, packed, y)
+    sigma2 = 0.7318
+    pr, _ = port.scan_yhat(np.zeros(n), sigma2)
+    # recoded genotypes, shared tau2 at its prior initialisation, alpha = 1
+    g = H.decode(packed, n, p)
+    freq = g.sum(1) / (2.0 * n)
+    g = np.where(freq[:, None] > 0.5, np.where(g == 0, 2, np.where(g == 2, 0, g)), g).astype(float)
+    tau2 = 3 * 0.02 / max(0.1, 3 - 2)
+    inv = 1.0 / tau2
+    # beta-binomial hyper-parameters (src/prior.hpp:273-290) and the add change (:144-150)
+    z_ = (2 - 2 * (1 - 2)) / ((p - 1) * 2)
+    ga = (z_ - 1) / (1 - p * z_ / 2)
+    gb = (p / 2 - 1) * ga
+    lmp = (math.log(ga) - math.log(gb + p - 1)) + (math.log(1.0) - math.log(1.0))
+    for j in range(p):
+        x = g[j]
+        xx, yx, xs, rs = x @ x, y @ x, x.sum(), y.sum()
+        det = n * (xx + inv) - xs * xs
+        rxxr = (rs * rs * (xx + inv) - 2.0 * yx * rs * xs + yx * yx * n) / det
+        e = math.exp(0.5 * (math.log(n) - math.log(det)) + 0.5 * math.log(inv)
+                     - 0.5 * (rs * rs / n - rxxr) / sigma2 + lmp)
+        assert pr[j] == pytest.approx(e / (1 + e), abs=1e-10)
+
+
+@pytest.mark.parametrize("name", ["small", "small_types", "example", "example_types"])
+def test_oracle_matches_reference_traces(bmg, oracle, tmp_path, name):
+    """The oracle reproduces the compiled reference's traces bit for bit."""
+    z = H.golden("ref_" + name)
+    ini = H.materialize(z, tmp_path)
+    opt = bmg.options_from_ini(ini)
+    packed, y, e = bmg.read_plink(opt)
+    port = oracle.Port(opt, packed, y, e)
+    col = port.run(opt.do_n_iter)
+    for c in range(opt.n_chains):
+        ref = H.ref_chain(z, c)
+        H.compare(ref, col.chain(c), rtol=0.0, label="%s chain %d" % (name, c))
+        rao, raot = port.rao(c)
+        assert np.array_equal(rao, ref["rao"])
+        if raot is not None:
+            assert np.array_equal(raot.reshape(-1), ref["rao_types"])
