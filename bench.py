@@ -1,0 +1,328 @@
+"""Throughput of the MCMC over SNP inclusion on one GB300.
+
+Workload (default "scan"): n = 10,000 individuals, p = 500,000 SNPs of
+synthetic genotypes in LD blocks of 50 (AR(1) latent Gaussian, rho 0.8,
+thresholded to MAF ~ U(0.05, 0.5)), 30 causal SNPs, additive coding,
+32 chains, the Rao-Blackwellised scan of all SNPs every iteration (n_rao = 1),
+add/remove/swap moves with the adaptive proposal.
+
+A step is one MCMC iteration of every chain: the moves of all chains, the
+p-wide scan, the proposal update.  value = chain-iterations per second with the
+genotypes resident on the device; e2e = the same metric through the C ABI from
+host buffers (genotype upload, precompute, run, read-back of the traces and
+posteriors inside the timed region).
+
+--impl reference times the CPU restatement of the reference sampler
+(oracle/port) on the host cores on a bounded sample of the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np
+
+WORKLOADS = {
+    "scan": dict(n=10000, p=500000, chains=32, n_rao=1, ld_block=50, causal=30, types="A"),
+    "batched": dict(n=5000, p=50000, chains=8, n_rao=500, ld_block=50, causal=20, types="A,AH"),
+    "plain": dict(n=1000, p=5000, chains=1, n_rao=500, ld_block=0, causal=10, types="A"),
+}
+PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM = 6800.0
+
+
+def env_rank():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), \
+        int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def options(bg, wl, seed0, iters):
+    from bmagwa_gb300 import abi
+    o = bg.default_options()
+    o.n, o.m_g, o.m_e = wl["n"], wl["p"], 0
+    types = [abi.TYPE_NAMES[t] for t in wl["types"].split(",")]
+    o.n_types = len(types)
+    for i, t in enumerate(sorted(types)):
+        o.types[i] = t
+    o.do_n_iter = iters
+    o.n_rao = wl["n_rao"]
+    o.thin = 1 if wl["n_rao"] < 10 else 10
+    o.n_rao_burnin = max(1, iters // (2 * wl["n_rao"]))
+    o.n_sample_tau2_and_missing = 10
+    o.max_move_size = 20
+    o.max_SNP_neighborhood_size = 20
+    o.p_move_size, o.p_move_size_nbs, o.p_move_size_nbc = 0.2, 0.7, 0.25
+    o.e_qg, o.var_qg, o.nu_sigma2, o.R2mode_sigma2, o.mu_alpha = 20, 300, 1, 0.2, 1
+    o.inv_tau2_e_const_val, o.inv_tau2_e_val = 0.0, 0.001
+    for t in range(4):
+        o.nu_tau2[t], o.s2_tau2[t] = 5, 0.05
+    o.max_model_size = 256
+    o.graph_iters = 64
+    o.quiet = 1
+    bg.set_seeds(o, [seed0 + 1000 * c for c in range(wl["chains"])])
+    return o
+
+
+def make_data(wl, seed, device):
+    from bmagwa_gb300 import synth
+    counts, _ = synth.genotypes(wl["n"], wl["p"], wl["ld_block"], seed, device=device)
+    y, _, _ = synth.phenotype(counts, wl["causal"], 0.2, 0, seed, device=device)
+    packed = synth.pack(counts).cpu().numpy().reshape(-1)
+    del counts
+    return packed, y
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.stop = threading.Event()
+
+    def _run(self):
+        while not self.stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                     timeout=5).stdout.strip()
+                if out:
+                    self.rows.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self.stop.wait(0.2)
+
+    def __enter__(self):
+        self.t = threading.Thread(target=self._run, daemon=True)
+        self.t.start()
+        return self
+
+    def __exit__(self, *a):
+        self.stop.set()
+        self.t.join(timeout=10)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4)
+                          if len(r) > 5 + k and r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def peak_hbm():
+    try:
+        with open(PEAKS) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM, "fallback"
+
+
+def scan_traffic_per_launch(workload):
+    """DRAM bytes per scan launch from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", "scan_%s_ncu.md" % workload)
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+def cpu_sample(wl, packed, y, threads, iters, seed0):
+    """The oracle on the host cores: `threads` chains for `iters` iterations each."""
+    import bmagwa_gb300 as bg
+    import oracle.port as op
+    o = options(bg, wl, seed0, iters)
+    o.max_model_size = 1024
+    bg.set_seeds(o, [seed0 + 1000 * c for c in range(threads)])
+    port = op.Port(o, packed, y)
+    t0 = time.perf_counter()
+    port.run(iters, threads=threads)
+    dt = time.perf_counter() - t0
+    return threads * iters / dt, dt
+
+
+def run_gb300(args, wl):
+    import torch
+    import bmagwa_gb300 as bg
+    rank, world, local = env_rank()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    bg.build()
+    seed = 1 + 7919 * rank
+    packed, y = make_data(wl, seed, "cuda")
+    iters_total = args.warmup + args.steps
+    o = options(bg, wl, seed, iters_total)
+    o.scan_impl = args.scan
+    ctx = bg.Context(o)
+    ctx.load_bed(packed)
+    ctx.set_phenotypes(y)
+    ctx.set_covariates(None)
+    ctx.precompute()
+    ctx.run(args.warmup, collect=False)
+    torch.cuda.synchronize()
+    ctx.reset_timings()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    with clocks:
+        t0 = time.perf_counter()
+        ctx.run(args.steps, collect=False)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+    ms = ctx.timings()
+    n_scans = ctx.reset_timings()
+    dev_s = ms[3] / 1000.0
+    if world > 1:
+        t = torch.tensor([dev_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_s = float(t.item())
+        dist.barrier()
+    units = args.steps * wl["chains"] * world
+    value = units / dev_s
+    # e2e: the whole job through the C ABI from host buffers
+    o2 = options(bg, wl, seed + 17, iters_total)
+    o2.scan_impl = args.scan
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ctx2 = bg.Context(o2)
+    ctx2.load_bed(packed)
+    ctx2.set_phenotypes(y)
+    ctx2.set_covariates(None)
+    ctx2.precompute()
+    col = ctx2.run(args.steps, collect=True)
+    rao = [ctx2.rao(c)[0] for c in range(wl["chains"])]
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    d2h = sum(int(sum(a.nbytes for a in col.chain(c).values())) for c in range(wl["chains"]))
+    d2h += sum(r.nbytes for r in rao)
+    h2d = packed.nbytes + y.nbytes
+    ctx2.close()
+    # roofline of the scan kernel
+    p, n, C = wl["p"], wl["n"], wl["chains"]
+    scan_ms = ms[1] / max(1, n_scans)
+    alg_bytes = p * ((n + 3) // 4) + p * C * (8 + 16) + C * n * 8
+    peak, peak_kind = peak_hbm()
+    achieved = alg_bytes / (scan_ms / 1000.0) / 1e9 if scan_ms > 0 else None
+    out = {
+        "metric": "MCMC chain-iterations/s (RB scan of all SNPs every iteration)",
+        "value": value,
+        "unit": "iter/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1000.0 * dev_s / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64 (moves) / bf16-limb exact int (scan)" if args.scan == 0 else "f64 / int64",
+        "data": "synthetic (seeded LD-block genotypes and phenotypes)",
+        "config": {"workload": args.workload, "n": n, "p": p, "chains": C, "n_rao": wl["n_rao"],
+                   "types": wl["types"], "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "inputs larger than L2 (%.2f GB packed genotypes)" % (packed.nbytes / 1e9),
+                   "scan_impl": "tcgen05" if args.scan == 0 else "simt"},
+        "e2e": {"value": args.steps * C / e2e_s, "unit": "iter/s",
+                "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps},
+        "gpu_launches": int(args.steps * (1 + 2) + args.steps * (1 if args.scan == 1 else 0)),
+        "phase_ms": {"move": ms[0], "scan": ms[1], "rebuild": ms[2], "total": ms[3],
+                     "scans": n_scans, "wall_s": dt},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None,
+                     "traffic": scan_traffic_per_launch(args.workload),
+                     "kernel": "scan", "peak_kind": peak_kind, "scan_ms": scan_ms,
+                     "alg_bytes_per_launch": alg_bytes},
+        "clocks": clocks.summary(),
+    }
+    if rank == 0 and args.cpu_baseline:
+        threads = max(1, min(C, os.cpu_count() or 1))
+        cv, cdt = cpu_sample(wl, packed, y, threads, 1, seed)
+        out["cpu_baseline"] = {"value": cv, "unit": "iter/s", "cores": threads, "kind": "port",
+                               "sample": "%d chains x 1 iteration of the same workload (%.1f s)"
+                                         % (threads, cdt)}
+    if rank == 0:
+        print(json.dumps(out))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def run_reference(args, wl):
+    rank, world, _ = env_rank()
+    if rank != 0:
+        return
+    import bmagwa_gb300 as bg
+    import oracle.port as op
+    bg.build()
+    op.build()
+    seed = 1
+    packed, y = make_data(wl, seed, "cpu")
+    threads = max(1, min(wl["chains"], os.cpu_count() or 1))
+    o = options(bg, wl, seed, args.warmup + args.steps)
+    o.max_model_size = 1024
+    bg.set_seeds(o, [seed + 1000 * c for c in range(threads)])
+    port = op.Port(o, packed, y)
+    if args.warmup:
+        port.run(1, threads=threads)
+    # each step is one iteration of `threads` chains; stop after about a minute
+    done, dt = 0, 0.0
+    while done < args.steps and (done == 0 or dt < 60.0):
+        t0 = time.perf_counter()
+        port.run(1, threads=threads)
+        dt += time.perf_counter() - t0
+        done += 1
+    args.steps = done
+    v = done * threads / dt
+    print(json.dumps({
+        "impl": "reference",
+        "metric": "MCMC chain-iterations/s (RB scan of all SNPs every iteration)",
+        "value": v, "unit": "iter/s", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded LD-block genotypes and phenotypes)",
+        "config": {"workload": args.workload, "n": wl["n"], "p": wl["p"], "chains": threads,
+                   "n_rao": wl["n_rao"], "types": wl["types"]},
+        "cpu_baseline": {"value": v, "unit": "iter/s", "cores": threads, "kind": "port",
+                         "sample": "%d chains x %d iterations (one pthread per chain)" % (threads, args.steps)},
+        "e2e": {"value": v, "unit": "iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="scan", choices=sorted(WORKLOADS))
+    ap.add_argument("--scan", type=int, default=0, help="0 tcgen05, 1 SIMT")
+    ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        run_reference(args, wl)
+    else:
+        run_gb300(args, wl)
+
+
+if __name__ == "__main__":
+    main()

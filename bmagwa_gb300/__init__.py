@@ -61,6 +61,7 @@ def lib():
         L.bmg_finish.argtypes = [vp]
         L.bmg_get_timings.argtypes = [vp, vp]
         L.bmg_get_proposal.argtypes = [vp, u32, vp, vp]
+        L.bmg_reset_timings.argtypes = [vp, C.POINTER(u64)]
         L.bmg_get_last_scan.argtypes = [vp, u32, vp, vp]
         L.bmg_get_data_stats.argtypes = [vp, vp]
         L.bmg_last_error.argtypes = [vp]
@@ -72,7 +73,7 @@ def lib():
         for name in ("bmg_create", "bmg_load_bed", "bmg_set_phenotypes", "bmg_set_covariates",
                      "bmg_precompute", "bmg_get_precomputed", "bmg_scan", "bmg_run", "bmg_get_state",
                      "bmg_get_rao", "bmg_finish", "bmg_get_timings", "bmg_get_data_stats",
-                     "bmg_get_proposal", "bmg_get_last_scan"):
+                     "bmg_get_proposal", "bmg_get_last_scan", "bmg_reset_timings"):
             getattr(L, name).restype = C.c_int
         _lib = L
     return _lib
@@ -228,6 +229,11 @@ class Context:
         out = np.zeros(4)
         self._check(lib().bmg_get_timings(self.h, _ptr(out)))
         return out
+
+    def reset_timings(self):
+        n = C.c_uint64()
+        self._check(lib().bmg_reset_timings(self.h, C.byref(n)))
+        return n.value
 
     def finish(self):
         self._check(lib().bmg_finish(self.h))

@@ -77,6 +77,8 @@ struct bmg_ctx {
   std::vector<ChainFiles> files;
   std::vector<DevChain> ch_h;
   double ms[4] = {0, 0, 0, 0};
+  uint64_t n_scans = 0;
+  cudaEvent_t ev[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   uint64_t n_iter = 0;
   time_t t_start = 0;
   int max_ms = 0;
@@ -97,6 +99,8 @@ struct bmg_ctx {
   }
   ~bmg_ctx()
   {
+    for (cudaEvent_t e : ev)
+      if (e) cudaEventDestroy(e);
     for (void* a : allocs) cudaFree(a);
     if (stream) cudaStreamDestroy(stream);
   }
@@ -178,6 +182,7 @@ static void device_error_check(bmg_ctx* ctx)
       case BMG_DERR_TRACE: what = "trace buffer overflow"; st = BMG_ECUDA; break;
       case BMG_DERR_REMSET: what = "model too large for the removal proposal set"; st = BMG_EINVAL; break;
       case BMG_DERR_START: what = "Sampler cannot start from non-finite likelihood."; st = BMG_ENOTPD; break;
+      case BMG_DERR_TIMEOUT: what = "a bounded device wait gave up"; st = BMG_ETIMEOUT; break;
     }
     throw bmg_error(st, std::string(what) + " (chain " + std::to_string(c) + ")");
   }
@@ -899,6 +904,8 @@ extern "C" bmg_status bmg_run(bmg_ctx* ctx, uint64_t n_iter, const bmg_trace_sin
   DevConst& K = ctx->K;
   const uint64_t n_rao = ctx->opt.n_rao;
   const uint32_t gi = ctx->opt.graph_iters;
+  for (int q = 0; q < 4; ++q)
+    if (!ctx->ev[q]) CK(cudaEventCreate(&ctx->ev[q]));
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
@@ -913,14 +920,30 @@ extern "C" bmg_status bmg_run(bmg_ctx* ctx, uint64_t n_iter, const bmg_trace_sin
       uint64_t t = ctx->n_iter;
       uint64_t next_rb = ((t / n_rao) + 1) * n_rao - 1;  // first iter >= t with (iter+1) % n_rao == 0
       uint64_t seg = std::min<uint64_t>(chunk - i, next_rb - t + 1);
+      CK(cudaEventRecord(ctx->ev[0], ctx->stream));
       bmg_move_kernel<<<ctx->C, BMG_MOVE_THREADS, 0, ctx->stream>>>(K, (int)seg);
       CK(cudaGetLastError());
+      CK(cudaEventRecord(ctx->ev[1], ctx->stream));
       ctx->n_iter += seg;
       i += seg;
-      if (ctx->n_iter - 1 == next_rb) {
+      bool rb = (ctx->n_iter - 1 == next_rb);
+      if (rb) {
         launch_scan(ctx);
+        CK(cudaEventRecord(ctx->ev[2], ctx->stream));
         bmg_rebuild_kernel<<<ctx->C, 1024, 0, ctx->stream>>>(K, 0);
         CK(cudaGetLastError());
+        CK(cudaEventRecord(ctx->ev[3], ctx->stream));
+      }
+      CK(cudaEventSynchronize(rb ? ctx->ev[3] : ctx->ev[1]));
+      float a = 0, b = 0, c2 = 0;
+      CK(cudaEventElapsedTime(&a, ctx->ev[0], ctx->ev[1]));
+      ctx->ms[0] += a;
+      if (rb) {
+        CK(cudaEventElapsedTime(&b, ctx->ev[1], ctx->ev[2]));
+        CK(cudaEventElapsedTime(&c2, ctx->ev[2], ctx->ev[3]));
+        ctx->ms[1] += b;
+        ctx->ms[2] += c2;
+        ctx->n_scans++;
       }
     }
     drain_traces(ctx, iter0, sink);
@@ -931,7 +954,7 @@ extern "C" bmg_status bmg_run(bmg_ctx* ctx, uint64_t n_iter, const bmg_trace_sin
   CK(cudaEventSynchronize(e1));
   float ms = 0;
   CK(cudaEventElapsedTime(&ms, e0, e1));
-  ctx->ms[3] = ms;
+  ctx->ms[3] += ms;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   return BMG_OK;
@@ -1064,6 +1087,15 @@ extern "C" bmg_status bmg_get_timings(bmg_ctx* ctx, double* ms4)
 {
   if (!ctx || !ms4) return BMG_EINVAL;
   for (int i = 0; i < 4; ++i) ms4[i] = ctx->ms[i];
+  return BMG_OK;
+}
+
+extern "C" bmg_status bmg_reset_timings(bmg_ctx* ctx, uint64_t* n_scans)
+{
+  if (!ctx) return BMG_EINVAL;
+  if (n_scans) *n_scans = ctx->n_scans;
+  for (int i = 0; i < 4; ++i) ctx->ms[i] = 0;
+  ctx->n_scans = 0;
   return BMG_OK;
 }
 

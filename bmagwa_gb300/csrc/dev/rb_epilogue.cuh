@@ -1,0 +1,141 @@
+// The Rao-Blackwell epilogue shared by both scan implementations: from the
+// exact products x_t(j)' r of one (SNP, chain) to the reference's single-SNP
+// posterior (src/sampler.cpp:89-258) and the running means (:739-776).
+#ifndef BMG_RB_EPILOGUE_CUH_
+#define BMG_RB_EPILOGUE_CUH_
+
+#include <math.h>
+
+#include "common.cuh"
+
+static __device__ __forceinline__ bool in_model(const DevConst& K, int c, uint64_t j)
+{
+  return (K.inbits[(size_t)c * ((K.p + 31) / 32) + (j >> 5)] >> (j & 31)) & 1u;
+}
+
+// xr[t] = x_t(j)' R_c for term type t (A,H,D,R), exact, residual scale 2^-s.
+// Writes p_r and updates the running means (src/sampler.cpp:739-776).
+static __device__ __noinline__ void rb_epilogue(const DevConst& K, int c, uint64_t j, const long long* xr_by_type)
+{
+  const RbParams& rp = K.rb[c];
+  const double n = (double)K.n;
+  double xr[4];
+  for (int t = 0; t < 4; ++t) xr[t] = (double)xr_by_type[t] * rp.scale;
+  double mr = rp.mr;
+  double itv[4] = {rp.itv[0], rp.itv[1], rp.itv[2], rp.itv[3]};
+  if (K.use_individual_tau2) {
+    // Prior::sample_single_inv_tau2_from_prior_times_alpha2 (src/prior.hpp:192-199)
+    // with Rand::rand_sinvchi2(nu, s2) (src/rand.hpp:85-97); slot of (j, term u)
+    uint64_t slot = rp.rng_slot + j * (uint64_t)K.n_terms;
+    for (int t = 0; t < 4; ++t) {
+      if (!K.allow_terms[t]) continue;
+      double nu = K.nu_tau2[t];
+      double g = bmg_gamma_at(rp.key0, rp.key1, slot++, 0.5 * nu);
+      double val = nu * K.s2_tau2[t] / (2.0 * g);
+      itv[t] = 1.0 / (rp.alpha2 * val);
+    }
+  }
+  const double* lmp = rp.lmp_add;
+  if (in_model(K, c, j)) {
+    const DevModel& M = K.cur[c];
+    int mi = K.model_inds[(size_t)c * K.p + j];
+    int type = K.types[M.type_inds[mi]];
+    int x1 = M.x_ind1[mi];
+    int t1 = M.xc_type[x1];
+    double b1 = M.beta[x1];
+    if (K.use_individual_tau2) {
+      if (type == 4) { itv[0] = M.inv[x1]; itv[1] = M.inv[M.x_ind2[mi]]; }
+      else itv[type] = M.inv[x1];
+    }
+    // r_om = r + x_j beta_j: products and mean from the genotype counts
+    double msum = b1 * (double)term_sum(K.cnt, j, t1);
+    for (int t = 0; t < 4; ++t)
+      if (K.allow_terms[t]) xr[t] += b1 * (double)term_cross_same(K.cnt, j, t, t1);
+    if (type == 4) {
+      int x2 = M.x_ind2[mi];
+      int t2 = M.xc_type[x2];
+      double b2 = M.beta[x2];
+      msum += b2 * (double)term_sum(K.cnt, j, t2);
+      for (int t = 0; t < 4; ++t)
+        if (K.allow_terms[t]) xr[t] += b2 * (double)term_cross_same(K.cnt, j, t, t2);
+    }
+    mr = mr + msum / n;
+    lmp = rp.lmp_rem[type];
+  }
+  const double* pre = K.pre + j * (size_t)K.offset;
+  const int nt = K.n_types;
+  const bool ut = nt > 1;
+  double pt[5];
+  double pr = 0;
+  double maxt = -INFINITY;
+  for (int t = 0; t < nt; ++t) {
+    int type = K.types[t];
+    double det, et, slq;
+    if (type == 4) {
+      double sa = pre[0], va = pre[1] + itv[0], sh = pre[2], vh = pre[3] + itv[1];
+      double vah = pre[K.offset - 1];
+      slq = -log(itv[0]) - log(itv[1]);
+      double rxa = xr[0] - sa * mr;
+      double rxh = xr[1] - sh * mr;
+      det = va * vh - vah * vah;
+      et = rxa * rxa * vh - 2.0 * rxa * rxh * vah + rxh * rxh * va;
+      et /= det;
+    } else {
+      int off = K.offset_type[type];
+      double sv = pre[off];
+      det = pre[off + 1] + itv[type];
+      slq = -log(itv[type]);
+      double rx = xr[type] - sv * mr;
+      et = (rx * rx) / det;
+    }
+    double p = et * rp.inv_2s2 - 0.5 * (log(det) + slq) + lmp[type];
+    if (ut) {
+      if (p > maxt) maxt = p;
+      pt[t] = p;
+    } else {
+      double e = exp(p);
+      pr = isfinite(e) ? e / (1 + e) : 1;
+    }
+  }
+  if (ut) {
+    if (!isfinite(maxt)) {
+      if (maxt > 0) {
+        double st = 0;
+        for (int t = 0; t < nt; ++t) { pt[t] = (!isfinite(pt[t]) && pt[t] > 0) ? 1 : 0; st += pt[t]; }
+        for (int t = 0; t < nt; ++t) pt[t] /= st;
+        pr = 1;
+      } else {
+        for (int t = 0; t < nt; ++t) pt[t] = 1.0 / nt;
+        pr = 0;
+      }
+      if (isnan(maxt)) atomicExch(&K.ch[c].error, BMG_DERR_NAN);
+    } else {
+      double st = 0;
+      for (int t = 0; t < nt; ++t) { pt[t] = exp(pt[t] - maxt); st += pt[t]; }
+      for (int t = 0; t < nt; ++t) pt[t] /= st;
+      st = exp(log(st) + maxt);
+      pr = isfinite(st) ? st / (1 + st) : 1;
+    }
+  }
+  const size_t cj = (size_t)c * K.p + j;
+  if (K.p_r) {
+    K.p_r[cj] = pr;
+    if (ut)
+      for (int t = 0; t < nt; ++t) K.p_r_types[cj * nt + t] = pt[t];
+  }
+  if (rp.acc_rao) {
+    K.p_rao[cj] = rp.rao_z2 * K.p_rao[cj] + pr / rp.rao_z1;
+    if (ut)
+      for (int t = 0; t < nt; ++t)
+        K.p_rao_types[cj * nt + t] = rp.rao_z2 * K.p_rao_types[cj * nt + t] + pt[t] / rp.rao_z1;
+  }
+  if (rp.adapt) {
+    size_t q = (size_t)c * K.p + K.pos[j];
+    K.p_prop[q] = rp.prop_z2 * K.p_prop[q] + pr / rp.prop_z1;
+    if (ut)
+      for (int t = 0; t < nt; ++t)
+        K.p_prop_types[cj * nt + t] = rp.prop_z2 * K.p_prop_types[cj * nt + t] + pt[t] / rp.prop_z1;
+  }
+}
+
+#endif

@@ -1,16 +1,375 @@
-// Tensor-core scan: placeholder until the tcgen05 GEMM lands; the SIMT scan
-// runs meanwhile.
-#include "common.cuh"
+// Tensor-core scan on sm_103a: D = A . B' with tcgen05.
+//
+//   A  (M x K): one row per (SNP, term) of the genotype coding, K = individuals;
+//      values 0/1/2 as bf16, decoded in shared memory from the 2-bit PLINK codes
+//   B  (N x K): the residual of every chain as L balanced base-256 digits
+//      (bf16, exact), N = chains x L
+//   D  (M x N): FP32 in tensor memory.  Every product is an integer of
+//      magnitude <= 2 * 128 and every partial sum stays below 2^24 for n below
+//      65,536, so D holds exact integers and x' r = sum_l D[., c L + l] 256^l
+//      is exact: the same int64 the SIMT scan produces.
+//
+// CTA roles (192 threads): warps 0-3 decode A and, after the main loop, read
+// the accumulator rows from tensor memory; warp 4 issues the TMA loads of the
+// packed genotype rows and of the residual digits; warp 5 owns tensor memory
+// and issues the MMAs.  Stages are handed over with mbarriers; every wait is
+// bounded and reports a timeout in the chain error word instead of spinning.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+
+#include "rb_epilogue.cuh"
+
+namespace {
+
+constexpr int TC_THREADS = 192;
+constexpr int TC_STAGES = 4;
+constexpr int TC_BM = 128;          // rows of D per CTA
+constexpr int TC_BK = 64;           // individuals per stage (128 bytes of bf16)
+constexpr uint32_t WAIT_LIMIT = 1u << 24;
+
+struct TcParams {
+  uint32_t tpad;           // rows per SNP (terms rounded up to 1, 2 or 4)
+  uint32_t snps_per_tile;  // TC_BM / tpad
+  uint32_t chains_tile;    // chains per N tile
+  uint32_t n_mma;          // N of the MMA (chains_tile * L rounded up to 16)
+  uint32_t k_chunks;       // n_pad / TC_BK
+  uint32_t stage_bytes;
+  uint32_t b_bytes, a_bytes, pk_bytes;
+  int32_t term_of_row[4];  // term of row u of a SNP (-1: unused)
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p)
+{
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
+{
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar)
+{
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_tx(uint64_t* bar, uint32_t bytes)
+{
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity)
+{
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// bounded wait: false after WAIT_LIMIT polls
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity)
+{
+  for (uint32_t it = 0; it < WAIT_LIMIT; ++it)
+    if (mbar_try(bar, parity)) return true;
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y)
+{
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+      ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// shared-memory matrix descriptor, K-major, 128-byte swizzle, 8-row atoms of 1024 B
+__device__ __forceinline__ uint64_t smem_desc(const void* p)
+{
+  uint64_t addr = smem_u32(p);
+  uint64_t d = 0;
+  d |= (addr >> 4) & 0x3FFFull;            // start address
+  d |= (uint64_t)1 << 16;                  // leading byte offset (unused for this layout)
+  d |= (uint64_t)(1024 >> 4) << 32;        // stride byte offset: next 8-row atom
+  d |= (uint64_t)1 << 46;                  // descriptor version
+  d |= (uint64_t)2 << 61;                  // 128-byte swizzle
+  return d;
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc)
+{
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar)
+{
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v)
+{
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+        "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+        "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
+        "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+}  // namespace
+
+extern "C" __global__ void __launch_bounds__(TC_THREADS, 1)
+bmg_scan_tc_kernel(DevConst K, TcParams P, const __grid_constant__ CUtensorMap map_b,
+                   const __grid_constant__ CUtensorMap map_g)
+{
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  // 1024-byte aligned base for the swizzled tiles
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  __shared__ uint64_t full_bar[TC_STAGES], aready_bar[TC_STAGES], empty_bar[TC_STAGES], acc_bar;
+  __shared__ uint32_t tmem_base_sh;
+  __shared__ int timed_out;
+  __shared__ uint2 lut[4][256];  // per term: byte -> 4 bf16 values
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t m_tile = blockIdx.x, n_tile = blockIdx.y;
+  const uint32_t snp0 = m_tile * P.snps_per_tile;
+  const uint32_t chain0 = n_tile * P.chains_tile;
+  const uint32_t L = K.limbs_n;
+  const uint32_t chains_here = min(P.chains_tile, K.n_chains - chain0);
+
+  // decode tables: bf16 bit patterns of 0, 1, 2 are 0x0000, 0x3F80, 0x4000
+  for (int e = tid; e < 4 * 256; e += TC_THREADS) {
+    int term = e >> 8, byte = e & 255;
+    uint16_t h[4];
+    for (int q = 0; q < 4; ++q) {
+      int code = (byte >> (2 * q)) & 3;
+      int v = term_value(code, term);
+      h[q] = v == 0 ? 0 : (v == 1 ? 0x3F80 : 0x4000);
+    }
+    lut[term][byte] = make_uint2((uint32_t)h[0] | ((uint32_t)h[1] << 16), (uint32_t)h[2] | ((uint32_t)h[3] << 16));
+  }
+  if (tid == 0) {
+    for (int s = 0; s < TC_STAGES; ++s) {
+      mbar_init(&full_bar[s], 1);
+      mbar_init(&aready_bar[s], 4);
+      mbar_init(&empty_bar[s], 1);
+    }
+    mbar_init(&acc_bar, 1);
+    timed_out = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 5) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_sh)),
+                 "r"(256u));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_base_sh;
+  const uint32_t nk = P.k_chunks;
+
+  if (warp == 4) {
+    if (lane == 0) {
+      // TMA producer: packed genotype rows and residual digits of each stage
+      for (uint32_t k = 0; k < nk; ++k) {
+        uint32_t s = k % TC_STAGES;
+        if (k >= TC_STAGES && !mbar_wait(&empty_bar[s], ((k / TC_STAGES) - 1) & 1)) { timed_out = 1; break; }
+        uint8_t* st = smem + s * P.stage_bytes;
+        mbar_arrive_tx(&full_bar[s], P.b_bytes + P.pk_bytes);
+        tma_load_2d(st, &map_b, &full_bar[s], (int)(k * TC_BK), (int)(chain0 * L));
+        tma_load_2d(st + P.b_bytes + P.a_bytes, &map_g, &full_bar[s], (int)(k * (TC_BK / 4)), (int)snp0);
+      }
+    }
+  } else if (warp == 5) {
+    if (lane == 0) {
+      // MMA issuer
+      const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((P.n_mma >> 3) << 17) | ((uint32_t)(TC_BM >> 4) << 24);
+      for (uint32_t k = 0; k < nk; ++k) {
+        uint32_t s = k % TC_STAGES, par = (k / TC_STAGES) & 1;
+        if (!mbar_wait(&full_bar[s], par) || !mbar_wait(&aready_bar[s], par)) { timed_out = 1; break; }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        uint8_t* st = smem + s * P.stage_bytes;
+        uint64_t bdesc = smem_desc(st), adesc = smem_desc(st + P.b_bytes);
+#pragma unroll
+        for (int kk = 0; kk < TC_BK / 16; ++kk)  // 16 bf16 = 32 bytes = 2 descriptor units
+          mma_bf16(tmem, adesc + 2 * kk, bdesc + 2 * kk, idesc, (k | kk) != 0);
+        mma_commit(&empty_bar[s]);
+      }
+      mma_commit(&acc_bar);
+    }
+  } else {
+    // decode warps: packed 2-bit codes -> bf16 rows of the swizzled A tile
+    const uint32_t row = tid;  // 0..127
+    const uint32_t sl = row / P.tpad, u = row % P.tpad;
+    const int term = P.term_of_row[u];
+    for (uint32_t k = 0; k < nk; ++k) {
+      uint32_t s = k % TC_STAGES, par = (k / TC_STAGES) & 1;
+      if (!mbar_wait(&full_bar[s], par)) { timed_out = 1; break; }
+      uint8_t* st = smem + s * P.stage_bytes;
+      uint8_t* a = st + P.b_bytes;
+      const uint8_t* pk = st + P.b_bytes + P.a_bytes + sl * 16;
+      uint4 bytes = *reinterpret_cast<const uint4*>(pk);
+      uint32_t w[4] = {bytes.x, bytes.y, bytes.z, bytes.w};
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        uint32_t two = (w[c >> 1] >> ((c & 1) * 16)) & 0xFFFF;
+        uint2 lo = (term >= 0) ? lut[term][two & 255] : make_uint2(0, 0);
+        uint2 hi = (term >= 0) ? lut[term][two >> 8] : make_uint2(0, 0);
+        uint4 v = make_uint4(lo.x, lo.y, hi.x, hi.y);
+        *reinterpret_cast<uint4*>(a + row * 128 + ((c ^ (row & 7)) << 4)) = v;
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&aready_bar[s]);
+    }
+  }
+
+  // epilogue: accumulator rows -> shared memory (exact integers in FP32)
+  float* raw = reinterpret_cast<float*>(smem);
+  const uint32_t rstride = P.n_mma + 1;
+  if (warp < 4) {
+    if (!mbar_wait(&acc_bar, 0)) timed_out = 1;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    for (uint32_t col = 0; col < P.n_mma; col += 32) {
+      float v[32];
+      tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + col, v);
+      const uint32_t row = warp * 32 + lane;
+      const uint32_t nq = min(32u, P.n_mma - col);
+      for (uint32_t q = 0; q < nq; ++q) raw[row * rstride + col + q] = v[q];
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (timed_out) {
+    if (tid == 0) atomicExch(&K.ch[0].error, BMG_DERR_TIMEOUT);
+  } else {
+    // one unit per (SNP, chain): combine the digits, then the RB epilogue
+    const uint32_t units = P.snps_per_tile * chains_here;
+    for (uint32_t u = tid; u < units; u += TC_THREADS) {
+      uint32_t cl = u % chains_here, sl = u / chains_here;
+      uint64_t j = (uint64_t)snp0 + sl;
+      uint32_t c = chain0 + cl;
+      if (j >= K.p || !K.rb[c].do_scan) continue;
+      long long xr[4] = {0, 0, 0, 0};
+      for (uint32_t q = 0; q < P.tpad; ++q) {
+        int term = P.term_of_row[q];
+        if (term < 0) continue;
+        const float* rr = raw + (sl * P.tpad + q) * rstride + cl * L;
+        long long acc = 0;
+        for (uint32_t l = 0; l < L; ++l) acc += (long long)rr[l] * (1ll << (8 * l));
+        xr[term] = acc;
+      }
+      rb_epilogue(K, (int)c, j, xr);
+    }
+  }
+  __syncthreads();
+  if (warp == 5) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(256u));
+  }
+}
+
+// ----------------------------------------------------------------- host side
+
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
+{
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    cudaDriverEntryPointQueryResult q;
+    void* p = nullptr;
+    if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+static bool tc_plan(const DevConst* K, TcParams* P)
+{
+  uint32_t T = K->n_terms;
+  P->tpad = T <= 1 ? 1 : (T <= 2 ? 2 : 4);
+  P->snps_per_tile = TC_BM / P->tpad;
+  for (uint32_t u = 0; u < 4; ++u) P->term_of_row[u] = (u < T) ? K->term_of[u] : -1;
+  const uint32_t L = K->limbs_n;
+  P->chains_tile = min(K->n_chains, 256u / L);
+  P->n_mma = ((P->chains_tile * L + 15) / 16) * 16;
+  if (P->n_mma > 256 || P->n_mma < 16) return false;
+  if (K->n_pad % TC_BK != 0 || K->n >= 65536) return false;  // exact FP32 sums need n < 2^16
+  P->k_chunks = K->n_pad / TC_BK;
+  P->b_bytes = P->n_mma * 128;
+  P->a_bytes = TC_BM * 128;
+  P->pk_bytes = P->snps_per_tile * 16;
+  P->stage_bytes = ((P->b_bytes + P->a_bytes + P->pk_bytes + 1023) / 1024) * 1024;
+  return true;
+}
 
 extern "C" int bmg_scan_tc_supported(const DevConst* K)
 {
-  (void)K;
-  return 0;
+  TcParams P;
+  if (!tc_plan(K, &P) || !encode_fn()) return 0;
+  int dev = 0, major = 0, minor = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+  cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
+  return (major == 10 && minor == 3) ? 1 : 0;
 }
 
 extern "C" int bmg_scan_tc_launch(const DevConst* K, cudaStream_t stream)
 {
-  (void)K;
-  (void)stream;
-  return 1;
+  TcParams P;
+  if (!tc_plan(K, &P)) return 1;
+  auto enc = encode_fn();
+  if (!enc) return 2;
+  CUtensorMap mb, mg;
+  {
+    cuuint64_t dims[2] = {K->n_pad, (cuuint64_t)K->n_chains * K->limbs_n};
+    cuuint64_t strides[1] = {(cuuint64_t)K->n_pad * 2};
+    cuuint32_t box[2] = {TC_BK, P.n_mma};
+    cuuint32_t es[2] = {1, 1};
+    if (enc(&mb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void*)K->limbs, dims, strides, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return 3;
+  }
+  {
+    cuuint64_t dims[2] = {K->gs, K->p};
+    cuuint64_t strides[1] = {K->gs};
+    cuuint32_t box[2] = {16, P.snps_per_tile};
+    cuuint32_t es[2] = {1, 1};
+    if (enc(&mg, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, (void*)K->geno, dims, strides, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return 4;
+  }
+  size_t raw_bytes = (size_t)TC_BM * (P.n_mma + 1) * 4;
+  size_t smem = std::max((size_t)TC_STAGES * P.stage_bytes, raw_bytes) + 1024;
+  if (smem > 227 * 1024) return 5;
+  static size_t configured = 0;
+  if (configured < smem) {
+    if (cudaFuncSetAttribute(bmg_scan_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+      return 6;
+    configured = smem;
+  }
+  dim3 grid((unsigned)((K->p + P.snps_per_tile - 1) / P.snps_per_tile),
+            (unsigned)((K->n_chains + P.chains_tile - 1) / P.chains_tile));
+  bmg_scan_tc_kernel<<<grid, TC_THREADS, smem, stream>>>(*K, P, mb, mg);
+  return cudaGetLastError() == cudaSuccess ? 0 : 7;
 }

@@ -100,6 +100,7 @@ struct DevChain {
 #define BMG_DERR_TRACE 5         // trace buffer overflow
 #define BMG_DERR_REMSET 6
 #define BMG_DERR_START 7         // non-finite likelihood at start
+#define BMG_DERR_TIMEOUT 8       // a bounded device wait gave up
 
 // Parameters the move kernel hands to the RB scan epilogue, per chain.
 struct RbParams {

@@ -40,7 +40,7 @@ def _normal_icdf(p):
     return math.sqrt(2.0) * torch.erfinv(2.0 * p - 1.0)
 
 
-def genotypes(n, p, ld_block, seed, device="cpu", rho=0.8, chunk=4096):
+def genotypes(n, p, ld_block, seed, device="cpu", rho=0.8, chunk=4096, block_group=None):
     """Allele counts (p x n, uint8) and MAFs (p,)."""
     g = torch.Generator(device=device)
     g.manual_seed(int(seed))
@@ -54,16 +54,21 @@ def genotypes(n, p, ld_block, seed, device="cpu", rho=0.8, chunk=4096):
             out[s:e] = (u < maf[s:e, None, None].float()).sum(-1).to(torch.uint8)
         return out, maf
     q = math.sqrt(1.0 - rho * rho)
-    z = torch.empty((n, 2), dtype=torch.float32, device=device)
-    for s in range(0, p, ld_block):
-        e = min(p, s + ld_block)
-        z.normal_(generator=g)
-        block = []
-        for j in range(s, e):
-            if j > s:
-                z = rho * z + q * torch.randn((n, 2), generator=g, device=device)
-            block.append((z > thr[j]).sum(-1).to(torch.uint8))
-        out[s:e] = torch.stack(block)
+    nb = (p + ld_block - 1) // ld_block
+    # blocks advance together: step j of every block of a group at once
+    group = block_group or max(1, min(nb, (1 << 26) // max(1, 2 * n)))
+    for b0 in range(0, nb, group):
+        b1 = min(nb, b0 + group)
+        z = torch.randn((b1 - b0, n, 2), generator=g, device=device)
+        for j in range(ld_block):
+            if j > 0:
+                z = rho * z + q * torch.randn((b1 - b0, n, 2), generator=g, device=device)
+            snps = torch.arange(b0, b1, device=device) * ld_block + j
+            ok = snps < p
+            if not bool(ok.any()):
+                break
+            snps = snps[ok]
+            out[snps] = (z[ok] > thr[snps][:, None, None]).sum(-1).to(torch.uint8)
     return out, maf
 
 

@@ -241,13 +241,17 @@ bmg_status bmg_get_last_scan(bmg_ctx* ctx, uint32_t chain, double* p_r, double* 
  * under opt.basename (src/sampler.cpp:838-858, src/sampler.hpp:384-390). */
 bmg_status bmg_finish(bmg_ctx* ctx);
 
-/* Device time of the phases of the last bmg_run, in milliseconds:
- * [0] move kernel, [1] scan, [2] proposal rebuild, [3] total. */
+/* Device time of the phases of bmg_run since the last bmg_reset_timings, in
+ * milliseconds: [0] move kernel, [1] scan, [2] proposal rebuild, [3] total. */
 bmg_status bmg_get_timings(bmg_ctx* ctx, double* ms4);
 
 /* var_x, mean_x, var_y, y'y of the loaded data (src/data.hpp:66-71; the
  * reference prints the first three at start, src/main.cpp:58-62). */
 bmg_status bmg_get_data_stats(bmg_ctx* ctx, double* out4);
+
+/* Zero the phase timers; n_scans (may be NULL) receives the scans since the
+ * last reset. */
+bmg_status bmg_reset_timings(bmg_ctx* ctx, uint64_t* n_scans);
 
 const char* bmg_last_error(const bmg_ctx* ctx);
 const char* bmg_status_string(bmg_status s);

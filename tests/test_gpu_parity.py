@@ -117,3 +117,21 @@ def test_gpu_writes_reference_files(bmg, tmp_path):
     assert (tmp_path / "out" / "chain0_log.txt").exists()
     assert (tmp_path / "out" / "chain_prior.txt").exists()
     assert (tmp_path / "out" / "chain1_samplerstats.txt").exists()
+
+
+def test_tc_scan_bitwise_equals_simt(bmg, tmp_path):
+    """The tensor-core scan's integer products equal the SIMT scan's: the last
+    in-loop posteriors and every trace are bit-identical."""
+    opt, packed, y, e = synth_case(bmg, tmp_path, name="batched", n=1000, p=5000, chains=3, iters=60,
+                                   n_rao=3)
+    res = {}
+    for scan in (1, 0):
+        opt.scan_impl = scan
+        ctx, col = run_gpu(bmg, opt, packed, y, e, 60)
+        res[scan] = (ctx, col)
+    for c in range(opt.n_chains):
+        H.compare(res[1][1].chain(c), res[0][1].chain(c), rtol=0.0, label="chain %d" % c)
+        a, at = res[1][0].last_scan(c)
+        b, bt = res[0][0].last_scan(c)
+        assert np.array_equal(a, b)
+        assert np.array_equal(at, bt)
