@@ -201,23 +201,28 @@ def run_gb300(args, wl):
     units = args.steps * wl["chains"] * world
     value = units / dev_s
     # e2e: the whole job through the C ABI from host buffers
-    o2 = options(bg, wl, seed + 17, iters_total)
-    o2.scan_impl = args.scan
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    ctx2 = bg.Context(o2)
-    ctx2.load_bed(packed)
-    ctx2.set_phenotypes(y)
-    ctx2.set_covariates(None)
-    ctx2.precompute()
-    col = ctx2.run(args.steps, collect=True)
-    rao = [ctx2.rao(c)[0] for c in range(wl["chains"])]
-    torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
-    d2h = sum(int(sum(a.nbytes for a in col.chain(c).values())) for c in range(wl["chains"]))
-    d2h += sum(r.nbytes for r in rao)
-    h2d = packed.nbytes + y.nbytes
-    ctx2.close()
+    ctx.close()
+    e2e = None
+    if args.e2e:
+        o2 = options(bg, wl, seed + 17, iters_total)
+        o2.scan_impl = args.scan
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx2 = bg.Context(o2)
+        ctx2.load_bed(packed)
+        ctx2.set_phenotypes(y)
+        ctx2.set_covariates(None)
+        ctx2.precompute()
+        col = ctx2.run(args.steps, collect=True)
+        rao = [ctx2.rao(c)[0] for c in range(wl["chains"])]
+        torch.cuda.synchronize()
+        e2e_s = time.perf_counter() - t0
+        d2h = sum(int(sum(a.nbytes for a in col.chain(c).values())) for c in range(wl["chains"]))
+        d2h += sum(r.nbytes for r in rao)
+        h2d = packed.nbytes + y.nbytes
+        ctx2.close()
+        e2e = {"value": args.steps * wl["chains"] * world / e2e_s, "unit": "iter/s",
+               "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps}
     # roofline of the scan kernel
     p, n, C = wl["p"], wl["n"], wl["chains"]
     scan_ms = ms[1] / max(1, n_scans)
@@ -241,8 +246,7 @@ def run_gb300(args, wl):
                    "types": wl["types"], "parallelism": "replicas" if world > 1 else "single",
                    "l2": "inputs larger than L2 (%.2f GB packed genotypes)" % (packed.nbytes / 1e9),
                    "scan_impl": "tcgen05" if args.scan == 0 else "simt"},
-        "e2e": {"value": args.steps * C / e2e_s, "unit": "iter/s",
-                "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps},
+        "e2e": e2e,
         "gpu_launches": int(args.steps * (1 + 2) + args.steps * (1 if args.scan == 1 else 0)),
         "phase_ms": {"move": ms[0], "scan": ms[1], "rebuild": ms[2], "total": ms[3],
                      "scans": n_scans, "wall_s": dt},
@@ -314,10 +318,17 @@ def main():
     ap.add_argument("--workload", default="scan", choices=sorted(WORKLOADS))
     ap.add_argument("--scan", type=int, default=0, help="0 tcgen05, 1 SIMT")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--p", type=int, default=None, help="override the SNP count (profiling)")
+    ap.add_argument("--n", type=int, default=None, help="override the individuals (profiling)")
+    ap.add_argument("--chains", type=int, default=None, help="override the chains (profiling)")
+    ap.add_argument("--no-e2e", dest="e2e", action="store_false")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    wl = WORKLOADS[args.workload]
+    wl = dict(WORKLOADS[args.workload])
+    for key in ("p", "n", "chains"):
+        if getattr(args, key):
+            wl[key] = getattr(args, key)
     if args.impl == "reference":
         run_reference(args, wl)
     else:
