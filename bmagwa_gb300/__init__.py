@@ -62,6 +62,9 @@ def lib():
         L.bmg_get_timings.argtypes = [vp, vp]
         L.bmg_get_proposal.argtypes = [vp, u32, vp, vp]
         L.bmg_reset_timings.argtypes = [vp, C.POINTER(u64)]
+        L.bmg_precompute_noalloc.argtypes = [vp, u64, u64, C.c_int32, C.POINTER(C.c_int32), u32, vp,
+                                             C.POINTER(u32), vp, vp]
+        L.bmg_precompute_noalloc.restype = C.c_int
         L.bmg_get_last_scan.argtypes = [vp, u32, vp, vp]
         L.bmg_get_data_stats.argtypes = [vp, vp]
         L.bmg_last_error.argtypes = [vp]
@@ -237,6 +240,18 @@ class Context:
 
     def finish(self):
         self._check(lib().bmg_finish(self.h))
+
+
+def precompute_noalloc(d_packed, n, p, recode, types, d_out, d_flag, stream=None):
+    """bmg_precompute_noalloc on caller-owned device buffers (raw pointers)."""
+    t = (C.c_int32 * len(types))(*types)
+    off = C.c_uint32()
+    rc = lib().bmg_precompute_noalloc(C.c_void_p(d_packed), n, p, int(recode), t, len(types),
+                                      C.c_void_p(d_out), C.byref(off), C.c_void_p(d_flag),
+                                      None if stream is None else C.c_void_p(stream))
+    if rc != 0:
+        raise BmgError(rc, "bmg_precompute_noalloc failed")
+    return off.value
 
 
 def run_ini(path, n_iter=None, write_files=True):

@@ -253,6 +253,24 @@ bmg_status bmg_get_data_stats(bmg_ctx* ctx, double* out4);
  * last reset. */
 bmg_status bmg_reset_timings(bmg_ctx* ctx, uint64_t* n_scans);
 
+/* Per-SNP precomputed sums, allocating nothing (no counterpart in the
+ * reference).  For callers that cannot call cudaMalloc, e.g. code running in
+ * another framework's memory pool or while a stream is being captured.
+ * Inputs and outputs are the caller's device buffers: d_packed holds p rows of
+ * ceil(n/4) bytes (the .bed payload), d_out receives p x offset doubles in the
+ * layout bmg_get_precomputed() returns (offset is written to *offset_out),
+ * d_flag one int32 set to 1 if any genotype call is missing (missing calls
+ * count as 0, as in the reference's precomputation).  `stream` is a
+ * cudaStream_t or NULL.  Working memory is a fixed array inside the library
+ * of 3 x 2^20 int32 (12 MB per device, kept until the process exits); p above
+ * 2^20 returns BMG_EINVAL.  The first call on each device looks up that
+ * array's device address, so make the first call before capturing a stream.
+ * Calls that overlap on the GPU share the array and race; calls ordered on
+ * one stream do not. */
+bmg_status bmg_precompute_noalloc(const uint8_t* d_packed, uint64_t n, uint64_t p, int32_t recode,
+                                  const int32_t* types, uint32_t n_types, double* d_out,
+                                  uint32_t* offset_out, int32_t* d_flag, void* stream);
+
 const char* bmg_last_error(const bmg_ctx* ctx);
 const char* bmg_status_string(bmg_status s);
 void bmg_destroy(bmg_ctx* ctx);
