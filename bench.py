@@ -39,8 +39,8 @@ FALLBACK_HBM = 6800.0
 
 
 def env_rank():
-    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), \
-        int(os.environ.get("LOCAL_RANK", "0"))
+    from bmagwa_gb300 import replicas
+    return replicas.rank_info()
 
 
 def options(bg, wl, seed0, iters):
@@ -193,13 +193,11 @@ def run_gb300(args, wl):
     ms = ctx.timings()
     n_scans = ctx.reset_timings()
     dev_s = ms[3] / 1000.0
+    from bmagwa_gb300 import replicas
     if world > 1:
-        t = torch.tensor([dev_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dev_s = float(t.item())
+        dev_s = replicas.max_over_ranks(dev_s, device="cuda")
         dist.barrier()
-    units = args.steps * wl["chains"] * world
-    value = units / dev_s
+    value = replicas.job_throughput(dev_s, args.steps, wl["chains"], world)
     # e2e: the whole job through the C ABI from host buffers
     ctx.close()
     e2e = None
@@ -223,6 +221,12 @@ def run_gb300(args, wl):
         ctx2.close()
         e2e = {"value": args.steps * wl["chains"] * world / e2e_s, "unit": "iter/s",
                "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps}
+        # inclusion-indicator ESS of the same run (Geyer initial monotone
+        # sequence over the thinned trace of each chain)
+        from bmagwa_gb300 import ess
+        tr = [col.chain(c) for c in range(wl["chains"])]
+        e2e["inclusion_ess"] = dict(ess.summarize([(t["modelsize"], t["loci"]) for t in tr if t], e2e_s),
+                                    samples_per_chain=int(len(tr[0]["modelsize"])) if tr[0] else 0)
     # roofline of the scan kernel
     p, n, C = wl["p"], wl["n"], wl["chains"]
     scan_ms = ms[1] / max(1, n_scans)

@@ -28,12 +28,15 @@
 extern "C" __global__ void bmg_prep_kernel(uint8_t* geno, uint64_t n, uint64_t p, uint32_t gs,
                                            int recode, int32_t* cnt, int32_t* missing);
 extern "C" __global__ void bmg_trace_reset_kernel(DevChain* ch, int n_chains);
+extern "C" __global__ void bmg_gsum_kernel(const uint8_t* geno, uint64_t n, uint64_t p, uint32_t gs,
+                                           const int64_t* yint, const int64_t* eint, uint32_t nv, int64_t* gsum);
 extern "C" __global__ void bmg_init_kernel(DevConst K);
 extern "C" __global__ void bmg_rbprep_kernel(DevConst K);
 extern "C" __global__ void bmg_move_kernel(DevConst K, int max_iters);
 extern "C" __global__ void bmg_scan_simt_kernel(DevConst K, const int64_t* resid_t);
 extern "C" __global__ void bmg_resid_transpose_kernel(DevConst K, int64_t* resid_t);
 extern "C" __global__ void bmg_rebuild_kernel(DevConst K, int force);
+extern "C" cudaError_t bmg_move_configure(size_t* smem_bytes);
 // tensor-core scan (scan_tc.cu)
 extern "C" int bmg_scan_tc_launch(const DevConst* K, cudaStream_t stream);
 extern "C" int bmg_scan_tc_supported(const DevConst* K);
@@ -78,6 +81,7 @@ struct bmg_ctx {
   std::vector<DevChain> ch_h;
   double ms[4] = {0, 0, 0, 0};
   uint64_t n_scans = 0;
+  size_t move_smem = 0;   // dynamic shared memory of a move CTA
   cudaEvent_t ev[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   uint64_t n_iter = 0;
   time_t t_start = 0;
@@ -94,7 +98,9 @@ struct bmg_ctx {
     size_t bytes = std::max<size_t>(1, count * sizeof(T));
     CK(cudaMalloc(&ptr, bytes));
     allocs.push_back(ptr);
-    if (zero) CK(cudaMemset(ptr, 0, bytes));
+    // on the context's own (non-blocking) stream: a legacy-stream memset is
+    // not ordered with the uploads that follow on `stream`
+    if (zero) CK(cudaMemsetAsync(ptr, 0, bytes, stream));
     return static_cast<T*>(ptr);
   }
   ~bmg_ctx()
@@ -476,6 +482,15 @@ extern "C" bmg_status bmg_precompute(bmg_ctx* ctx)
   K.e = dE;
   K.eint = dEi;
   K.se = dse;
+  {
+    // X'y and X'E of every SNP and term, from exact per-SNP H/R sums
+    const uint32_t nv = std::max<uint32_t>(1, me);
+    int64_t* gsum = ctx->dalloc<int64_t>((size_t)K.p * nv * 2, false);
+    const uint64_t blocks = std::min<uint64_t>((K.p + 7) / 8, 152 * 8);
+    bmg_gsum_kernel<<<(unsigned)blocks, 256, 0, ctx->stream>>>(K.geno, n, K.p, K.gs, K.yint, dEi, nv, gsum);
+    CK(cudaGetLastError());
+    K.gsum = gsum;
+  }
   K.ee = dee;
   K.ey = dey;
   K.e_absmax = demax;
@@ -668,7 +683,7 @@ extern "C" bmg_status bmg_precompute(bmg_ctx* ctx)
     DevModel& M = models[c];
     std::memset(&M, 0, sizeof(M));
     M.xx = ctx->dalloc<double>((size_t)km * km);
-    M.l = ctx->dalloc<double>((size_t)km * km);
+    M.l = ctx->dalloc<double>((size_t)km * (km + 1) / 2);  // packed upper triangle
     M.xy = ctx->dalloc<double>(km);
     M.v = ctx->dalloc<double>(km);
     M.inv = ctx->dalloc<double>(km);
@@ -728,7 +743,8 @@ extern "C" bmg_status bmg_precompute(bmg_ctx* ctx)
     std::vector<double> ft(pc * o.n_types, 1.0 / o.n_types);
     CK(cudaMemcpyAsync(K.p_prop_types, ft.data(), 8 * ft.size(), cudaMemcpyHostToDevice, ctx->stream));
   }
-  bmg_init_kernel<<<C, 32, 0, ctx->stream>>>(K);
+  CK(bmg_move_configure(&ctx->move_smem));
+  bmg_init_kernel<<<C, 32, ctx->move_smem, ctx->stream>>>(K);
   CK(cudaGetLastError());
   bmg_rebuild_kernel<<<C, 1024, 0, ctx->stream>>>(K, 1);
   CK(cudaGetLastError());
@@ -921,7 +937,7 @@ extern "C" bmg_status bmg_run(bmg_ctx* ctx, uint64_t n_iter, const bmg_trace_sin
       uint64_t next_rb = ((t / n_rao) + 1) * n_rao - 1;  // first iter >= t with (iter+1) % n_rao == 0
       uint64_t seg = std::min<uint64_t>(chunk - i, next_rb - t + 1);
       CK(cudaEventRecord(ctx->ev[0], ctx->stream));
-      bmg_move_kernel<<<ctx->C, BMG_MOVE_THREADS, 0, ctx->stream>>>(K, (int)seg);
+      bmg_move_kernel<<<ctx->C, BMG_MOVE_THREADS, ctx->move_smem, ctx->stream>>>(K, (int)seg);
       CK(cudaGetLastError());
       CK(cudaEventRecord(ctx->ev[1], ctx->stream));
       ctx->n_iter += seg;
@@ -967,7 +983,7 @@ extern "C" bmg_status bmg_scan(bmg_ctx* ctx, double* p_r, double* p_r_types)
   API_BEGIN
   check_ready(ctx);
   DevConst& K = ctx->K;
-  bmg_rbprep_kernel<<<ctx->C, BMG_MOVE_THREADS, 0, ctx->stream>>>(K);
+  bmg_rbprep_kernel<<<ctx->C, BMG_MOVE_THREADS, ctx->move_smem, ctx->stream>>>(K);
   CK(cudaGetLastError());
   launch_scan(ctx);
   const size_t pc = (size_t)ctx->p * ctx->C;
@@ -1007,7 +1023,8 @@ extern "C" bmg_status bmg_get_state(bmg_ctx* ctx, uint32_t chain, bmg_chain_stat
     int ng = 0;
     const uint32_t tw = ctx->K.tw;
     std::vector<double> tab((size_t)22 * tw);
-    CK(cudaMemcpy(tab.data(), ctx->K.tab, 8 * tab.size(), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpyAsync(tab.data(), ctx->K.tab, 8 * tab.size(), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
     for (int i = 0; i < 5; ++i)
       if (ctx->K.allow_types[i]) { lp += tab[(size_t)(14 + i) * tw + M.Ns[i]]; ng += M.Ns[i]; }
     lp += tab[(size_t)19 * tw + ng] + tab[(size_t)20 * tw + ng] - tab[(size_t)21 * tw + ng];
@@ -1106,7 +1123,8 @@ extern "C" bmg_status bmg_finish(bmg_ctx* ctx)
   check_ready(ctx);
   const bmg_options& o = ctx->opt;
   const uint32_t C = ctx->C;
-  CK(cudaMemcpy(ctx->ch_h.data(), ctx->K.ch, sizeof(DevChain) * C, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpyAsync(ctx->ch_h.data(), ctx->K.ch, sizeof(DevChain) * C, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
   double elapsed = ctx->t_start ? difftime(time(nullptr), ctx->t_start) : 0.0;
   for (uint32_t c = 0; c < C; ++c) {
     std::string b = std::string(o.basename) + std::to_string(c);

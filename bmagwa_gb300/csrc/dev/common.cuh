@@ -83,8 +83,9 @@ __device__ __forceinline__ uint64_t ld_u64(const uint8_t* p) { return *(const ui
 // Rebuild the dd_add prefix of chain c with the calling CTA (all threads):
 // weights in the in-order position order of the reference's proposal tree
 // (src/discrete_distribution.hpp:217-314), zero for SNPs in the current
-// model, exclusive prefix sums in fixed point (weight * 2^qs).
-__device__ inline void rebuild_chain(const DevConst& K, int c, long long* part)
+// model, exclusive prefix sums in fixed point (weight * 2^qs).  The totals
+// go to `chain` (the chain's state in global or shared memory).
+__device__ inline void rebuild_chain(const DevConst& K, int c, long long* part, DevChain* chain)
 {
   const int tid = threadIdx.x, nth = blockDim.x;
   const uint64_t p = K.p;
@@ -121,9 +122,9 @@ __device__ inline void rebuild_chain(const DevConst& K, int c, long long* part)
   __syncthreads();
   if (tid == nth - 1) {
     cadd[p] = part[nth - 1];
-    K.ch[c].cadd_total = part[nth - 1];
-    K.ch[c].n_pend = 0;
-    K.ch[c].rebuild = 0;
+    chain->cadd_total = part[nth - 1];
+    chain->n_pend = 0;
+    chain->rebuild = 0;
   }
   __syncthreads();
 }

@@ -20,7 +20,7 @@ static __device__ __noinline__ void rb_epilogue(const DevConst& K, int c, uint64
   const RbParams& rp = K.rb[c];
   const double n = (double)K.n;
   double xr[4];
-  for (int t = 0; t < 4; ++t) xr[t] = (double)xr_by_type[t] * rp.scale;
+  for (int t = 0; t < 4; ++t) xr[t] = K.allow_terms[t] ? (double)xr_by_type[t] * rp.scale : 0.0;
   double mr = rp.mr;
   double itv[4] = {rp.itv[0], rp.itv[1], rp.itv[2], rp.itv[3]};
   if (K.use_individual_tau2) {
@@ -36,6 +36,9 @@ static __device__ __noinline__ void rb_epilogue(const DevConst& K, int c, uint64
     }
   }
   const double* lmp = rp.lmp_add;
+  // -log(itv[t]) of the shared tau2 is the chain's constant; per-SNP draws
+  // and in-model precisions need their own
+  bool own_itv = K.use_individual_tau2;
   if (in_model(K, c, j)) {
     const DevModel& M = K.cur[c];
     int mi = K.model_inds[(size_t)c * K.p + j];
@@ -74,7 +77,7 @@ static __device__ __noinline__ void rb_epilogue(const DevConst& K, int c, uint64
     if (type == 4) {
       double sa = pre[0], va = pre[1] + itv[0], sh = pre[2], vh = pre[3] + itv[1];
       double vah = pre[K.offset - 1];
-      slq = -log(itv[0]) - log(itv[1]);
+      slq = own_itv ? -log(itv[0]) - log(itv[1]) : rp.nlog_itv[0] - log(itv[1]);
       double rxa = xr[0] - sa * mr;
       double rxh = xr[1] - sh * mr;
       det = va * vh - vah * vah;
@@ -84,7 +87,7 @@ static __device__ __noinline__ void rb_epilogue(const DevConst& K, int c, uint64
       int off = K.offset_type[type];
       double sv = pre[off];
       det = pre[off + 1] + itv[type];
-      slq = -log(itv[type]);
+      slq = own_itv ? -log(itv[type]) : rp.nlog_itv[type];
       double rx = xr[type] - sv * mr;
       et = (rx * rx) / det;
     }

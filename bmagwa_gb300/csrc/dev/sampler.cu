@@ -31,7 +31,20 @@
 
 #define LOG_HALF_D -0.69314718055994528622676398299518041312694549560546875
 
+// Cholesky factors and v of both models stay in shared memory while their
+// order is at most SMK; larger models live in global memory (same packed
+// upper-triangular layout: column c holds rows 0..c at c (c + 1) / 2).
+#define SMK 128
+#define SM_TRI (SMK * (SMK + 1) / 2)
+
 struct MoveShared {
+  DevModel mod[2];      // current (0) and proposed (1) model headers
+  DevChain chs;         // the chain's dynamic state
+  double Ls[2][SM_TRI];
+  double vs[2][SMK];
+  double tv[2][SMK];    // work vectors for beta and its mean
+  double cs[SMK], sn[SMK];  // Givens rotations of a downdate
+  int l_smem[2];        // factor and v of model i are in shared memory
   uint32_t move_inds[BMG_MAX_MS + 1];
   uint32_t move_add[BMG_MAX_MS + 1];
   uint32_t move_rem[BMG_MAX_MS + 1];
@@ -87,10 +100,10 @@ struct Warp {
   unsigned km;
 
   __device__ Warp(const DevConst& k, int chain, MoveShared& sh)
-  : K(k), c(chain), ch(k.ch + chain), cur(k.cur + chain), nm(k.nm + chain), s(sh),
+  : K(k), c(chain), ch(&sh.chs), cur(&sh.mod[0]), nm(&sh.mod[1]), s(sh),
     lane(threadIdx.x & 31), km(k.km)
   {
-    rng = ch->rng;
+    rng = sh.chs.rng;
   }
 
   __device__ void fail(int code)
@@ -196,26 +209,60 @@ struct Warp {
   }
 
   // ------------------------------------------------------- model arrays
+  __device__ static size_t TRI(int r, int col) { return (size_t)col * (col + 1) / 2 + r; }
+  __device__ int midx(const DevModel* M) const { return M == cur ? 0 : 1; }
+  __device__ double* Lb(const DevModel* M) const
+  {
+    int i = midx(M);
+    return s.l_smem[i] ? s.Ls[i] : M->l;
+  }
+  __device__ double* Vb(const DevModel* M) const
+  {
+    int i = midx(M);
+    return s.l_smem[i] ? s.vs[i] : M->v;
+  }
   __device__ double& XX(DevModel* M, int r, int col) const { return M->xx[(size_t)col * km + r]; }
-  __device__ double& L(DevModel* M, int r, int col) const { return M->l[(size_t)col * km + r]; }
+  __device__ double& L(DevModel* M, int r, int col) const { return Lb(M)[TRI(r, col)]; }
+
+  // move a model's factor and v from shared to global memory (it outgrew SMK)
+  __device__ void spill(DevModel* M)
+  {
+    int i = midx(M);
+    if (!s.l_smem[i]) return;
+    size_t tri = TRI(0, min(M->llen, SMK));
+    for (size_t q = lane; q < tri; q += 32) M->l[q] = s.Ls[i][q];
+    for (int q = lane; q < min(M->vlen, SMK); q += 32) M->v[q] = s.vs[i][q];
+    __syncwarp();
+    if (lane == 0) s.l_smem[i] = 0;
+    __syncwarp();
+  }
 
   /* src/model.hpp:115-162: copy the active parts of a model */
   __device__ void copy_model(DevModel* d, const DevModel* src)
   {
     int xc = src->xcols, ll = src->llen;
+    if (ll > SMK || src->vlen > SMK) spill(d);
     for (int col = 0; col < xc; ++col)
       for (int r = lane; r <= col; r += 32) d->xx[(size_t)col * km + r] = src->xx[(size_t)col * km + r];
-    for (int col = 0; col < ll; ++col)
-      for (int r = lane; r <= col; r += 32) d->l[(size_t)col * km + r] = src->l[(size_t)col * km + r];
+    {
+      const double* ls = Lb(src);
+      double* ld = Lb(d);
+      size_t tri = TRI(0, ll);
+      for (size_t q = lane; q < tri; q += 32) ld[q] = ls[q];
+    }
     for (int i = lane; i < xc; i += 32) {
       d->xy[i] = src->xy[i];
       d->inv[i] = src->inv[i];
       d->xc_snp[i] = src->xc_snp[i];
       d->xc_type[i] = src->xc_type[i];
     }
+    {
+      const double* vs = Vb(src);
+      double* vd = Vb(d);
+      for (int i = lane; i < src->vlen; i += 32) vd[i] = vs[i];
+    }
     int vb = max(src->vlen, src->blen);
     for (int i = lane; i < vb; i += 32) {
-      d->v[i] = src->v[i];
       d->beta[i] = src->beta[i];
       d->mu_beta[i] = src->mu_beta[i];
     }
@@ -246,11 +293,13 @@ struct Warp {
   // solve U' x = b in place (forward substitution), U = first len of L
   __device__ void trsv_T(const DevModel* M, double* x, int len)
   {
+    const double* lb = Lb(M);
     for (int j = 0; j < len; ++j) {
+      const double* colj = lb + TRI(0, j);
       double part = 0.0;
-      for (int i = lane; i < j; i += 32) part += M->l[(size_t)j * km + i] * x[i];
+      for (int i = lane; i < j; i += 32) part += colj[i] * x[i];
       part = warp_sum_d(part);
-      double xj = (x[j] - part) / M->l[(size_t)j * km + j];
+      double xj = (x[j] - part) / colj[j];
       __syncwarp();
       if (lane == 0) x[j] = xj;
       __syncwarp();
@@ -259,12 +308,14 @@ struct Warp {
   // solve U x = b in place (back substitution, column sweep)
   __device__ void trsv_N(const DevModel* M, double* x, int len)
   {
+    const double* lb = Lb(M);
     for (int j = len - 1; j >= 0; --j) {
+      const double* colj = lb + TRI(0, j);
       double xj = x[j];
       __syncwarp();
       if (xj != 0.0) {
-        xj = xj / M->l[(size_t)j * km + j];
-        for (int i = lane; i < j; i += 32) x[i] -= xj * M->l[(size_t)j * km + i];
+        xj = xj / colj[j];
+        for (int i = lane; i < j; i += 32) x[i] -= xj * colj[i];
         if (lane == 0) x[j] = xj;
       }
       __syncwarp();
@@ -287,28 +338,33 @@ struct Warp {
       return;
     }
     if (lane == 0) ch->n_lik_full++;
+    if (m > SMK) spill(M);
+    double* lb = Lb(M);
+    double* vb = Vb(M);
     for (int col = 0; col < m; ++col)
-      for (int r = lane; r <= col; r += 32) M->l[(size_t)col * km + r] = M->xx[(size_t)col * km + r];
+      for (int r = lane; r <= col; r += 32) lb[TRI(r, col)] = M->xx[(size_t)col * km + r];
     __syncwarp();
     double log_sum_2 = 0;
-    if (lane == 0) M->l[0] += M->inv[0];
+    if (lane == 0) lb[0] += M->inv[0];
     for (int i = 1; i < m; ++i) {
-      if (lane == 0) M->l[(size_t)i * km + i] += M->inv[i];
+      if (lane == 0) lb[TRI(i, i)] += M->inv[i];
       log_sum_2 += log(M->inv[i]);
     }
     __syncwarp();
     double ldq = 0.5 * log_sum_2;
     bool ok = true;
     for (int j = 0; j < m && ok; ++j) {
-      double ajj = M->l[(size_t)j * km + j] - dot(&M->l[(size_t)j * km], &M->l[(size_t)j * km], j);
+      double* colj = lb + TRI(0, j);
+      double ajj = colj[j] - dot(colj, colj, j);
       if (ajj <= 0.0 || isnan(ajj)) { ok = false; break; }
       ajj = sqrt(ajj);
       __syncwarp();
-      if (lane == 0) M->l[(size_t)j * km + j] = ajj;
+      if (lane == 0) colj[j] = ajj;
       for (int cc = j + 1 + lane; cc < m; cc += 32) {
-        double t = M->l[(size_t)cc * km + j];
-        for (int q = 0; q < j; ++q) t -= M->l[(size_t)j * km + q] * M->l[(size_t)cc * km + q];
-        M->l[(size_t)cc * km + j] = t / ajj;
+        double* colc = lb + TRI(0, cc);
+        double t = colc[j];
+        for (int q = 0; q < j; ++q) t -= colj[q] * colc[q];
+        colc[j] = t / ajj;
       }
       __syncwarp();
     }
@@ -326,12 +382,12 @@ struct Warp {
       __syncwarp();
       return;
     }
-    for (int i = lane; i < m; i += 32) M->v[i] = M->xy[i];
+    for (int i = lane; i < m; i += 32) vb[i] = M->xy[i];
     __syncwarp();
-    trsv_T(M, M->v, m);
-    double vv = dot(M->v, M->v, m);
+    trsv_T(M, vb, m);
+    double vv = dot(vb, vb, m);
     double ldqx = 0;
-    for (int i = 0; i < m; ++i) ldqx += log(M->l[(size_t)i * km + i]);
+    for (int i = 0; i < m; ++i) ldqx += log(lb[TRI(i, i)]);
     double syx = K.nus2_plus_yy - vv;
     if (lane == 0) {
       M->vlen = m;
@@ -344,20 +400,13 @@ struct Warp {
   }
 
   // ------------------------------------------------- genotype products
-  // sum_i x_t(g_i) * Y_i with a fixed-point vector Y (length n)
-  __device__ long long geno_dot_fixed(uint32_t snp, int term, const int64_t* Y)
+  // sum_i x_t(g_i) * vec_i for the phenotype (v = 0) or covariate v, in the
+  // vector's fixed point, from the per-SNP H and R sums
+  __device__ long long geno_dot_fixed(uint32_t snp, int term, int v)
   {
-    const uint8_t* row = K.geno + (size_t)snp * K.gs;
-    long long acc;
-    // lanes take individuals lane, lane+32, ...: each reads its own 2 bits
-    acc = 0;
-    for (uint64_t i = lane; i < K.n; i += 32) {
-      int code = (row[i >> 2] >> ((i & 3) * 2)) & 3;
-      int v = term_value(code, term);
-      if (v == 1) acc += Y[i];
-      else if (v == 2) acc += 2 * Y[i];
-    }
-    return warp_sum_ll(acc);
+    const size_t nv = K.m_e > 1 ? K.m_e : 1;
+    const int64_t* g = K.gsum + ((size_t)snp * nv + v) * 2;
+    return (long long)coefH(term) * g[0] + (long long)coefR(term) * g[1];
   }
   // exact sum_i x_t(g_a,i) x_u(g_b,i) from the 2-bit codes
   __device__ long long geno_cross(uint32_t a, int t, uint32_t b, int u)
@@ -386,10 +435,60 @@ struct Warp {
   {
     if (r < (int)K.m_e) {
       if (r == 0) return (double)term_sum(K.cnt, snp, term);
-      long long acc = geno_dot_fixed(snp, term, K.eint + (size_t)r * K.n);
+      long long acc = geno_dot_fixed(snp, term, r);
       return (double)acc * ldexp(1.0, -K.se[r]);
     }
     return (double)geno_cross(M->xc_snp[r], M->xc_type[r], snp, term);
+  }
+  // The same for the genotype columns r0 <= r < r1, four at a time: each
+  // word of the new column is loaded once per four model columns, and the
+  // four rows' loads are independent.  Exact integer popcounts.
+  __device__ void cross_cols(const DevModel* M, int r0, int r1, uint32_t snp, int term, double* out)
+  {
+    const uint64_t* rb = (const uint64_t*)(K.geno + (size_t)snp * K.gs);
+    const unsigned nw64 = K.gs / 8;
+    const uint64_t m5 = 0x5555555555555555ull;
+    const int cHu = coefH(term), cRu = coefR(term);
+    for (int r = r0; r < r1; r += 4) {
+      const int cnt = min(4, r1 - r);
+      const uint64_t* ra[4];
+      int cH[4], cR[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int idx = r + min(q, cnt - 1);
+        ra[q] = (const uint64_t*)(K.geno + (size_t)M->xc_snp[idx] * K.gs);
+        cH[q] = coefH(M->xc_type[idx]);
+        cR[q] = coefR(M->xc_type[idx]);
+      }
+      int hh[4] = {0, 0, 0, 0}, hr[4] = {0, 0, 0, 0}, rh[4] = {0, 0, 0, 0}, rr[4] = {0, 0, 0, 0};
+      for (unsigned w = lane; w < nw64; w += 32) {
+        const uint64_t y = rb[w];
+        const uint64_t yh = (y >> 1) & m5, yl = y & m5;
+        const uint64_t Hy = yh & ~yl, Ry = yh & yl;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const uint64_t x = ra[q][w];
+          const uint64_t xh = (x >> 1) & m5, xl = x & m5;
+          const uint64_t Hx = xh & ~xl, Rx = xh & xl;
+          hh[q] += __popcll(Hx & Hy);
+          hr[q] += __popcll(Hx & Ry);
+          rh[q] += __popcll(Rx & Hy);
+          rr[q] += __popcll(Rx & Ry);
+        }
+      }
+      long long v[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        v[q] = (long long)cH[q] * cHu * hh[q] + (long long)cH[q] * cRu * hr[q] +
+               (long long)cR[q] * cHu * rh[q] + (long long)cR[q] * cRu * rr[q];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) v[q] += __shfl_xor_sync(FULL_MASK, v[q], o);
+      }
+      if (lane == 0)
+        for (int q = 0; q < cnt; ++q) out[r + q] = (double)v[q];
+    }
   }
 
   // --------------------------------------------------------- model updates
@@ -397,6 +496,7 @@ struct Warp {
   __device__ void upd_add(DevModel* M, uint32_t snp, int mi, int term, bool is2, double invv, bool update)
   {
     int col = M->xcols;
+    if (col + 1 > SMK) spill(M);
     if (lane == 0) {
       if (is2) M->x_ind2[mi] = col;
       else { M->x_ind1[mi] = col; M->x_ind2[mi] = 0; }
@@ -405,15 +505,18 @@ struct Warp {
       M->xcols = col + 1;
       M->inv[col] = invv;
     }
-    long long xyi = geno_dot_fixed(snp, term, K.yint);
+    long long xyi = geno_dot_fixed(snp, term, 0);
     double xyc = (double)xyi * ldexp(1.0, -K.sy);
     __syncwarp();
     if (lane == 0) M->xy[col] = xyc;
     double* xxcol = &M->xx[(size_t)col * km];
-    for (int r = 0; r <= col; ++r) {
-      double v = (r == col) ? (double)term_cross_same(K.cnt, snp, term, term) : cross_col(M, r, snp, term);
+    const int me = min((int)K.m_e, col);
+    for (int r = 0; r < me; ++r) {
+      double v = cross_col(M, r, snp, term);
       if (lane == 0) xxcol[r] = v;
     }
+    cross_cols(M, me, col, snp, term, xxcol);
+    if (lane == 0) xxcol[col] = (double)term_cross_same(K.cnt, snp, term, term);
     __syncwarp();
     if (!update) {
       if (lane == 0) { M->llen = col + 1; M->vlen = col + 1; }
@@ -421,7 +524,7 @@ struct Warp {
       return;
     }
     if (lane == 0) ch->n_lik_add++;
-    double* lcol = &M->l[(size_t)col * km];
+    double* lcol = Lb(M) + TRI(0, col);
     for (int r = lane; r <= col; r += 32) lcol[r] = xxcol[r];
     __syncwarp();
     trsv_T(M, lcol, col);
@@ -439,7 +542,8 @@ struct Warp {
       return;
     }
     double lcc = sqrt(lmm2);
-    double vm2 = M->xy[col] - dot(lcol, M->v, col);
+    double* vb = Vb(M);
+    double vm2 = M->xy[col] - dot(lcol, vb, col);
     double vc = vm2 / lcc;
     double syx = M->syx - vc * vc;
     double ldq = M->ldq + 0.5 * log(invv);
@@ -448,7 +552,7 @@ struct Warp {
     if (lane == 0) {
       lcol[col] = lcc;
       M->vlen = col + 1;
-      M->v[col] = vc;
+      vb[col] = vc;
       M->syx = syx;
       M->ldq = ldq;
       M->ldqx = ldqx;
@@ -497,11 +601,12 @@ struct Warp {
   __device__ void dchex_left(DevModel* M, int x_ind, int order, double* cs, double* sn)
   {
     // one lane: the rotation chain is sequential
+    if (order <= SMK) { cs = s.cs; sn = s.sn; }
     if (lane == 0) {
       const int k = x_ind + 1, l = order, p = order;
       const int km1 = k - 1, lmk = l - k;
-      double* r = M->l;
-#define R_(i, j) r[(size_t)((j) - 1) * km + (size_t)((i) - 1)]
+      double* r = Lb(M);
+#define R_(i, j) r[TRI((i) - 1, (j) - 1)]
       for (int i = 1; i <= k; ++i) sn[lmk + i - 1] = R_(i, k);
       for (int j = k; j <= l - 1; ++j) {
         for (int i = 1; i <= j; ++i) R_(i, j) = R_(i, j + 1);
@@ -567,8 +672,8 @@ struct Warp {
     if (lane == 0) { M->xcols = xc; ch->n_lik_rem++; }
     __syncwarp();
     if (x_ind == xc) {
-      double lxx = M->l[(size_t)x_ind * km + x_ind];
-      double vx = M->v[x_ind];
+      double lxx = L(M, x_ind, x_ind);
+      double vx = Vb(M)[x_ind];
       double ldqx = M->ldqx - log(lxx);
       double syx = M->syx + vx * vx;
       __syncwarp();
@@ -584,17 +689,18 @@ struct Warp {
       dchex_left(M, x_ind, order, cs, sn);
       int nl = order - 1;
       for (int i = x_ind; i < nl; ++i) {
-        if (M->l[(size_t)i * km + i] < 0) {
-          for (int j = i + lane; j < nl; j += 32) M->l[(size_t)j * km + i] *= -1;
+        if (L(M, i, i) < 0) {
+          for (int j = i + lane; j < nl; j += 32) L(M, i, j) *= -1;
         }
         __syncwarp();
       }
-      for (int i = lane; i < xc; i += 32) M->v[i] = M->xy[i];
+      double* vb = Vb(M);
+      for (int i = lane; i < xc; i += 32) vb[i] = M->xy[i];
       __syncwarp();
-      trsv_T(M, M->v, nl);
+      trsv_T(M, vb, nl);
       double ldqx = 0;
-      for (int i = 0; i < nl; ++i) ldqx += log(M->l[(size_t)i * km + i]);
-      double syx = K.nus2_plus_yy - dot(M->v, M->v, xc);
+      for (int i = 0; i < nl; ++i) ldqx += log(L(M, i, i));
+      double syx = K.nus2_plus_yy - dot(vb, vb, xc);
       if (lane == 0) {
         M->llen = nl;
         M->vlen = xc;
@@ -660,25 +766,29 @@ struct Warp {
   {
     double s2 = sinvchi2(M->syx / K.n_plus_nu);
     int len = M->vlen;
+    // the triangular solves run on shared copies when the model fits
+    const bool on_chip = len <= SMK && M->llen <= SMK;
+    double* mu = on_chip ? s.tv[0] : M->mu_beta;
+    double* bt = on_chip ? s.tv[1] : M->beta;
     if (!M->mu_beta_computed) {
-      for (int i = lane; i < len; i += 32) M->mu_beta[i] = M->v[i];
+      const double* vb = Vb(M);
+      for (int i = lane; i < len; i += 32) mu[i] = vb[i];
       __syncwarp();
-      trsv_N(M, M->mu_beta, M->llen);
+      trsv_N(M, mu, M->llen);
       if (lane == 0) M->mu_beta_computed = 1;
+    } else if (on_chip) {
+      for (int i = lane; i < len; i += 32) mu[i] = M->mu_beta[i];
     }
-    // the normals are drawn in order by every lane; lane i keeps draw i
-    for (int base = 0; base < len; base += 32) {
-      double z = 0;
-      for (int i = 0; i < 32 && base + i < len; ++i) {
-        double d = nrm();
-        if (i == lane) z = d;
-      }
-      if (base + lane < len) M->beta[base + lane] = z;
-    }
+    // normal i of the vector is the chain's draw at slot + i
+    for (int i = lane; i < len; i += 32) bt[i] = bmg_normal_at(rng.key0, rng.key1, rng.slot + i);
+    rng.slot += len;
     __syncwarp();
-    trsv_N(M, M->beta, M->llen);
+    trsv_N(M, bt, M->llen);
     double sc = sqrt(s2);
-    for (int i = lane; i < len; i += 32) M->beta[i] = sc * M->beta[i] + M->mu_beta[i];
+    for (int i = lane; i < len; i += 32) {
+      M->beta[i] = sc * bt[i] + mu[i];
+      if (on_chip) M->mu_beta[i] = mu[i];
+    }
     if (lane == 0) {
       M->sigma2 = s2;
       M->blen = len;
@@ -1330,9 +1440,13 @@ struct Warp {
         q_p = __dmul_rn(q_p, q);
       }
       __syncwarp();
-      double p_best = 0.01, pp = 0.01, h_best = -INFINITY;
-      double step = 0.98 / 49.0;
-      for (int j = 0; j < 50; ++j) {
+      // grid point j = lane, lane + 32 (the host table holds the grid's
+      // sequentially accumulated values); the first strict maximum wins, as
+      // in the reference's ascending loop, and 0.01 when none is finite
+      double hb = -INFINITY;
+      int jb = 1 << 30;
+      for (int j = lane; j < 50; j += 32) {
+        const double pp = K.ms_grid[j];
         double h = 0.0, z = 0.0, qq = 1.0 - pp, qp = pp;
         for (int i = 0; i < mx; ++i) {
           double ratio = __ddiv_rn(qp, q_p0[i]);
@@ -1341,10 +1455,14 @@ struct Warp {
           qp = __dmul_rn(qp, qq);
         }
         h = __ddiv_rn(h, z);
-        if (h > h_best) { h_best = h; p_best = pp; }
-        pp = __dadd_rn(pp, step);
+        if (h > hb) { hb = h; jb = j; }
       }
-      pms = p_best;
+      for (int o = 16; o > 0; o >>= 1) {
+        const double ho = __shfl_xor_sync(FULL_MASK, hb, o);
+        const int jo = __shfl_xor_sync(FULL_MASK, jb, o);
+        if (ho > hb || (ho == hb && jo < jb)) { hb = ho; jb = jo; }
+      }
+      pms = (hb > -INFINITY) ? K.ms_grid[jb] : 0.01;
     }
     // Utils::geometric_dist_cdf
     double* qms = K.q_ms + (size_t)c * 256;
@@ -1472,7 +1590,7 @@ __device__ void bulk_phase(const DevConst& K, int c, MoveShared& s, BulkCols& bc
     if (mode & BULK_PVE) {
       double m = 0;
       for (int ww = 0; ww < (nth >> 5); ++ww) m = fmax(m, s.bmax[ww]);
-      K.ch[c].yhat_absmax = m;
+      s.chs.yhat_absmax = m;
     }
   }
   __syncthreads();
@@ -1573,7 +1691,10 @@ __device__ void prep_rb(Warp& W, bool scan_only)
     rp->inv_2s2 = 1.0 / (2 * M->sigma2);
     rp->scale = ldexp(1.0, -W.s.bulk_s);
     rp->mr = (double)W.s.bsuml[0] * ldexp(1.0, -W.s.bulk_s) / (double)K.n;
-    for (int t = 0; t < 4; ++t) rp->itv[t] = ch->inv_t2a2[t];
+    for (int t = 0; t < 4; ++t) {
+      rp->itv[t] = ch->inv_t2a2[t];
+      rp->nlog_itv[t] = -log(ch->inv_t2a2[t]);
+    }
   }
   // log prior changes of the scan (src/sampler.cpp:51-76)
   int Ns[5];
@@ -1609,18 +1730,81 @@ __device__ void prep_rb(Warp& W, bool scan_only)
 }
 
 // ------------------------------------------------------------- kernels
+// A move CTA's shared memory: ~190 KB, so it is dynamic (one CTA per SM).
+struct MoveSmem {
+  MoveShared s;
+  BulkCols bc;
+  long long part[BMG_MOVE_THREADS];
+};
+static_assert(sizeof(MoveSmem) <= 227 * 1024, "a move CTA's shared memory exceeds one SM's");
+
+__device__ __forceinline__ MoveSmem& move_smem()
+{
+  extern __shared__ __align__(16) unsigned char bmg_move_dsm[];
+  return *reinterpret_cast<MoveSmem*>(bmg_move_dsm);
+}
+
+template <class T>
+__device__ void block_copy(T* dst, const T* src)
+{
+  static_assert(sizeof(T) % 4 == 0, "word copy");
+  uint32_t* d = reinterpret_cast<uint32_t*>(dst);
+  const uint32_t* q = reinterpret_cast<const uint32_t*>(src);
+  for (unsigned i = threadIdx.x; i < sizeof(T) / 4; i += blockDim.x) d[i] = q[i];
+}
+
+// All threads: chain c's dynamic state and both model headers into shared
+// memory, with the factors and v of each model that fits in SMK.
+__device__ void load_state(const DevConst& K, int c, MoveShared& s)
+{
+  block_copy(&s.chs, K.ch + c);
+  block_copy(&s.mod[0], K.cur + c);
+  block_copy(&s.mod[1], K.nm + c);
+  __syncthreads();
+  for (int i = 0; i < 2; ++i) {
+    const DevModel& M = s.mod[i];
+    const bool on = M.llen <= SMK && M.vlen <= SMK && M.xcols <= SMK;
+    if (on) {
+      const size_t tri = (size_t)M.llen * (M.llen + 1) / 2;
+      for (size_t q = threadIdx.x; q < tri; q += blockDim.x) s.Ls[i][q] = M.l[q];
+      for (int q = threadIdx.x; q < M.vlen; q += blockDim.x) s.vs[i][q] = M.v[q];
+    }
+    if (threadIdx.x == 0) s.l_smem[i] = on;
+  }
+  __syncthreads();
+}
+
+// All threads: the inverse of load_state.
+__device__ void store_state(const DevConst& K, int c, MoveShared& s)
+{
+  __syncthreads();
+  for (int i = 0; i < 2; ++i) {
+    const DevModel& M = s.mod[i];
+    if (!s.l_smem[i]) continue;
+    const int ll = min(M.llen, SMK);
+    const size_t tri = (size_t)ll * (ll + 1) / 2;
+    for (size_t q = threadIdx.x; q < tri; q += blockDim.x) M.l[q] = s.Ls[i][q];
+    for (int q = threadIdx.x; q < min(M.vlen, SMK); q += blockDim.x) M.v[q] = s.vs[i][q];
+  }
+  block_copy(K.ch + c, &s.chs);
+  block_copy(K.cur + c, &s.mod[0]);
+  block_copy(K.nm + c, &s.mod[1]);
+}
+
 // Model of every chain at construction (src/model.hpp:49-113): the covariate
 // block is set by the host; here its likelihood, then new = current.
 extern "C" __global__ void __launch_bounds__(32)
 bmg_init_kernel(DevConst K)
 {
-  __shared__ MoveShared s;
+  MoveShared& s = move_smem().s;
+  load_state(K, blockIdx.x, s);
   if (threadIdx.x == 0) s.err = 0;
   __syncwarp();
   Warp W(K, blockIdx.x, s);
   W.compute_log_likelihood(W.cur);
   W.copy_model(W.nm, W.cur);
   if (W.lane == 0 && s.err) W.ch->error = s.err;
+  store_state(K, blockIdx.x, s);
 }
 
 // Residual limbs and RbParams of every chain at its current beta, for a scan
@@ -1628,9 +1812,10 @@ bmg_init_kernel(DevConst K)
 extern "C" __global__ void __launch_bounds__(BMG_MOVE_THREADS, 1)
 bmg_rbprep_kernel(DevConst K)
 {
-  __shared__ MoveShared s;
-  __shared__ BulkCols bc;
+  MoveShared& s = move_smem().s;
+  BulkCols& bc = move_smem().bc;
   const int c = blockIdx.x, tid = threadIdx.x;
+  load_state(K, c, s);
   if (tid == 0) s.err = 0;
   __syncthreads();
   Warp W(K, c, s);
@@ -1639,8 +1824,9 @@ bmg_rbprep_kernel(DevConst K)
   bulk_phase(K, c, s, bc);
   if (tid < 32) {
     prep_rb(W, true);
-    if (W.lane == 0) K.ch[c].rng = W.rng;
+    if (W.lane == 0) s.chs.rng = W.rng;
   }
+  store_state(K, c, s);
 }
 
 // Runs iterations of chain blockIdx.x until `max_iters` are done or an RB
@@ -1648,12 +1834,13 @@ bmg_rbprep_kernel(DevConst K)
 extern "C" __global__ void __launch_bounds__(BMG_MOVE_THREADS, 1)
 bmg_move_kernel(DevConst K, int max_iters)
 {
-  __shared__ MoveShared s;
-  __shared__ BulkCols bc;
-  __shared__ long long part[BMG_MOVE_THREADS];
+  MoveShared& s = move_smem().s;
+  BulkCols& bc = move_smem().bc;
+  long long* part = move_smem().part;
   const int c = blockIdx.x;
   const int tid = threadIdx.x;
-  DevChain* ch = K.ch + c;
+  load_state(K, c, s);
+  DevChain* ch = &s.chs;
   if (tid == 0) {
     s.err = ch->error;
     s.n_pend = ch->n_pend;
@@ -1698,7 +1885,7 @@ bmg_move_kernel(DevConst K, int max_iters)
     // room for one more move's flips of dd_add, else rebuild its prefix here
     if (s.n_pend > BMG_PEND_MAX - 2 * (int)K.max_move_size - 2) {
       if (tid == 0) ch->n_pend = 0;
-      rebuild_chain(K, c, part);
+      rebuild_chain(K, c, part, ch);
       if (tid == 0) s.n_pend = 0;
       __syncthreads();
     }
@@ -1871,4 +2058,18 @@ bmg_move_kernel(DevConst K, int max_iters)
     for (int i = 0; i < s.n_pend; ++i) ch->pend_snp[i] = s.pend_snp[i];
     if (s.err) ch->error = s.err;
   }
+  store_state(K, c, s);
+}
+
+// dynamic shared memory of the three kernels above
+extern "C" cudaError_t bmg_move_configure(size_t* smem_bytes)
+{
+  const int bytes = (int)sizeof(MoveSmem);
+  cudaError_t e = cudaFuncSetAttribute(bmg_init_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(bmg_rbprep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(bmg_move_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (smem_bytes) *smem_bytes = sizeof(MoveSmem);
+  return e;
 }

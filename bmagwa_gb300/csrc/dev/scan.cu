@@ -60,5 +60,5 @@ bmg_rebuild_kernel(DevConst K, int force)
   __shared__ long long part[1024];
   const int c = blockIdx.x;
   if (!force && !K.ch[c].rebuild) return;
-  rebuild_chain(K, c, part);
+  rebuild_chain(K, c, part, K.ch + c);
 }

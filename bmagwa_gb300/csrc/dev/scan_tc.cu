@@ -24,7 +24,7 @@
 namespace {
 
 constexpr int TC_THREADS = 192;
-constexpr int TC_STAGES = 4;
+constexpr int TC_STAGES = 2;         // two CTAs per SM: one's epilogue overlaps the other's main loop
 constexpr int TC_BM = 128;          // rows of D per CTA
 constexpr int TC_BK = 64;           // individuals per stage (128 bytes of bf16)
 constexpr uint32_t WAIT_LIMIT = 1u << 24;
@@ -135,7 +135,7 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v)
 
 }  // namespace
 
-extern "C" __global__ void __launch_bounds__(TC_THREADS, 1)
+extern "C" __global__ void __launch_bounds__(TC_THREADS, 2)
 bmg_scan_tc_kernel(DevConst K, TcParams P, const __grid_constant__ CUtensorMap map_b,
                    const __grid_constant__ CUtensorMap map_g)
 {
@@ -261,10 +261,12 @@ bmg_scan_tc_kernel(DevConst K, TcParams P, const __grid_constant__ CUtensorMap m
   if (timed_out) {
     if (tid == 0) atomicExch(&K.ch[0].error, BMG_DERR_TIMEOUT);
   } else {
-    // one unit per (SNP, chain): combine the digits, then the RB epilogue
+    // one unit per (SNP, chain), SNPs fastest so that a warp's stores to the
+    // chain-major running means are contiguous: combine the digits, then the
+    // RB epilogue
     const uint32_t units = P.snps_per_tile * chains_here;
     for (uint32_t u = tid; u < units; u += TC_THREADS) {
-      uint32_t cl = u % chains_here, sl = u / chains_here;
+      uint32_t sl = u % P.snps_per_tile, cl = u / P.snps_per_tile;
       uint64_t j = (uint64_t)snp0 + sl;
       uint32_t c = chain0 + cl;
       if (j >= K.p || !K.rb[c].do_scan) continue;

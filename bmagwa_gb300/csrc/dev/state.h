@@ -108,6 +108,7 @@ struct RbParams {
   double mr;                // mean residual
   double scale;             // 2^-s of the fixed-point residual
   double itv[4];            // inv_tau2_alpha2 per term (shared tau2)
+  double nlog_itv[4];       // -log(itv[t]), once per chain
   double lmp_add[5];
   double lmp_rem[5][5];
   double rao_z1, rao_z2;    // running-mean weights of p_rao
@@ -204,6 +205,7 @@ struct DevConst {
   int32_t sy;
   const double* e;      // n x m_e column-major (column 0 = 1)
   const int64_t* eint;  // m_e x n fixed point covariates (column 0 unused)
+  const int64_t* gsum;  // p x max(m_e,1) x 2: H and R sums of y (v = 0) and covariate v, fixed point
   const int32_t* se;    // per covariate scale exponent
   const double* ee;     // m_e x m_e upper: E'E (host, FP64)
   const double* ey;     // m_e: E'y

@@ -135,3 +135,26 @@ def test_tc_scan_bitwise_equals_simt(bmg, tmp_path):
         b, bt = res[0][0].last_scan(c)
         assert np.array_equal(a, b)
         assert np.array_equal(at, bt)
+
+
+def test_setup_is_ordered_against_a_busy_default_stream(bmg, tmp_path):
+    """The context's allocations, zeroing and uploads all go on its own
+    stream: queued work on the caller's default stream must not reorder them
+    (every chain starts from the covariate block's finite likelihood)."""
+    import math
+    import torch
+    opt, packed, y, e = synth_case(bmg, tmp_path, "plain", n=800, p=3000, chains=24, iters=10, n_rao=1)
+    x = torch.randn(4096, 4096, device="cuda")
+    for _ in range(40):
+        x = torch.tanh(x @ x * 1e-3)
+    ctx = bmg.Context(opt)
+    ctx.load_bed(packed)
+    ctx.set_phenotypes(y)
+    ctx.set_covariates(e)
+    ctx.precompute()
+    lls = [ctx.state(c)[0].log_likelihood for c in range(opt.n_chains)]
+    assert all(math.isfinite(v) for v in lls), lls
+    assert len(set(lls)) == 1
+    ctx.run(5, collect=False)
+    torch.cuda.synchronize()
+    ctx.close()
