@@ -230,7 +230,11 @@ def run_gb300(args, wl):
     # roofline of the scan kernel
     p, n, C = wl["p"], wl["n"], wl["chains"]
     scan_ms = ms[1] / max(1, n_scans)
-    alg_bytes = p * ((n + 3) // 4) + p * C * (8 + 16) + C * n * 8
+    # packed genotypes + per (SNP, chain) the p_r write and one running mean
+    # read and written (p_proposal during burn-in, p_rao after) + the residual
+    # limbs (L bf16 digits per individual and chain)
+    L = int(o.scan_limbs) if o.scan_limbs else 6
+    alg_bytes = p * ((n + 3) // 4) + p * C * (8 + 16) + C * n * 2 * L
     peak, peak_kind = peak_hbm()
     achieved = alg_bytes / (scan_ms / 1000.0) / 1e9 if scan_ms > 0 else None
     out = {
