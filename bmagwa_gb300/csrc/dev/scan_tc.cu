@@ -9,11 +9,15 @@
 //      65,536, so D holds exact integers and x' r = sum_l D[., c L + l] 256^l
 //      is exact: the same int64 the SIMT scan produces.
 //
-// CTA roles (192 threads): warps 0-3 decode A and, after the main loop, read
-// the accumulator rows from tensor memory; warp 4 issues the TMA loads of the
-// packed genotype rows and of the residual digits; warp 5 owns tensor memory
-// and issues the MMAs.  Stages are handed over with mbarriers; every wait is
-// bounded and reports a timeout in the chain error word instead of spinning.
+// Persistent, warp-specialised: one CTA per SM walks the tiles
+// (tile = blockIdx.x + i gridDim.x).  Warps 0-3 decode A into the swizzled
+// stage buffers, warp 4 issues the TMA loads of the packed genotype rows and
+// of the residual digits, warp 5 owns tensor memory and issues the MMAs into
+// one of two accumulators (2 x 256 columns), and TC_EPI_WARPS epilogue warps
+// drain the other accumulator: tensor memory -> exact int64 sums in shared
+// memory -> the FP64 Rao-Blackwell epilogue.  The epilogue of tile i thus
+// overlaps the main loop of tile i + 1.  Every mbarrier wait is bounded; a
+// timeout sets the chain error word and every role leaves its loop.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
@@ -23,10 +27,13 @@
 
 namespace {
 
-constexpr int TC_THREADS = 192;
-constexpr int TC_STAGES = 2;         // two CTAs per SM: one's epilogue overlaps the other's main loop
-constexpr int TC_BM = 128;          // rows of D per CTA
+constexpr int TC_EPI_WARPS = 12;    // epilogue warps (three per TMEM lane quarter)
+constexpr int TC_THREADS = 192 + 32 * TC_EPI_WARPS;
+constexpr int TC_MAX_STAGES = 4;
+constexpr int TC_BM = 128;          // rows of D per tile
 constexpr int TC_BK = 64;           // individuals per stage (128 bytes of bf16)
+constexpr uint32_t TC_ACC_COLS = 256;  // columns of one accumulator
+constexpr uint32_t TC_TMEM_COLS = 512; // two accumulators
 constexpr uint32_t WAIT_LIMIT = 1u << 24;
 
 struct TcParams {
@@ -35,6 +42,9 @@ struct TcParams {
   uint32_t chains_tile;    // chains per N tile
   uint32_t n_mma;          // N of the MMA (chains_tile * L rounded up to 16)
   uint32_t k_chunks;       // n_pad / TC_BK
+  uint32_t stages;         // pipeline depth (2..TC_MAX_STAGES)
+  uint32_t m_tiles, n_tiles, tiles;
+  uint32_t xr_bytes;       // TC_BM x chains_tile int64 sums
   uint32_t stage_bytes;
   uint32_t b_bytes, a_bytes, pk_bytes;
   int32_t term_of_row[4];  // term of row u of a SNP (-1: unused)
@@ -116,6 +126,11 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar)
                : "memory");
 }
 
+__device__ __forceinline__ void named_bar_sync(uint32_t id, uint32_t threads)
+{
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(threads) : "memory");
+}
+
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v)
 {
   uint32_t r[32];
@@ -135,24 +150,26 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v)
 
 }  // namespace
 
-extern "C" __global__ void __launch_bounds__(TC_THREADS, 2)
+extern "C" __global__ void __launch_bounds__(TC_THREADS, 1)
 bmg_scan_tc_kernel(DevConst K, TcParams P, const __grid_constant__ CUtensorMap map_b,
                    const __grid_constant__ CUtensorMap map_g)
 {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
-  // 1024-byte aligned base for the swizzled tiles
+  // 1024-byte aligned base for the swizzled tiles; the int64 sums follow the stages
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  __shared__ uint64_t full_bar[TC_STAGES], aready_bar[TC_STAGES], empty_bar[TC_STAGES], acc_bar;
+  long long* xr_s = reinterpret_cast<long long*>(smem + P.stages * P.stage_bytes);
+  __shared__ uint64_t full_bar[TC_MAX_STAGES], aready_bar[TC_MAX_STAGES], empty_bar[TC_MAX_STAGES];
+  __shared__ uint64_t acc_full[2], acc_empty[2], drain_bar;
   __shared__ uint32_t tmem_base_sh;
-  __shared__ int timed_out;
+  __shared__ volatile int abort_flag;
+  __shared__ int epi_ok;
   __shared__ uint2 lut[4][256];  // per term: byte -> 4 bf16 values
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const uint32_t m_tile = blockIdx.x, n_tile = blockIdx.y;
-  const uint32_t snp0 = m_tile * P.snps_per_tile;
-  const uint32_t chain0 = n_tile * P.chains_tile;
   const uint32_t L = K.limbs_n;
-  const uint32_t chains_here = min(P.chains_tile, K.n_chains - chain0);
+  const uint32_t nk = P.k_chunks, S = P.stages;
+  const uint32_t ct = P.chains_tile;
+  const uint32_t my_tiles = (P.tiles > blockIdx.x) ? (P.tiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
 
   // decode tables: bf16 bit patterns of 0, 1, 2 are 0x0000, 0x3F80, 0x4000
   for (int e = tid; e < 4 * 256; e += TC_THREADS) {
@@ -166,66 +183,92 @@ bmg_scan_tc_kernel(DevConst K, TcParams P, const __grid_constant__ CUtensorMap m
     lut[term][byte] = make_uint2((uint32_t)h[0] | ((uint32_t)h[1] << 16), (uint32_t)h[2] | ((uint32_t)h[3] << 16));
   }
   if (tid == 0) {
-    for (int s = 0; s < TC_STAGES; ++s) {
-      mbar_init(&full_bar[s], 1);
-      mbar_init(&aready_bar[s], 4);
-      mbar_init(&empty_bar[s], 1);
+    for (uint32_t st = 0; st < S; ++st) {
+      mbar_init(&full_bar[st], 1);
+      mbar_init(&aready_bar[st], 4);
+      mbar_init(&empty_bar[st], 1);
     }
-    mbar_init(&acc_bar, 1);
-    timed_out = 0;
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&acc_full[b], 1);
+      mbar_init(&acc_empty[b], TC_EPI_WARPS);
+    }
+    mbar_init(&drain_bar, 1);
+    abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 5) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_sh)),
-                 "r"(256u));
+                 "r"(TC_TMEM_COLS));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_base_sh;
-  const uint32_t nk = P.k_chunks;
 
   if (warp == 4) {
     if (lane == 0) {
       // TMA producer: packed genotype rows and residual digits of each stage
-      for (uint32_t k = 0; k < nk; ++k) {
-        uint32_t s = k % TC_STAGES;
-        if (k >= TC_STAGES && !mbar_wait(&empty_bar[s], ((k / TC_STAGES) - 1) & 1)) { timed_out = 1; break; }
-        uint8_t* st = smem + s * P.stage_bytes;
-        mbar_arrive_tx(&full_bar[s], P.b_bytes + P.pk_bytes);
-        tma_load_2d(st, &map_b, &full_bar[s], (int)(k * TC_BK), (int)(chain0 * L));
-        tma_load_2d(st + P.b_bytes + P.a_bytes, &map_g, &full_bar[s], (int)(k * (TC_BK / 4)), (int)snp0);
+      uint32_t issued = 0;
+      for (uint32_t i = 0; i < my_tiles && !abort_flag; ++i) {
+        const uint32_t tile = blockIdx.x + i * gridDim.x;
+        const uint32_t snp0 = (tile % P.m_tiles) * P.snps_per_tile;
+        const uint32_t chain0 = (tile / P.m_tiles) * ct;
+        for (uint32_t k = 0; k < nk; ++k) {
+          const uint32_t g = i * nk + k, st = g % S;
+          if (g >= S && !mbar_wait(&empty_bar[st], ((g / S) - 1) & 1)) { abort_flag = 1; break; }
+          uint8_t* sp = smem + st * P.stage_bytes;
+          mbar_arrive_tx(&full_bar[st], P.b_bytes + P.pk_bytes);
+          tma_load_2d(sp, &map_b, &full_bar[st], (int)(k * TC_BK), (int)(chain0 * L));
+          tma_load_2d(sp + P.b_bytes + P.a_bytes, &map_g, &full_bar[st], (int)(k * (TC_BK / 4)), (int)snp0);
+          ++issued;
+        }
       }
+      // no load may still be landing in shared memory when the CTA exits:
+      // wait (bounded) for the last load of every stage
+      for (uint32_t g = issued > S ? issued - S : 0; g < issued; ++g) mbar_wait(&full_bar[g % S], (g / S) & 1);
     }
   } else if (warp == 5) {
     if (lane == 0) {
-      // MMA issuer
+      // MMA issuer: tile i accumulates into buffer i & 1
       const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((P.n_mma >> 3) << 17) | ((uint32_t)(TC_BM >> 4) << 24);
-      for (uint32_t k = 0; k < nk; ++k) {
-        uint32_t s = k % TC_STAGES, par = (k / TC_STAGES) & 1;
-        if (!mbar_wait(&full_bar[s], par) || !mbar_wait(&aready_bar[s], par)) { timed_out = 1; break; }
+      for (uint32_t i = 0; i < my_tiles && !abort_flag; ++i) {
+        const uint32_t b = i & 1, u = i >> 1;
+        if (u >= 1 && !mbar_wait(&acc_empty[b], (u - 1) & 1)) { abort_flag = 1; break; }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        uint8_t* st = smem + s * P.stage_bytes;
-        uint64_t bdesc = smem_desc(st), adesc = smem_desc(st + P.b_bytes);
+        const uint32_t d = tmem + b * TC_ACC_COLS;
+        bool ok = true;
+        for (uint32_t k = 0; k < nk; ++k) {
+          const uint32_t g = i * nk + k, st = g % S, par = (g / S) & 1;
+          if (!mbar_wait(&full_bar[st], par) || !mbar_wait(&aready_bar[st], par)) { ok = false; break; }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          uint8_t* sp = smem + st * P.stage_bytes;
+          uint64_t bdesc = smem_desc(sp), adesc = smem_desc(sp + P.b_bytes);
 #pragma unroll
-        for (int kk = 0; kk < TC_BK / 16; ++kk)  // 16 bf16 = 32 bytes = 2 descriptor units
-          mma_bf16(tmem, adesc + 2 * kk, bdesc + 2 * kk, idesc, (k | kk) != 0);
-        mma_commit(&empty_bar[s]);
+          for (int kk = 0; kk < TC_BK / 16; ++kk)  // 16 bf16 = 32 bytes = 2 descriptor units
+            mma_bf16(d, adesc + 2 * kk, bdesc + 2 * kk, idesc, (k | kk) != 0);
+          mma_commit(&empty_bar[st]);
+        }
+        if (!ok) { abort_flag = 1; break; }
+        mma_commit(&acc_full[b]);
       }
-      mma_commit(&acc_bar);
+      // every MMA issued has completed before tensor memory is freed
+      mma_commit(&drain_bar);
+      if (!mbar_wait(&drain_bar, 0)) abort_flag = 1;
     }
-  } else {
+  } else if (warp < 4) {
     // decode warps: packed 2-bit codes -> bf16 rows of the swizzled A tile
     const uint32_t row = tid;  // 0..127
     const uint32_t sl = row / P.tpad, u = row % P.tpad;
     const int term = P.term_of_row[u];
-    for (uint32_t k = 0; k < nk; ++k) {
-      uint32_t s = k % TC_STAGES, par = (k / TC_STAGES) & 1;
-      if (!mbar_wait(&full_bar[s], par)) { timed_out = 1; break; }
-      uint8_t* st = smem + s * P.stage_bytes;
-      uint8_t* a = st + P.b_bytes;
-      const uint8_t* pk = st + P.b_bytes + P.a_bytes + sl * 16;
+    const uint32_t total = my_tiles * nk;
+    for (uint32_t g = 0; g < total; ++g) {
+      if (abort_flag) break;
+      const uint32_t st = g % S, par = (g / S) & 1;
+      if (!mbar_wait(&full_bar[st], par)) { abort_flag = 1; break; }
+      uint8_t* sp = smem + st * P.stage_bytes;
+      uint8_t* a = sp + P.b_bytes;
+      const uint8_t* pk = sp + P.b_bytes + P.a_bytes + sl * 16;
       uint4 bytes = *reinterpret_cast<const uint4*>(pk);
       uint32_t w[4] = {bytes.x, bytes.y, bytes.z, bytes.w};
 #pragma unroll
@@ -238,54 +281,88 @@ bmg_scan_tc_kernel(DevConst K, TcParams P, const __grid_constant__ CUtensorMap m
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       __syncwarp();
-      if (lane == 0) mbar_arrive(&aready_bar[s]);
+      if (lane == 0) mbar_arrive(&aready_bar[st]);
+    }
+  } else {
+    // epilogue warps: warp w reads TMEM lanes 32 (w % 4) .. +31 (the rows of
+    // the tile); the TC_EPI_WARPS / 4 warps of a quarter split the chains
+    const uint32_t e = warp - 6;
+    const uint32_t quarter = warp & 3, part = e >> 2, nparts = TC_EPI_WARPS / 4;
+    const uint32_t row = quarter * 32 + lane;
+    const uint32_t c_lo = part * ct / nparts, c_hi = (part + 1) * ct / nparts;
+    const uint32_t col_lo = c_lo * L, col_hi = c_hi * L;
+    const uint32_t ethreads = 32 * TC_EPI_WARPS;
+    for (uint32_t i = 0; i < my_tiles; ++i) {
+      const uint32_t tile = blockIdx.x + i * gridDim.x;
+      const uint32_t snp0 = (tile % P.m_tiles) * P.snps_per_tile;
+      const uint32_t chain0 = (tile / P.m_tiles) * ct;
+      const uint32_t chains_here = min(ct, K.n_chains - chain0);
+      const uint32_t b = i & 1, u = i >> 1;
+      // one warp waits; the verdict is shared so that all epilogue warps take
+      // the same number of named-barrier steps
+      if (e == 0) {
+        bool ok = false;
+        if (lane == 0) ok = !abort_flag && mbar_wait(&acc_full[b], u & 1);
+        ok = __shfl_sync(0xffffffffu, ok, 0);
+        if (lane == 0) {
+          epi_ok = ok;
+          if (!ok) abort_flag = 1;
+        }
+      }
+      named_bar_sync(1, ethreads);
+      if (!epi_ok) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      // exact int64 sums: x' r of chain c = sum_l D[row, c L + l] 256^l
+      {
+        uint32_t chain = c_lo, limb = 0;
+        long long acc = 0;
+        for (uint32_t chunk = col_lo & ~31u; chunk < col_hi; chunk += 32) {
+          float v[32];
+          tmem_ld32(tmem + ((quarter * 32) << 16) + b * TC_ACC_COLS + chunk, v);
+#pragma unroll
+          for (uint32_t q = 0; q < 32; ++q) {
+            const uint32_t col = chunk + q;
+            if (col < col_lo || col >= col_hi) continue;
+            // |D| < 2^24: an exact float integer, converted through int32
+            acc += (long long)__float2int_rn(v[q]) * (1ll << (8 * limb));
+            if (++limb == L) {
+              xr_s[row * ct + chain] = acc;
+              acc = 0;
+              limb = 0;
+              ++chain;
+            }
+          }
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&acc_empty[b]);
+      named_bar_sync(1, ethreads);
+      // one unit per (SNP, chain), SNPs fastest so that a warp's stores to
+      // the chain-major running means are contiguous
+      const uint32_t units = P.snps_per_tile * chains_here;
+      for (uint32_t uu = e * 32 + lane; uu < units; uu += ethreads) {
+        const uint32_t sl = uu % P.snps_per_tile, cl = uu / P.snps_per_tile;
+        const uint64_t j = (uint64_t)snp0 + sl;
+        const uint32_t c = chain0 + cl;
+        if (j >= K.p || !K.rb[c].do_scan) continue;
+        long long xr[4] = {0, 0, 0, 0};
+        for (uint32_t q = 0; q < P.tpad; ++q) {
+          const int term = P.term_of_row[q];
+          if (term >= 0) xr[term] = xr_s[(sl * P.tpad + q) * ct + cl];
+        }
+        rb_epilogue(K, (int)c, j, xr);
+      }
+      named_bar_sync(1, ethreads);
     }
   }
 
-  // epilogue: accumulator rows -> shared memory (exact integers in FP32)
-  float* raw = reinterpret_cast<float*>(smem);
-  const uint32_t rstride = P.n_mma + 1;
-  if (warp < 4) {
-    if (!mbar_wait(&acc_bar, 0)) timed_out = 1;
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    for (uint32_t col = 0; col < P.n_mma; col += 32) {
-      float v[32];
-      tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + col, v);
-      const uint32_t row = warp * 32 + lane;
-      const uint32_t nq = min(32u, P.n_mma - col);
-      for (uint32_t q = 0; q < nq; ++q) raw[row * rstride + col + q] = v[q];
-    }
-  }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  if (timed_out) {
-    if (tid == 0) atomicExch(&K.ch[0].error, BMG_DERR_TIMEOUT);
-  } else {
-    // one unit per (SNP, chain), SNPs fastest so that a warp's stores to the
-    // chain-major running means are contiguous: combine the digits, then the
-    // RB epilogue
-    const uint32_t units = P.snps_per_tile * chains_here;
-    for (uint32_t u = tid; u < units; u += TC_THREADS) {
-      uint32_t sl = u % P.snps_per_tile, cl = u / P.snps_per_tile;
-      uint64_t j = (uint64_t)snp0 + sl;
-      uint32_t c = chain0 + cl;
-      if (j >= K.p || !K.rb[c].do_scan) continue;
-      long long xr[4] = {0, 0, 0, 0};
-      for (uint32_t q = 0; q < P.tpad; ++q) {
-        int term = P.term_of_row[q];
-        if (term < 0) continue;
-        const float* rr = raw + (sl * P.tpad + q) * rstride + cl * L;
-        long long acc = 0;
-        for (uint32_t l = 0; l < L; ++l) acc += (long long)rr[l] * (1ll << (8 * l));
-        xr[term] = acc;
-      }
-      rb_epilogue(K, (int)c, j, xr);
-    }
-  }
-  __syncthreads();
+  if (tid == 0 && abort_flag) atomicExch(&K.ch[0].error, BMG_DERR_TIMEOUT);
   if (warp == 5) {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(256u));
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS));
   }
 }
 
@@ -304,6 +381,15 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
   return fn;
 }
 
+// dynamic shared memory of a plan: the stage ring, the int64 sums, alignment slack
+static size_t tc_smem_bytes(const TcParams& P)
+{
+  return (size_t)P.stages * P.stage_bytes + P.xr_bytes + 1024;
+}
+
+// static shared memory of the kernel (decode tables and barriers) is below 9 KB
+constexpr size_t TC_SMEM_LIMIT = 227 * 1024 - 9 * 1024;
+
 static bool tc_plan(const DevConst* K, TcParams* P)
 {
   uint32_t T = K->n_terms;
@@ -311,16 +397,30 @@ static bool tc_plan(const DevConst* K, TcParams* P)
   P->snps_per_tile = TC_BM / P->tpad;
   for (uint32_t u = 0; u < 4; ++u) P->term_of_row[u] = (u < T) ? K->term_of[u] : -1;
   const uint32_t L = K->limbs_n;
-  P->chains_tile = min(K->n_chains, 256u / L);
-  P->n_mma = ((P->chains_tile * L + 15) / 16) * 16;
-  if (P->n_mma > 256 || P->n_mma < 16) return false;
   if (K->n_pad % TC_BK != 0 || K->n >= 65536) return false;  // exact FP32 sums need n < 2^16
   P->k_chunks = K->n_pad / TC_BK;
-  P->b_bytes = P->n_mma * 128;
   P->a_bytes = TC_BM * 128;
   P->pk_bytes = P->snps_per_tile * 16;
-  P->stage_bytes = ((P->b_bytes + P->a_bytes + P->pk_bytes + 1023) / 1024) * 1024;
-  return true;
+  // widest chain tile whose accumulator fits one TMEM buffer and whose stages
+  // (at least two) and sums fit shared memory
+  for (uint32_t ct = std::min(K->n_chains, TC_ACC_COLS / L); ct >= 1; --ct) {
+    P->chains_tile = ct;
+    P->n_mma = ((ct * L + 15) / 16) * 16;
+    if (P->n_mma > TC_ACC_COLS || P->n_mma < 16) continue;
+    P->b_bytes = P->n_mma * 128;
+    P->stage_bytes = ((P->b_bytes + P->a_bytes + P->pk_bytes + 1023) / 1024) * 1024;
+    P->xr_bytes = TC_BM * ct * 8;
+    for (uint32_t st = TC_MAX_STAGES; st >= 2; --st) {
+      P->stages = st;
+      if (tc_smem_bytes(*P) <= TC_SMEM_LIMIT) {
+        P->m_tiles = (uint32_t)((K->p + P->snps_per_tile - 1) / P->snps_per_tile);
+        P->n_tiles = (K->n_chains + ct - 1) / ct;
+        P->tiles = P->m_tiles * P->n_tiles;
+        return true;
+      }
+    }
+  }
+  return false;
 }
 
 extern "C" int bmg_scan_tc_supported(const DevConst* K)
@@ -361,17 +461,21 @@ extern "C" int bmg_scan_tc_launch(const DevConst* K, cudaStream_t stream)
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
       return 4;
   }
-  size_t raw_bytes = (size_t)TC_BM * (P.n_mma + 1) * 4;
-  size_t smem = std::max((size_t)TC_STAGES * P.stage_bytes, raw_bytes) + 1024;
-  if (smem > 227 * 1024) return 5;
+  const size_t smem = tc_smem_bytes(P);
   static size_t configured = 0;
   if (configured < smem) {
     if (cudaFuncSetAttribute(bmg_scan_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
       return 6;
     configured = smem;
   }
-  dim3 grid((unsigned)((K->p + P.snps_per_tile - 1) / P.snps_per_tile),
-            (unsigned)((K->n_chains + P.chains_tile - 1) / P.chains_tile));
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  const unsigned grid = (unsigned)std::min<uint32_t>(P.tiles, (uint32_t)sms);
   bmg_scan_tc_kernel<<<grid, TC_THREADS, smem, stream>>>(*K, P, mb, mg);
   return cudaGetLastError() == cudaSuccess ? 0 : 7;
 }
