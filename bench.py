@@ -191,6 +191,7 @@ def run_gb300(args, wl):
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
     ms = ctx.timings()
+    launches = ctx.launch_count()
     n_scans = ctx.reset_timings()
     dev_s = ms[3] / 1000.0
     from bmagwa_gb300 import replicas
@@ -255,7 +256,7 @@ def run_gb300(args, wl):
                    "l2": "inputs larger than L2 (%.2f GB packed genotypes)" % (packed.nbytes / 1e9),
                    "scan_impl": "tcgen05" if args.scan == 0 else "simt"},
         "e2e": e2e,
-        "gpu_launches": int(args.steps * (1 + 2) + args.steps * (1 if args.scan == 1 else 0)),
+        "gpu_launches": launches,
         "phase_ms": {"move": ms[0], "scan": ms[1], "rebuild": ms[2], "total": ms[3],
                      "scans": n_scans, "wall_s": dt},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -67,6 +67,7 @@ def lib():
         L.bmg_precompute_noalloc.restype = C.c_int
         L.bmg_get_last_scan.argtypes = [vp, u32, vp, vp]
         L.bmg_get_data_stats.argtypes = [vp, vp]
+        L.bmg_get_launch_count.argtypes = [vp, C.POINTER(u64)]
         L.bmg_last_error.argtypes = [vp]
         L.bmg_last_error.restype = C.c_char_p
         L.bmg_status_string.argtypes = [C.c_int]
@@ -232,6 +233,12 @@ class Context:
         out = np.zeros(4)
         self._check(lib().bmg_get_timings(self.h, _ptr(out)))
         return out
+
+    def launch_count(self):
+        """Kernels launched since the last reset_timings()."""
+        n = C.c_uint64(0)
+        self._check(lib().bmg_get_launch_count(self.h, C.byref(n)))
+        return int(n.value)
 
     def reset_timings(self):
         n = C.c_uint64()

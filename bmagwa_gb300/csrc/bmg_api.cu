@@ -17,6 +17,7 @@
 #include <memory>
 #include <sstream>
 #include <string>
+#include <cstdlib>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -35,7 +36,8 @@ extern "C" __global__ void bmg_rbprep_kernel(DevConst K);
 extern "C" __global__ void bmg_move_kernel(DevConst K, int max_iters);
 extern "C" __global__ void bmg_scan_simt_kernel(DevConst K, const int64_t* resid_t);
 extern "C" __global__ void bmg_resid_transpose_kernel(DevConst K, int64_t* resid_t);
-extern "C" __global__ void bmg_rebuild_kernel(DevConst K, int force);
+extern "C" __global__ void bmg_rebuild_sums_kernel(DevConst K, int force);
+extern "C" __global__ void bmg_rebuild_write_kernel(DevConst K);
 extern "C" cudaError_t bmg_move_configure(size_t* smem_bytes);
 // tensor-core scan (scan_tc.cu)
 extern "C" int bmg_scan_tc_launch(const DevConst* K, cudaStream_t stream);
@@ -50,6 +52,16 @@ namespace {
     cudaError_t e_ = (x);                                                           \
     if (e_ != cudaSuccess)                                                          \
       throw bmg_error(BMG_ECUDA, std::string(#x) + ": " + cudaGetErrorString(e_));  \
+  } while (0)
+
+// after a kernel launch: the launch error, and with sync_check the kernel's
+// own execution error, named
+#define LAUNCHED(ctx, name)                                                                      \
+  do {                                                                                           \
+    cudaError_t e_ = cudaGetLastError();                                                         \
+    ++(ctx)->n_launches;                                                                         \
+    if (e_ == cudaSuccess && (ctx)->sync_check) e_ = cudaStreamSynchronize((ctx)->stream);       \
+    if (e_ != cudaSuccess) throw bmg_error(BMG_ECUDA, std::string(name) + ": " + cudaGetErrorString(e_)); \
   } while (0)
 
 struct ChainFiles {
@@ -82,6 +94,8 @@ struct bmg_ctx {
   double ms[4] = {0, 0, 0, 0};
   uint64_t n_scans = 0;
   size_t move_smem = 0;   // dynamic shared memory of a move CTA
+  bool sync_check = false; // BMG_SYNC_CHECK=1: synchronise after every launch
+  uint64_t n_launches = 0; // kernels of this library launched since the last counter reset
   cudaEvent_t ev[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   uint64_t n_iter = 0;
   time_t t_start = 0;
@@ -230,6 +244,8 @@ extern "C" bmg_status bmg_create(const bmg_options* opt, bmg_ctx** out)
     c->n_pad = (uint32_t)(((c->n + 127) / 128) * 128);
     c->gs = c->n_pad / 4;
     CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    const char* sc = std::getenv("BMG_SYNC_CHECK");
+    c->sync_check = sc && sc[0] && sc[0] != '0';
     c->ch_h.resize(c->C);
     *out = c.release();
     return BMG_OK;
@@ -284,7 +300,7 @@ extern "C" bmg_status bmg_load_bed(bmg_ctx* ctx, const uint8_t* packed, uint64_t
   unsigned blocks = (unsigned)std::min<uint64_t>((p + 7) / 8, 152 * 16);
   bmg_prep_kernel<<<blocks, 256, 0, ctx->stream>>>(g, n, p, ctx->gs, ctx->opt.recode_g_to_minor_allele_count,
                                                    cnt, miss);
-  CK(cudaGetLastError());
+  LAUNCHED(ctx, "bmg_prep_kernel");
   ctx->cnt_h.resize(2 * p);
   std::vector<int32_t> miss_h(p);
   CK(cudaMemcpyAsync(ctx->cnt_h.data(), cnt, 8 * p, cudaMemcpyDeviceToHost, ctx->stream));
@@ -366,6 +382,17 @@ extern "C" bmg_status bmg_set_covariates(bmg_ctx* ctx, const double* e, uint32_t
   ctx->have_e = true;
   return BMG_OK;
   API_END
+}
+
+// The dd_add prefix of the chains that asked for it (all with force).
+static void launch_rebuild(bmg_ctx* ctx, int force)
+{
+  const DevConst& K = ctx->K;
+  dim3 grid((unsigned)((K.p + BMG_REBUILD_TILE - 1) / BMG_REBUILD_TILE), ctx->C);
+  bmg_rebuild_sums_kernel<<<grid, 256, 0, ctx->stream>>>(K, force);
+  LAUNCHED(ctx, "bmg_rebuild_sums_kernel");
+  bmg_rebuild_write_kernel<<<grid, 256, 0, ctx->stream>>>(K);
+  LAUNCHED(ctx, "bmg_rebuild_write_kernel");
 }
 
 // ------------------------------------------------------------- precompute
@@ -488,7 +515,7 @@ extern "C" bmg_status bmg_precompute(bmg_ctx* ctx)
     int64_t* gsum = ctx->dalloc<int64_t>((size_t)K.p * nv * 2, false);
     const uint64_t blocks = std::min<uint64_t>((K.p + 7) / 8, 152 * 8);
     bmg_gsum_kernel<<<(unsigned)blocks, 256, 0, ctx->stream>>>(K.geno, n, K.p, K.gs, K.yint, dEi, nv, gsum);
-    CK(cudaGetLastError());
+    LAUNCHED(ctx, "bmg_gsum_kernel");
     K.gsum = gsum;
   }
   K.ee = dee;
@@ -646,6 +673,8 @@ extern "C" bmg_status bmg_precompute(bmg_ctx* ctx)
   const size_t words = (p + 31) / 32;
   K.inbits = ctx->dalloc<uint32_t>(words * C);
   K.basebits = ctx->dalloc<uint32_t>(words * C);
+  K.tile_sums = ctx->dalloc<int64_t>((size_t)C * ((p + BMG_REBUILD_TILE - 1) / BMG_REBUILD_TILE));
+  K.rebuild_active = ctx->dalloc<int32_t>(C);
   K.model_inds = ctx->dalloc<int32_t>(pc, false);
   CK(cudaMemsetAsync(K.model_inds, 0xff, 4 * pc, ctx->stream));
   K.n_pad = ctx->n_pad;
@@ -745,9 +774,8 @@ extern "C" bmg_status bmg_precompute(bmg_ctx* ctx)
   }
   CK(bmg_move_configure(&ctx->move_smem));
   bmg_init_kernel<<<C, 32, ctx->move_smem, ctx->stream>>>(K);
-  CK(cudaGetLastError());
-  bmg_rebuild_kernel<<<C, 1024, 0, ctx->stream>>>(K, 1);
-  CK(cudaGetLastError());
+  LAUNCHED(ctx, "bmg_init_kernel");
+  launch_rebuild(ctx, 1);
   CK(cudaStreamSynchronize(ctx->stream));
   device_error_check(ctx);
   ctx->ready = true;
@@ -773,13 +801,18 @@ static void launch_scan(bmg_ctx* ctx)
   DevConst& K = ctx->K;
   bool tc = ctx->opt.scan_impl == BMG_SCAN_TCGEN05 && bmg_scan_tc_supported(&K);
   if (tc) {
-    if (bmg_scan_tc_launch(&K, ctx->stream) != 0) throw bmg_error(BMG_ECUDA, "tensor-core scan launch failed");
+    int rc = bmg_scan_tc_launch(&K, ctx->stream);
+    if (rc != 0)
+      throw bmg_error(BMG_ECUDA, "tensor-core scan launch failed (step " + std::to_string(rc) +
+                                     "): " + cudaGetErrorString(cudaGetLastError()));
+    LAUNCHED(ctx, "bmg_scan_tc_kernel");
   } else {
     bmg_resid_transpose_kernel<<<1024, 256, 0, ctx->stream>>>(K, ctx->resid_t);
+    LAUNCHED(ctx, "bmg_resid_transpose_kernel");
     unsigned blocks = 152 * 8;
     bmg_scan_simt_kernel<<<blocks, 256, 0, ctx->stream>>>(K, ctx->resid_t);
+    LAUNCHED(ctx, "bmg_scan_simt_kernel");
   }
-  CK(cudaGetLastError());
 }
 
 static void open_files(bmg_ctx* ctx)
@@ -931,6 +964,7 @@ extern "C" bmg_status bmg_run(bmg_ctx* ctx, uint64_t n_iter, const bmg_trace_sin
     uint64_t chunk = std::min<uint64_t>(n_iter - done, gi);
     uint64_t iter0 = ctx->n_iter;
     bmg_trace_reset_kernel<<<(ctx->C + 127) / 128, 128, 0, ctx->stream>>>(K.ch, (int)ctx->C);
+    LAUNCHED(ctx, "bmg_trace_reset_kernel");
     uint64_t i = 0;
     while (i < chunk) {
       uint64_t t = ctx->n_iter;
@@ -938,7 +972,7 @@ extern "C" bmg_status bmg_run(bmg_ctx* ctx, uint64_t n_iter, const bmg_trace_sin
       uint64_t seg = std::min<uint64_t>(chunk - i, next_rb - t + 1);
       CK(cudaEventRecord(ctx->ev[0], ctx->stream));
       bmg_move_kernel<<<ctx->C, BMG_MOVE_THREADS, ctx->move_smem, ctx->stream>>>(K, (int)seg);
-      CK(cudaGetLastError());
+      LAUNCHED(ctx, "bmg_move_kernel");
       CK(cudaEventRecord(ctx->ev[1], ctx->stream));
       ctx->n_iter += seg;
       i += seg;
@@ -946,8 +980,7 @@ extern "C" bmg_status bmg_run(bmg_ctx* ctx, uint64_t n_iter, const bmg_trace_sin
       if (rb) {
         launch_scan(ctx);
         CK(cudaEventRecord(ctx->ev[2], ctx->stream));
-        bmg_rebuild_kernel<<<ctx->C, 1024, 0, ctx->stream>>>(K, 0);
-        CK(cudaGetLastError());
+        launch_rebuild(ctx, 0);
         CK(cudaEventRecord(ctx->ev[3], ctx->stream));
       }
       CK(cudaEventSynchronize(rb ? ctx->ev[3] : ctx->ev[1]));
@@ -984,7 +1017,7 @@ extern "C" bmg_status bmg_scan(bmg_ctx* ctx, double* p_r, double* p_r_types)
   check_ready(ctx);
   DevConst& K = ctx->K;
   bmg_rbprep_kernel<<<ctx->C, BMG_MOVE_THREADS, ctx->move_smem, ctx->stream>>>(K);
-  CK(cudaGetLastError());
+  LAUNCHED(ctx, "bmg_rbprep_kernel");
   launch_scan(ctx);
   const size_t pc = (size_t)ctx->p * ctx->C;
   if (p_r) CK(cudaMemcpyAsync(p_r, K.p_r, 8 * pc, cudaMemcpyDeviceToHost, ctx->stream));
@@ -1113,6 +1146,14 @@ extern "C" bmg_status bmg_reset_timings(bmg_ctx* ctx, uint64_t* n_scans)
   if (n_scans) *n_scans = ctx->n_scans;
   for (int i = 0; i < 4; ++i) ctx->ms[i] = 0;
   ctx->n_scans = 0;
+  ctx->n_launches = 0;
+  return BMG_OK;
+}
+
+extern "C" bmg_status bmg_get_launch_count(bmg_ctx* ctx, uint64_t* n_launches)
+{
+  if (!ctx || !n_launches) return BMG_EINVAL;
+  *n_launches = ctx->n_launches;
   return BMG_OK;
 }
 

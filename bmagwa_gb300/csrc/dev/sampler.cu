@@ -461,6 +461,7 @@ struct Warp {
         cR[q] = coefR(M->xc_type[idx]);
       }
       int hh[4] = {0, 0, 0, 0}, hr[4] = {0, 0, 0, 0}, rh[4] = {0, 0, 0, 0}, rr[4] = {0, 0, 0, 0};
+#pragma unroll 4
       for (unsigned w = lane; w < nw64; w += 32) {
         const uint64_t y = rb[w];
         const uint64_t yh = (y >> 1) & m5, yl = y & m5;
@@ -1500,69 +1501,93 @@ __device__ void bulk_phase(const DevConst& K, int c, MoveShared& s, BulkCols& bc
   // (src/sampler.cpp:735).  The same update is reproduced here.
   const bool stale = (nt == 0) && (me > 1);
   double* yhat = K.yhat + (size_t)c * K.n;
-  for (uint64_t i = tid; i < K.n_pad; i += nth) {
-    long long yg = 0;
-    double ye = 0;
-    bool live = i < K.n;
-    if (live) {
+  const int dsh = K.sy - sh;
+  // a thread takes 16 individuals at a time: one 32-bit word of every model
+  // column's packed codes, so each column costs one coalesced load per word
+  const uint32_t words = (uint32_t)(K.n_pad / 16);
+  for (uint32_t w = tid; w < words; w += nth) {
+    long long yg16[16];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) yg16[q] = 0;
+    if ((uint64_t)16 * w < K.n) {
       for (int j = 0; j < nt; ++j) {
-        const uint8_t* row = K.geno + (size_t)bc.snp[j] * K.gs;
-        int code = (row[i >> 2] >> ((i & 3) * 2)) & 3;
-        int v = term_value(code, bc.term[j]);
-        if (v == 1) yg += bc.coef[j];
-        else if (v == 2) yg += 2 * bc.coef[j];
-      }
-      if (me > 1) {
-        for (int e = 0; e < me; ++e) ye += K.e[(size_t)e * K.n + i] * s.bulk_e[e];
-      } else {
-        ye = s.bulk_b0;
+        const uint32_t code = reinterpret_cast<const uint32_t*>(K.geno + (size_t)bc.snp[j] * K.gs)[w];
+        const int t = bc.term[j];
+        const long long vh = coefH(t) * bc.coef[j], vr = coefR(t) * bc.coef[j];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+          const uint32_t c2 = (code >> (2 * q)) & 3u;  // 2 = het, 3 = hom-alt
+          yg16[q] += (c2 == 2u) ? vh : ((c2 == 3u) ? vr : 0ll);
+        }
       }
     }
-    double ygd = (double)yg * sc;
-    double yh = 0;
-    if (live && (mode & BULK_PVE)) {
-      yh = stale ? yhat[i] + ye : ygd + ye;
-      yhat[i] = yh;
-      ymax = fmax(ymax, fabs(yh));
-    }
-    if (live && (mode & (BULK_PVE | BULK_ALPHA))) {
-      s1g += ygd;
-      s2g += ygd * ygd;
-      if (mode & BULK_ALPHA) {
-        // eb = E beta_E - y, xb = fitted genotype part
-        s1e += (ye - K.y[i]) * ygd;
-      } else {
-        s1e += ye;
-        s2e += ye * ye;
-        double yt = ygd + ye;
-        s1t += yt;
-        s2t += yt * yt;
-      }
-    }
-    if (mode & BULK_RESID) {
-      long long R = 0;
+    long long R16[16];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      const uint64_t i = (uint64_t)16 * w + q;
+      const bool live = i < K.n;
+      const long long yg = yg16[q];
+      double ye = 0;
       if (live) {
-        long long Y = K.yint[i];
-        int d = K.sy - sh;
-        long long Ys = (d > 0) ? ((Y + (1ll << (d - 1))) >> d) : (Y << (-d));
+        if (me > 1) {
+          for (int e = 0; e < me; ++e) ye += K.e[(size_t)e * K.n + i] * s.bulk_e[e];
+        } else {
+          ye = s.bulk_b0;
+        }
+      }
+      const double ygd = (double)yg * sc;
+      double yh = 0;
+      if (live && (mode & BULK_PVE)) {
+        yh = stale ? yhat[i] + ye : ygd + ye;
+        yhat[i] = yh;
+        ymax = fmax(ymax, fabs(yh));
+      }
+      if (live && (mode & (BULK_PVE | BULK_ALPHA))) {
+        s1g += ygd;
+        s2g += ygd * ygd;
+        if (mode & BULK_ALPHA) {
+          // eb = E beta_E - y, xb = fitted genotype part
+          s1e += (ye - K.y[i]) * ygd;
+        } else {
+          s1e += ye;
+          s2e += ye * ye;
+          const double yt = ygd + ye;
+          s1t += yt;
+          s2t += yt * yt;
+        }
+      }
+      long long R = 0;
+      if (live && (mode & BULK_RESID)) {
+        const long long Y = K.yint[i];
+        const long long Ys = (dsh > 0) ? ((Y + (1ll << (dsh - 1))) >> dsh) : (Y << (-dsh));
         if (stale) {
-          double yv = (mode & BULK_PVE) ? yh : yhat[i];
+          const double yv = (mode & BULK_PVE) ? yh : yhat[i];
           R = Ys - __double2ll_rn(yv * ldexp(1.0, sh));
         } else {
-          long long E = (me > 1) ? __double2ll_rn(ye * ldexp(1.0, sh)) : s.bulk_b0i;
+          const long long E = (me > 1) ? __double2ll_rn(ye * ldexp(1.0, sh)) : s.bulk_b0i;
           R = Ys - E - yg;
         }
         K.resid[(size_t)c * K.n_pad + i] = R;
       }
+      R16[q] = R;
       rsum += R;
-      // balanced base-256 limbs, exact as bf16
-      long long rr = R;
+    }
+    if (mode & BULK_RESID) {
+      // balanced base-256 digits of the 16 residuals, exact as bf16, stored
+      // as two 16-byte vectors per digit
       for (uint32_t l = 0; l < L; ++l) {
-        int d8 = (int)(signed char)(rr & 0xff);
-        rr = (rr - d8) >> 8;
-        float f = (float)d8;
-        uint32_t bits = __float_as_uint(f);
-        K.limbs[((size_t)c * L + l) * K.n_pad + i] = (uint16_t)(bits >> 16);
+        uint32_t pk[8];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+          const int d8 = (int)(signed char)(R16[q] & 0xff);
+          R16[q] = (R16[q] - d8) >> 8;
+          const uint32_t bits = __float_as_uint((float)d8) >> 16;
+          if (q & 1) pk[q >> 1] |= bits << 16;
+          else pk[q >> 1] = bits;
+        }
+        uint4* dst = reinterpret_cast<uint4*>(K.limbs + ((size_t)c * L + l) * K.n_pad + (size_t)16 * w);
+        dst[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+        dst[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
       }
     }
   }
@@ -1725,6 +1750,9 @@ __device__ void prep_rb(Warp& W, bool scan_only)
       if (!K.flat_proposal_dist) ch->rebuild = 1;
     }
   }
+  // many pending flips make every proposal draw slower: ask the rebuild
+  // that follows the scan for a fresh prefix
+  if (W.lane == 0 && W.s.n_pend > BMG_PEND_REBUILD) ch->rebuild = 1;
   if (W.lane == 0) ch->rb_pending = do_scan || adapt;
   __syncwarp();
 }

@@ -53,12 +53,99 @@ extern "C" __global__ void bmg_resid_transpose_kernel(DevConst K, int64_t* resid
   }
 }
 
-// Rebuild the dd_add prefix of every chain whose proposal weights changed.
-extern "C" __global__ void __launch_bounds__(1024)
-bmg_rebuild_kernel(DevConst K, int force)
+// Rebuild the dd_add prefix of every chain whose proposal weights changed
+// (or of all chains with force), in two passes over tiles of
+// BMG_REBUILD_TILE in-order positions: tile sums, then each tile's exclusive
+// prefix written with its offset.  The weights and their order are those of
+// rebuild_chain (common.cuh).
+extern "C" __global__ void __launch_bounds__(256)
+bmg_rebuild_sums_kernel(DevConst K, int force)
 {
-  __shared__ long long part[1024];
-  const int c = blockIdx.x;
-  if (!force && !K.ch[c].rebuild) return;
-  rebuild_chain(K, c, part, K.ch + c);
+  __shared__ long long red[8];
+  const uint32_t t = blockIdx.x, c = blockIdx.y;
+  const bool active = force || K.ch[c].rebuild;
+  if (t == 0 && threadIdx.x == 0) K.rebuild_active[c] = active;
+  if (!active) return;
+  const uint64_t p = K.p, q0 = (uint64_t)t * BMG_REBUILD_TILE;
+  const uint64_t q1 = min(p, q0 + BMG_REBUILD_TILE);
+  const double* pp = K.p_prop + (size_t)c * p;
+  const uint32_t* ib = K.inbits + (size_t)c * ((p + 31) / 32);
+  const double sc = ldexp(1.0, K.qs);
+  long long sum = 0;
+  for (uint64_t q = q0 + threadIdx.x; q < q1; q += blockDim.x) {
+    const uint32_t snp = (uint32_t)K.inv[q];
+    if (!((ib[snp >> 5] >> (snp & 31)) & 1u)) sum += __double2ll_rn(fmax(pp[q], K.q_add_min) * sc);
+  }
+  sum = warp_sum_ll(sum);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = sum;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    long long tot = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += red[w];
+    K.tile_sums[(size_t)c * gridDim.x + t] = tot;
+  }
+}
+
+extern "C" __global__ void __launch_bounds__(256)
+bmg_rebuild_write_kernel(DevConst K)
+{
+  constexpr int PER = BMG_REBUILD_TILE / 256;  // consecutive positions per thread
+  __shared__ long long part[256];
+  __shared__ long long base_sh;
+  const uint32_t t = blockIdx.x, c = blockIdx.y, tiles = gridDim.x;
+  if (!K.rebuild_active[c]) return;
+  const int tid = threadIdx.x;
+  const uint64_t p = K.p;
+  // offset of this tile: the sum of the earlier tiles' sums
+  if (tid < 32) {
+    long long o = 0;
+    for (uint32_t u = tid; u < t; u += 32) o += K.tile_sums[(size_t)c * tiles + u];
+    o = warp_sum_ll(o);
+    if (tid == 0) base_sh = o;
+  }
+  const double* pp = K.p_prop + (size_t)c * p;
+  const uint32_t* ib = K.inbits + (size_t)c * ((p + 31) / 32);
+  const double sc = ldexp(1.0, K.qs);
+  const uint64_t q0 = (uint64_t)t * BMG_REBUILD_TILE + (uint64_t)tid * PER;
+  long long w[PER];
+  long long mine = 0;
+#pragma unroll
+  for (int r = 0; r < PER; ++r) {
+    const uint64_t q = q0 + r;
+    long long v = 0;
+    if (q < p) {
+      const uint32_t snp = (uint32_t)K.inv[q];
+      if (!((ib[snp >> 5] >> (snp & 31)) & 1u)) v = __double2ll_rn(fmax(pp[q], K.q_add_min) * sc);
+    }
+    w[r] = v;
+    mine += v;
+  }
+  part[tid] = mine;
+  __syncthreads();
+  for (int o = 1; o < 256; o <<= 1) {
+    long long v = (tid >= o) ? part[tid - o] : 0;
+    __syncthreads();
+    part[tid] += v;
+    __syncthreads();
+  }
+  long long run = base_sh + part[tid] - mine;
+  int64_t* cadd = K.cadd + (size_t)c * (p + 1);
+#pragma unroll
+  for (int r = 0; r < PER; ++r) {
+    const uint64_t q = q0 + r;
+    if (q < p) cadd[q] = run;
+    run += w[r];
+  }
+  // the zero state of the new base: this tile's share of the bitmap words
+  const uint64_t nwords = (p + 31) / 32;
+  uint32_t* bb = K.basebits + (size_t)c * nwords;
+  for (uint64_t wd = (uint64_t)t * (BMG_REBUILD_TILE / 32) + tid; wd < min(nwords, (uint64_t)(t + 1) * (BMG_REBUILD_TILE / 32));
+       wd += blockDim.x)
+    bb[wd] = ib[wd];
+  if (t == tiles - 1 && tid == 255) {
+    cadd[p] = run;
+    K.ch[c].cadd_total = run;
+    K.ch[c].n_pend = 0;
+    K.ch[c].rebuild = 0;
+  }
 }

@@ -22,6 +22,8 @@
 
 #define BMG_MOVE_THREADS 256
 #define BMG_PEND_MAX 64          /* pending zero/unzero flips of dd_add */
+#define BMG_PEND_REBUILD 8       /* more pending flips at an RB step: rebuild the prefix */
+#define BMG_REBUILD_TILE 4096    /* in-order positions per CTA of the prefix rebuild */
 #define BMG_MAX_MS 255
 #define BMG_REMSET_MAX 1280      /* in-model SNPs + moved SNPs for dd_rem */
 
@@ -234,6 +236,8 @@ struct DevConst {
   int64_t* cadd;        // chains x (p + 1) prefix of dd_add weights (x 2^qs) in in-order
   uint32_t* inbits;     // chains x ceil(p/32): SNP in current model
   uint32_t* basebits;   // chains x ceil(p/32): zeroed in the cadd base
+  int64_t* tile_sums;   // chains x ceil(p / BMG_REBUILD_TILE): rebuild pass 1
+  int32_t* rebuild_active;  // chains: this rebuild covers the chain
   int32_t* model_inds;  // chains x p: current model's index or -1
   int64_t* resid;       // chains x n_pad: fixed-point residual of the last RB step
   double* yhat;         // chains x n: Model::y_hat as compute_pve leaves it

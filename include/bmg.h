@@ -253,6 +253,10 @@ bmg_status bmg_get_data_stats(bmg_ctx* ctx, double* out4);
  * last reset. */
 bmg_status bmg_reset_timings(bmg_ctx* ctx, uint64_t* n_scans);
 
+/* Kernels of this library launched by ctx since the last bmg_reset_timings
+ * (no counterpart in the reference; a measurement aid). */
+bmg_status bmg_get_launch_count(bmg_ctx* ctx, uint64_t* n_launches);
+
 /* Per-SNP precomputed sums, allocating nothing (no counterpart in the
  * reference).  For callers that cannot call cudaMalloc, e.g. code running in
  * another framework's memory pool or while a stream is being captured.
