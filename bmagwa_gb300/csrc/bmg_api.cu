@@ -230,6 +230,11 @@ extern "C" bmg_status bmg_create(const bmg_options* opt, bmg_ctx** out)
     if (opt->thin == 0 || opt->n_rao == 0 || opt->n_sample_tau2_and_missing == 0)
       throw bmg_error(BMG_EINVAL, "thin, n_rao and n_sample_tau2_and_missing must be positive");
     if (opt->n_rao % opt->thin != 0) throw bmg_error(BMG_EINVAL, "Config error: n_rao should be a multiple of thin");
+    // the state-change move permutes 2 x neighbourhood positions in a
+    // fixed-size on-chip list
+    if (2ull * opt->max_SNP_neighborhood_size > BMG_MAX_MS + 1)
+      throw bmg_error(BMG_EINVAL, "max_SNP_neighborhood_size above " + std::to_string((BMG_MAX_MS + 1) / 2) +
+                                      " is not supported");
     c->n = opt->n;
     c->p = opt->m_g;
     c->C = opt->n_chains;

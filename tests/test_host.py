@@ -195,3 +195,20 @@ def test_alternate_phenotype_and_covariates(tmp_path):
     open(prefix + ".y", "w").write("\n".join(lines[1:]) + "\n")
     with pytest.raises(bg.BmgError, match="Alternate phenotype file does not contain all phenotypes"):
         bg.read_plink(o)
+
+
+def test_create_rejects_unsupported_options_before_touching_the_device(tmp_path):
+    """Option checks of bmg_create run before any CUDA call, so they hold on
+    a host without a GPU too."""
+    o = bg.options_from_ini(_ini(tmp_path))
+    h = C.c_void_p()
+    L = bg.lib()
+    for field, value, status in [("max_SNP_neighborhood_size", 129, "BMG_EINVAL"),
+                                 ("delay_rejection", 10, "BMG_EUNSUPPORTED"),
+                                 ("sampler_type", 1, "BMG_EUNSUPPORTED")]:
+        old = getattr(o, field)
+        setattr(o, field, value)
+        rc = L.bmg_create(C.byref(o), C.byref(h))
+        L.bmg_status_string.restype = C.c_char_p
+        assert L.bmg_status_string(rc).decode() == status, field
+        setattr(o, field, old)
