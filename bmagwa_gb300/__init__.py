@@ -68,6 +68,7 @@ def lib():
         L.bmg_get_last_scan.argtypes = [vp, u32, vp, vp]
         L.bmg_get_data_stats.argtypes = [vp, vp]
         L.bmg_get_launch_count.argtypes = [vp, C.POINTER(u64)]
+        L.bmg_get_scan_shape.argtypes = [vp, C.POINTER(C.c_int32), C.c_char_p, C.c_size_t]
         L.bmg_last_error.argtypes = [vp]
         L.bmg_last_error.restype = C.c_char_p
         L.bmg_status_string.argtypes = [C.c_int]
@@ -239,6 +240,13 @@ class Context:
         n = C.c_uint64(0)
         self._check(lib().bmg_get_launch_count(self.h, C.byref(n)))
         return int(n.value)
+
+    def scan_shape(self):
+        """(variant, description) of the tensor-core scan's launch shape."""
+        v = C.c_int32(-1)
+        buf = C.create_string_buffer(128)
+        self._check(lib().bmg_get_scan_shape(self.h, C.byref(v), buf, 128))
+        return int(v.value), buf.value.decode()
 
     def reset_timings(self):
         n = C.c_uint64()

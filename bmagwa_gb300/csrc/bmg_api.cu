@@ -40,7 +40,9 @@ extern "C" __global__ void bmg_rebuild_sums_kernel(DevConst K, int force);
 extern "C" __global__ void bmg_rebuild_write_kernel(DevConst K);
 extern "C" cudaError_t bmg_move_configure(size_t* smem_bytes);
 // tensor-core scan (scan_tc.cu)
-extern "C" int bmg_scan_tc_launch(const DevConst* K, cudaStream_t stream);
+extern "C" int bmg_scan_tc_launch(const DevConst* K, cudaStream_t stream, int variant);
+extern "C" int bmg_scan_tc_variants();
+extern "C" void bmg_scan_tc_variant_name(int v, char* buf, size_t len);
 extern "C" int bmg_scan_tc_supported(const DevConst* K);
 
 using bmg_host::bmg_error;
@@ -96,6 +98,14 @@ struct bmg_ctx {
   size_t move_smem = 0;   // dynamic shared memory of a move CTA
   bool sync_check = false; // BMG_SYNC_CHECK=1: synchronise after every launch
   uint64_t n_launches = 0; // kernels of this library launched since the last counter reset
+  // launch-shape autotuner of the tensor-core scan: the first scan warms
+  // up, the next ones time one shape each, then the fastest is kept
+  int tc_forced = -1;      // BMG_SCAN_VARIANT
+  int tc_variant = -1;     // chosen shape (-1 while tuning)
+  int tc_tuned = 0;        // tuning scans issued
+  int tc_pending = -1;     // shape whose timing events are not read yet
+  cudaEvent_t tc_ev[2] = {nullptr, nullptr};
+  std::vector<float> tc_ms;
   cudaEvent_t ev[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   uint64_t n_iter = 0;
   time_t t_start = 0;
@@ -120,6 +130,8 @@ struct bmg_ctx {
   ~bmg_ctx()
   {
     for (cudaEvent_t e : ev)
+      if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : tc_ev)
       if (e) cudaEventDestroy(e);
     for (void* a : allocs) cudaFree(a);
     if (stream) cudaStreamDestroy(stream);
@@ -251,6 +263,8 @@ extern "C" bmg_status bmg_create(const bmg_options* opt, bmg_ctx** out)
     CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     const char* sc = std::getenv("BMG_SYNC_CHECK");
     c->sync_check = sc && sc[0] && sc[0] != '0';
+    const char* sv = std::getenv("BMG_SCAN_VARIANT");
+    if (sv && sv[0]) c->tc_forced = std::max(0, std::min(bmg_scan_tc_variants() - 1, std::atoi(sv)));
     c->ch_h.resize(c->C);
     *out = c.release();
     return BMG_OK;
@@ -806,7 +820,34 @@ static void launch_scan(bmg_ctx* ctx)
   DevConst& K = ctx->K;
   bool tc = ctx->opt.scan_impl == BMG_SCAN_TCGEN05 && bmg_scan_tc_supported(&K);
   if (tc) {
-    int rc = bmg_scan_tc_launch(&K, ctx->stream);
+    int v = ctx->tc_forced >= 0 ? ctx->tc_forced : ctx->tc_variant;
+    const int nv = bmg_scan_tc_variants();
+    if (v < 0) {
+      // read the previous tuning scan, then time the next shape
+      if (ctx->tc_pending >= 0) {
+        float ms = 0;
+        CK(cudaEventSynchronize(ctx->tc_ev[1]));
+        CK(cudaEventElapsedTime(&ms, ctx->tc_ev[0], ctx->tc_ev[1]));
+        if (ctx->tc_tuned > 1) ctx->tc_ms[ctx->tc_pending] = ms;  // the first scan only warms up
+        ctx->tc_pending = -1;
+      }
+      if (ctx->tc_ms.empty()) ctx->tc_ms.assign(nv, -1.0f);
+      if (ctx->tc_tuned > nv) {
+        int best = 0;
+        for (int i = 1; i < nv; ++i)
+          if (ctx->tc_ms[i] >= 0 && (ctx->tc_ms[best] < 0 || ctx->tc_ms[i] < ctx->tc_ms[best])) best = i;
+        ctx->tc_variant = v = best;
+      } else {
+        v = ctx->tc_tuned == 0 ? 0 : ctx->tc_tuned - 1;
+        ctx->tc_pending = v;
+        ++ctx->tc_tuned;
+        for (int q = 0; q < 2; ++q)
+          if (!ctx->tc_ev[q]) CK(cudaEventCreate(&ctx->tc_ev[q]));
+        CK(cudaEventRecord(ctx->tc_ev[0], ctx->stream));
+      }
+    }
+    int rc = bmg_scan_tc_launch(&K, ctx->stream, v);
+    if (ctx->tc_pending >= 0 && rc == 0) CK(cudaEventRecord(ctx->tc_ev[1], ctx->stream));
     if (rc != 0)
       throw bmg_error(BMG_ECUDA, "tensor-core scan launch failed (step " + std::to_string(rc) +
                                      "): " + cudaGetErrorString(cudaGetLastError()));
@@ -1152,6 +1193,18 @@ extern "C" bmg_status bmg_reset_timings(bmg_ctx* ctx, uint64_t* n_scans)
   for (int i = 0; i < 4; ++i) ctx->ms[i] = 0;
   ctx->n_scans = 0;
   ctx->n_launches = 0;
+  return BMG_OK;
+}
+
+extern "C" bmg_status bmg_get_scan_shape(bmg_ctx* ctx, int32_t* variant, char* name, size_t name_len)
+{
+  if (!ctx) return BMG_EINVAL;
+  const int v = ctx->tc_forced >= 0 ? ctx->tc_forced : ctx->tc_variant;
+  if (variant) *variant = v;
+  if (name && name_len) {
+    if (v >= 0) bmg_scan_tc_variant_name(v, name, name_len);
+    else snprintf(name, name_len, "tuning");
+  }
   return BMG_OK;
 }
 

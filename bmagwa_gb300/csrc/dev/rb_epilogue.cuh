@@ -13,6 +13,46 @@ static __device__ __forceinline__ bool in_model(const DevConst& K, int c, uint64
   return (K.inbits[(size_t)c * ((K.p + 31) / 32) + (j >> 5)] >> (j & 31)) & 1u;
 }
 
+// The common case: one non-AH effect type and the chain's shared tau2.  For
+// a SNP outside the model the posterior needs no branch, so a thread can
+// evaluate two (SNP, chain) units back to back and their FP64 chains overlap.
+// The expressions are those of rb_epilogue below, term by term.
+static __device__ __forceinline__ bool rb_fast_ok(const DevConst& K)
+{
+  return !K.use_individual_tau2 && K.n_types == 1 && K.types[0] != 4;
+}
+
+// p_r of (SNP j, chain c) from the exact product xi = x_t(j)' R_c
+static __device__ __forceinline__ double rb_fast_pr(const DevConst& K, int c, uint64_t j, long long xi)
+{
+  const RbParams& rp = K.rb[c];
+  const int type = K.types[0];
+  const double* pre = K.pre + j * (size_t)K.offset;
+  const int off = K.offset_type[type];
+  const double xr = (double)xi * rp.scale;
+  const double det = pre[off + 1] + rp.itv[type];
+  const double slq = rp.nlog_itv[type];
+  const double rx = xr - pre[off] * rp.mr;
+  const double et = (rx * rx) / det;
+  const double p = et * rp.inv_2s2 - 0.5 * (log(det) + slq) + rp.lmp_add[type];
+  const double e = exp(p);
+  return isfinite(e) ? e / (1 + e) : 1;
+}
+
+// p_r and the running means of one (SNP, chain) with one effect type
+// (src/sampler.cpp:739-776)
+static __device__ __forceinline__ void rb_store1(const DevConst& K, int c, uint64_t j, double pr)
+{
+  const RbParams& rp = K.rb[c];
+  const size_t cj = (size_t)c * K.p + j;
+  if (K.p_r) K.p_r[cj] = pr;
+  if (rp.acc_rao) K.p_rao[cj] = rp.rao_z2 * K.p_rao[cj] + pr / rp.rao_z1;
+  if (rp.adapt) {
+    const size_t q = (size_t)c * K.p + K.pos[j];
+    K.p_prop[q] = rp.prop_z2 * K.p_prop[q] + pr / rp.prop_z1;
+  }
+}
+
 // xr[t] = x_t(j)' R_c for term type t (A,H,D,R), exact, residual scale 2^-s.
 // Writes p_r and updates the running means (src/sampler.cpp:739-776).
 static __device__ __noinline__ void rb_epilogue(const DevConst& K, int c, uint64_t j, const long long* xr_by_type)

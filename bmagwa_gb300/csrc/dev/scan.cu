@@ -38,7 +38,10 @@ bmg_scan_simt_kernel(DevConst K, const int64_t* resid_t)
         if (g == 2) acc[3] += R;         // R
       }
     }
-    if (need) rb_epilogue(K, c, j, acc);
+    if (need) {
+      if (rb_fast_ok(K) && !in_model(K, c, j)) rb_store1(K, c, j, rb_fast_pr(K, c, j, acc[K.types[0]]));
+      else rb_epilogue(K, c, j, acc);
+    }
   }
 }
 

@@ -22,13 +22,18 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <cstdio>
 
 #include "rb_epilogue.cuh"
 
 namespace {
 
-constexpr int TC_EPI_WARPS = 12;    // epilogue warps (three per TMEM lane quarter)
-constexpr int TC_THREADS = 192 + 32 * TC_EPI_WARPS;
+// epilogue warps: a multiple of 4 (each TMEM lane quarter gets the same
+// number); the kernel is instantiated for 8 and 12 and the host picks
+template <int EPI>
+struct TcShape {
+  static constexpr int threads = 192 + 32 * EPI;
+};
 constexpr int TC_MAX_STAGES = 4;
 constexpr int TC_BM = 128;          // rows of D per tile
 constexpr int TC_BK = 64;           // individuals per stage (128 bytes of bf16)
@@ -150,10 +155,12 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v)
 
 }  // namespace
 
-extern "C" __global__ void __launch_bounds__(TC_THREADS, 1)
+template <int TC_EPI_WARPS>
+__global__ void __launch_bounds__(TcShape<TC_EPI_WARPS>::threads, 1)
 bmg_scan_tc_kernel(DevConst K, TcParams P, const __grid_constant__ CUtensorMap map_b,
                    const __grid_constant__ CUtensorMap map_g)
 {
+  constexpr int TC_THREADS = TcShape<TC_EPI_WARPS>::threads;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   // 1024-byte aligned base for the swizzled tiles; the int64 sums follow the stages
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -339,19 +346,50 @@ bmg_scan_tc_kernel(DevConst K, TcParams P, const __grid_constant__ CUtensorMap m
       if (lane == 0) mbar_arrive(&acc_empty[b]);
       named_bar_sync(1, ethreads);
       // one unit per (SNP, chain), SNPs fastest so that a warp's stores to
-      // the chain-major running means are contiguous
+      // the chain-major running means are contiguous; two units per step
       const uint32_t units = P.snps_per_tile * chains_here;
-      for (uint32_t uu = e * 32 + lane; uu < units; uu += ethreads) {
-        const uint32_t sl = uu % P.snps_per_tile, cl = uu / P.snps_per_tile;
-        const uint64_t j = (uint64_t)snp0 + sl;
-        const uint32_t c = chain0 + cl;
-        if (j >= K.p || !K.rb[c].do_scan) continue;
-        long long xr[4] = {0, 0, 0, 0};
-        for (uint32_t q = 0; q < P.tpad; ++q) {
-          const int term = P.term_of_row[q];
-          if (term >= 0) xr[term] = xr_s[(sl * P.tpad + q) * ct + cl];
+      const bool fast = rb_fast_ok(K);
+      for (uint32_t ua = e * 32 + lane; ua < units; ua += 2 * ethreads) {
+        uint64_t j[2];
+        uint32_t c[2], sl[2], cl[2];
+        bool live[2];
+        for (int h = 0; h < 2; ++h) {
+          const uint32_t uu = ua + h * ethreads;
+          const bool in_tile = uu < units;
+          sl[h] = in_tile ? uu % P.snps_per_tile : 0;
+          cl[h] = in_tile ? uu / P.snps_per_tile : 0;
+          j[h] = (uint64_t)snp0 + sl[h];
+          c[h] = chain0 + cl[h];
+          live[h] = in_tile && j[h] < K.p && K.rb[c[h]].do_scan;
+          if (j[h] >= K.p) j[h] = snp0;  // a valid address for the unused half
         }
-        rb_epilogue(K, (int)c, j, xr);
+        if (fast) {
+          const long long xa = xr_s[sl[0] * ct + cl[0]], xb = xr_s[sl[1] * ct + cl[1]];
+          const double pa = rb_fast_pr(K, (int)c[0], j[0], xa);
+          const double pb = rb_fast_pr(K, (int)c[1], j[1], xb);
+          const double pr[2] = {pa, pb};
+          const long long xi[2] = {xa, xb};
+          for (int h = 0; h < 2; ++h) {
+            if (!live[h]) continue;
+            if (!in_model(K, (int)c[h], j[h])) {
+              rb_store1(K, (int)c[h], j[h], pr[h]);
+            } else {
+              long long xr[4] = {0, 0, 0, 0};
+              xr[K.types[0]] = xi[h];
+              rb_epilogue(K, (int)c[h], j[h], xr);
+            }
+          }
+        } else {
+          for (int h = 0; h < 2; ++h) {
+            if (!live[h]) continue;
+            long long xr[4] = {0, 0, 0, 0};
+            for (uint32_t q = 0; q < P.tpad; ++q) {
+              const int term = P.term_of_row[q];
+              if (term >= 0) xr[term] = xr_s[(sl[h] * P.tpad + q) * ct + cl[h]];
+            }
+            rb_epilogue(K, (int)c[h], j[h], xr);
+          }
+        }
       }
       named_bar_sync(1, ethreads);
     }
@@ -390,7 +428,7 @@ static size_t tc_smem_bytes(const TcParams& P)
 // static shared memory of the kernel (decode tables and barriers) is below 9 KB
 constexpr size_t TC_SMEM_LIMIT = 227 * 1024 - 9 * 1024;
 
-static bool tc_plan(const DevConst* K, TcParams* P)
+static bool tc_plan(const DevConst* K, TcParams* P, uint32_t ct_cap)
 {
   uint32_t T = K->n_terms;
   P->tpad = T <= 1 ? 1 : (T <= 2 ? 2 : 4);
@@ -403,7 +441,7 @@ static bool tc_plan(const DevConst* K, TcParams* P)
   P->pk_bytes = P->snps_per_tile * 16;
   // widest chain tile whose accumulator fits one TMEM buffer and whose stages
   // (at least two) and sums fit shared memory
-  for (uint32_t ct = std::min(K->n_chains, TC_ACC_COLS / L); ct >= 1; --ct) {
+  for (uint32_t ct = std::min(std::min(K->n_chains, TC_ACC_COLS / L), std::max(1u, ct_cap)); ct >= 1; --ct) {
     P->chains_tile = ct;
     P->n_mma = ((ct * L + 15) / 16) * 16;
     if (P->n_mma > TC_ACC_COLS || P->n_mma < 16) continue;
@@ -423,10 +461,34 @@ static bool tc_plan(const DevConst* K, TcParams* P)
   return false;
 }
 
+// Launch shapes the autotuner chooses between: epilogue warps and a cap on
+// the chains of one N tile (0: as many as one accumulator holds).  All of
+// them compute the same exact sums and the same posterior, bit for bit.
+struct TcVariant {
+  int epi;
+  int ct_div;  // chains per tile = ceil(chains / ct_div)
+};
+static const TcVariant kTcVariants[] = {{12, 1}, {8, 1}, {12, 2}, {8, 2}};
+constexpr int kTcVariantCount = sizeof(kTcVariants) / sizeof(kTcVariants[0]);
+
+extern "C" int bmg_scan_tc_variants() { return kTcVariantCount; }
+
+extern "C" void bmg_scan_tc_variant_name(int v, char* buf, size_t len)
+{
+  if (v < 0 || v >= kTcVariantCount) v = 0;
+  snprintf(buf, len, "epilogue_warps=%d chains_per_tile=1/%d", kTcVariants[v].epi, kTcVariants[v].ct_div);
+}
+
+static uint32_t tc_cap(const DevConst* K, int v)
+{
+  const int d = kTcVariants[v].ct_div;
+  return (K->n_chains + d - 1) / d;
+}
+
 extern "C" int bmg_scan_tc_supported(const DevConst* K)
 {
   TcParams P;
-  if (!tc_plan(K, &P) || !encode_fn()) return 0;
+  if (!tc_plan(K, &P, K->n_chains) || !encode_fn()) return 0;
   int dev = 0, major = 0, minor = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
@@ -434,10 +496,35 @@ extern "C" int bmg_scan_tc_supported(const DevConst* K)
   return (major == 10 && minor == 3) ? 1 : 0;
 }
 
-extern "C" int bmg_scan_tc_launch(const DevConst* K, cudaStream_t stream)
+template <int EPI>
+static int tc_launch_shape(const DevConst* K, const TcParams& P, const CUtensorMap& mb, const CUtensorMap& mg,
+                           cudaStream_t stream)
 {
+  const size_t smem = tc_smem_bytes(P);
+  static size_t configured = 0;
+  if (configured < smem) {
+    if (cudaFuncSetAttribute(bmg_scan_tc_kernel<EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
+      return 6;
+    configured = smem;
+  }
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  const unsigned grid = (unsigned)std::min<uint32_t>(P.tiles, (uint32_t)sms);
+  bmg_scan_tc_kernel<EPI><<<grid, TcShape<EPI>::threads, smem, stream>>>(*K, P, mb, mg);
+  return cudaGetLastError() == cudaSuccess ? 0 : 7;
+}
+
+extern "C" int bmg_scan_tc_launch(const DevConst* K, cudaStream_t stream, int variant)
+{
+  if (variant < 0 || variant >= kTcVariantCount) variant = 0;
   TcParams P;
-  if (!tc_plan(K, &P)) return 1;
+  if (!tc_plan(K, &P, tc_cap(K, variant))) return 1;
   auto enc = encode_fn();
   if (!enc) return 2;
   CUtensorMap mb, mg;
@@ -461,21 +548,6 @@ extern "C" int bmg_scan_tc_launch(const DevConst* K, cudaStream_t stream)
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
       return 4;
   }
-  const size_t smem = tc_smem_bytes(P);
-  static size_t configured = 0;
-  if (configured < smem) {
-    if (cudaFuncSetAttribute(bmg_scan_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-      return 6;
-    configured = smem;
-  }
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 1;
-  }
-  const unsigned grid = (unsigned)std::min<uint32_t>(P.tiles, (uint32_t)sms);
-  bmg_scan_tc_kernel<<<grid, TC_THREADS, smem, stream>>>(*K, P, mb, mg);
-  return cudaGetLastError() == cudaSuccess ? 0 : 7;
+  return kTcVariants[variant].epi == 8 ? tc_launch_shape<8>(K, P, mb, mg, stream)
+                                       : tc_launch_shape<12>(K, P, mb, mg, stream);
 }

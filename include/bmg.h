@@ -257,6 +257,12 @@ bmg_status bmg_reset_timings(bmg_ctx* ctx, uint64_t* n_scans);
  * (no counterpart in the reference; a measurement aid). */
 bmg_status bmg_get_launch_count(bmg_ctx* ctx, uint64_t* n_launches);
 
+/* Launch shape of the tensor-core scan (no counterpart in the reference).
+ * The first scans of a context time each shape once and keep the fastest;
+ * every shape gives the same results bit for bit.  variant is -1 while
+ * tuning; BMG_SCAN_VARIANT=<i> in the environment at bmg_create fixes it. */
+bmg_status bmg_get_scan_shape(bmg_ctx* ctx, int32_t* variant, char* name, size_t name_len);
+
 /* Per-SNP precomputed sums, allocating nothing (no counterpart in the
  * reference).  For callers that cannot call cudaMalloc, e.g. code running in
  * another framework's memory pool or while a stream is being captured.

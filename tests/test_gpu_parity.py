@@ -158,3 +158,32 @@ def test_setup_is_ordered_against_a_busy_default_stream(bmg, tmp_path):
     ctx.run(5, collect=False)
     torch.cuda.synchronize()
     ctx.close()
+
+
+@pytest.mark.parametrize("name,types", [("plain", None), ("batched", None)])
+def test_every_scan_shape_gives_the_same_results(bmg, tmp_path, monkeypatch, name, types):
+    """The launch shapes the scan's autotuner chooses between (epilogue warps,
+    chains per tile) agree with each other and with the SIMT scan bit for bit."""
+    opt, packed, y, e = synth_case(bmg, tmp_path, name, n=640, p=2000, chains=3, iters=40, n_rao=2)
+    ref = None
+    shapes = list(range(4)) + ["simt"]
+    for v in shapes:
+        if v == "simt":
+            monkeypatch.delenv("BMG_SCAN_VARIANT", raising=False)
+            opt.scan_impl = 1
+        else:
+            monkeypatch.setenv("BMG_SCAN_VARIANT", str(v))
+            opt.scan_impl = 0
+        ctx, col = run_gpu(bmg, opt, packed, y, e, 40)
+        if v != "simt":
+            assert ctx.scan_shape()[0] == v
+        out = [np.concatenate([ctx.rao(c)[0], ctx.proposal(c)[0]]) for c in range(opt.n_chains)]
+        traces = [col.chain(c)["loci"] for c in range(opt.n_chains)]
+        ctx.close()
+        if ref is None:
+            ref = (out, traces)
+        else:
+            for a, b in zip(ref[0], out):
+                np.testing.assert_array_equal(a, b)
+            for a, b in zip(ref[1], traces):
+                np.testing.assert_array_equal(a, b)
