@@ -61,7 +61,7 @@ namespace {
 #define LAUNCHED(ctx, name)                                                                      \
   do {                                                                                           \
     cudaError_t e_ = cudaGetLastError();                                                         \
-    ++(ctx)->n_launches;                                                                         \
+    if ((ctx)->capturing) ++(ctx)->graph_launches; else ++(ctx)->n_launches;                     \
     if (e_ == cudaSuccess && (ctx)->sync_check) e_ = cudaStreamSynchronize((ctx)->stream);       \
     if (e_ != cudaSuccess) throw bmg_error(BMG_ECUDA, std::string(name) + ": " + cudaGetErrorString(e_)); \
   } while (0)
@@ -75,6 +75,14 @@ struct ChainFiles {
 const char* kTypeName[5] = {"A", "H", "D", "R", "AH"};
 
 }  // namespace
+
+// One chunk of iterations as a list of segments: seg iterations of the move
+// kernel, then (rb) the scan and the prefix rebuild.
+struct Segment {
+  uint64_t iters;
+  bool rb;
+  bool operator==(const Segment& o) const { return iters == o.iters && rb == o.rb; }
+};
 
 struct bmg_ctx {
   bmg_options opt;
@@ -100,6 +108,12 @@ struct bmg_ctx {
   uint64_t n_launches = 0; // kernels of this library launched since the last counter reset
   // launch-shape autotuner of the tensor-core scan: the first scan warms
   // up, the next ones time one shape each, then the fastest is kept
+  bool eager = false;      // BMG_EAGER=1: no CUDA graphs
+  bool capturing = false;  // a chunk is being captured into a graph
+  std::vector<cudaEvent_t> seg_ev;             // 4 events per segment of a chunk
+  cudaGraphExec_t graph_exec = nullptr;        // the captured chunk
+  std::vector<Segment> graph_segs;             // ... and its segment pattern
+  uint64_t graph_launches = 0;                 // kernels in the captured chunk
   int tc_forced = -1;      // BMG_SCAN_VARIANT
   int tc_variant = -1;     // chosen shape (-1 while tuning)
   int tc_tuned = 0;        // tuning scans issued
@@ -133,6 +147,8 @@ struct bmg_ctx {
       if (e) cudaEventDestroy(e);
     for (cudaEvent_t e : tc_ev)
       if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : seg_ev) cudaEventDestroy(e);
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
     for (void* a : allocs) cudaFree(a);
     if (stream) cudaStreamDestroy(stream);
   }
@@ -263,6 +279,8 @@ extern "C" bmg_status bmg_create(const bmg_options* opt, bmg_ctx** out)
     CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     const char* sc = std::getenv("BMG_SYNC_CHECK");
     c->sync_check = sc && sc[0] && sc[0] != '0';
+    const char* eg = std::getenv("BMG_EAGER");
+    c->eager = eg && eg[0] && eg[0] != '0';
     const char* sv = std::getenv("BMG_SCAN_VARIANT");
     if (sv && sv[0]) c->tc_forced = std::max(0, std::min(bmg_scan_tc_variants() - 1, std::atoi(sv)));
     c->ch_h.resize(c->C);
@@ -989,6 +1007,43 @@ static void drain_traces(bmg_ctx* ctx, uint64_t iter0, const bmg_trace_sink* sin
   }
 }
 
+static std::vector<Segment> plan_chunk(uint64_t first_iter, uint64_t chunk, uint64_t n_rao)
+{
+  std::vector<Segment> segs;
+  uint64_t t = first_iter, i = 0;
+  while (i < chunk) {
+    const uint64_t next_rb = ((t / n_rao) + 1) * n_rao - 1;  // first iter >= t with (iter+1) % n_rao == 0
+    const uint64_t seg = std::min<uint64_t>(chunk - i, next_rb - t + 1);
+    t += seg;
+    i += seg;
+    segs.push_back({seg, t - 1 == next_rb});
+  }
+  return segs;
+}
+
+// Issue a chunk on the context stream, with an event before the move kernel,
+// after it, after the scan and after the rebuild of every segment.
+static void issue_chunk(bmg_ctx* ctx, const std::vector<Segment>& segs)
+{
+  const DevConst& K = ctx->K;
+  bmg_trace_reset_kernel<<<(ctx->C + 127) / 128, 128, 0, ctx->stream>>>(K.ch, (int)ctx->C);
+  LAUNCHED(ctx, "bmg_trace_reset_kernel");
+  const unsigned rec = ctx->capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
+  for (size_t q = 0; q < segs.size(); ++q) {
+    cudaEvent_t* ev = &ctx->seg_ev[4 * q];
+    CK(cudaEventRecordWithFlags(ev[0], ctx->stream, rec));
+    bmg_move_kernel<<<ctx->C, BMG_MOVE_THREADS, ctx->move_smem, ctx->stream>>>(K, (int)segs[q].iters);
+    LAUNCHED(ctx, "bmg_move_kernel");
+    CK(cudaEventRecordWithFlags(ev[1], ctx->stream, rec));
+    if (segs[q].rb) {
+      launch_scan(ctx);
+      CK(cudaEventRecordWithFlags(ev[2], ctx->stream, rec));
+      launch_rebuild(ctx, 0);
+      CK(cudaEventRecordWithFlags(ev[3], ctx->stream, rec));
+    }
+  }
+}
+
 extern "C" bmg_status bmg_run(bmg_ctx* ctx, uint64_t n_iter, const bmg_trace_sink* sink)
 {
   if (!ctx) return BMG_EINVAL;
@@ -996,50 +1051,71 @@ extern "C" bmg_status bmg_run(bmg_ctx* ctx, uint64_t n_iter, const bmg_trace_sin
   check_ready(ctx);
   if (ctx->n_iter == 0) ctx->t_start = time(nullptr);
   open_files(ctx);
-  DevConst& K = ctx->K;
   const uint64_t n_rao = ctx->opt.n_rao;
-  const uint32_t gi = ctx->opt.graph_iters;
-  for (int q = 0; q < 4; ++q)
-    if (!ctx->ev[q]) CK(cudaEventCreate(&ctx->ev[q]));
+  const uint32_t gi = ctx->opt.graph_iters ? ctx->opt.graph_iters : 64;
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
   CK(cudaEventRecord(e0, ctx->stream));
   uint64_t done = 0;
   while (done < n_iter) {
-    uint64_t chunk = std::min<uint64_t>(n_iter - done, gi);
-    uint64_t iter0 = ctx->n_iter;
-    bmg_trace_reset_kernel<<<(ctx->C + 127) / 128, 128, 0, ctx->stream>>>(K.ch, (int)ctx->C);
-    LAUNCHED(ctx, "bmg_trace_reset_kernel");
-    uint64_t i = 0;
-    while (i < chunk) {
-      uint64_t t = ctx->n_iter;
-      uint64_t next_rb = ((t / n_rao) + 1) * n_rao - 1;  // first iter >= t with (iter+1) % n_rao == 0
-      uint64_t seg = std::min<uint64_t>(chunk - i, next_rb - t + 1);
-      CK(cudaEventRecord(ctx->ev[0], ctx->stream));
-      bmg_move_kernel<<<ctx->C, BMG_MOVE_THREADS, ctx->move_smem, ctx->stream>>>(K, (int)seg);
-      LAUNCHED(ctx, "bmg_move_kernel");
-      CK(cudaEventRecord(ctx->ev[1], ctx->stream));
-      ctx->n_iter += seg;
-      i += seg;
-      bool rb = (ctx->n_iter - 1 == next_rb);
-      if (rb) {
-        launch_scan(ctx);
-        CK(cudaEventRecord(ctx->ev[2], ctx->stream));
-        launch_rebuild(ctx, 0);
-        CK(cudaEventRecord(ctx->ev[3], ctx->stream));
+    const uint64_t chunk = std::min<uint64_t>(n_iter - done, gi);
+    const uint64_t iter0 = ctx->n_iter;
+    const std::vector<Segment> segs = plan_chunk(iter0, chunk, n_rao);
+    while (ctx->seg_ev.size() < 4 * segs.size()) {
+      cudaEvent_t e;
+      CK(cudaEventCreate(&e));
+      ctx->seg_ev.push_back(e);
+    }
+    // a graph once the scan's launch shape is settled (its tuner reads
+    // timings between launches); BMG_EAGER=1 or BMG_SYNC_CHECK=1 keep plain
+    // launches
+    const bool tuning = ctx->opt.scan_impl == BMG_SCAN_TCGEN05 && ctx->tc_forced < 0 && ctx->tc_variant < 0;
+    const bool graph = !ctx->eager && !ctx->sync_check && !tuning;
+    if (graph) {
+      if (!ctx->graph_exec || !(ctx->graph_segs == segs)) {
+        if (ctx->graph_exec) {
+          cudaGraphExecDestroy(ctx->graph_exec);
+          ctx->graph_exec = nullptr;
+        }
+        cudaGraph_t g = nullptr;
+        CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        ctx->capturing = true;
+        ctx->graph_launches = 0;
+        try {
+          issue_chunk(ctx, segs);
+        } catch (...) {
+          ctx->capturing = false;
+          cudaStreamEndCapture(ctx->stream, &g);
+          if (g) cudaGraphDestroy(g);
+          throw;
+        }
+        ctx->capturing = false;
+        CK(cudaStreamEndCapture(ctx->stream, &g));
+        cudaError_t ie = cudaGraphInstantiate(&ctx->graph_exec, g, 0);
+        cudaGraphDestroy(g);
+        CK(ie);
+        ctx->graph_segs = segs;
       }
-      CK(cudaEventSynchronize(rb ? ctx->ev[3] : ctx->ev[1]));
+      CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+      ctx->n_launches += ctx->graph_launches;
+    } else {
+      issue_chunk(ctx, segs);
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    for (size_t q = 0; q < segs.size(); ++q) {
+      cudaEvent_t* ev = &ctx->seg_ev[4 * q];
       float a = 0, b = 0, c2 = 0;
-      CK(cudaEventElapsedTime(&a, ctx->ev[0], ctx->ev[1]));
+      CK(cudaEventElapsedTime(&a, ev[0], ev[1]));
       ctx->ms[0] += a;
-      if (rb) {
-        CK(cudaEventElapsedTime(&b, ctx->ev[1], ctx->ev[2]));
-        CK(cudaEventElapsedTime(&c2, ctx->ev[2], ctx->ev[3]));
+      if (segs[q].rb) {
+        CK(cudaEventElapsedTime(&b, ev[1], ev[2]));
+        CK(cudaEventElapsedTime(&c2, ev[2], ev[3]));
         ctx->ms[1] += b;
         ctx->ms[2] += c2;
         ctx->n_scans++;
       }
+      ctx->n_iter += segs[q].iters;
     }
     drain_traces(ctx, iter0, sink);
     device_error_check(ctx);

@@ -187,3 +187,23 @@ def test_every_scan_shape_gives_the_same_results(bmg, tmp_path, monkeypatch, nam
                 np.testing.assert_array_equal(a, b)
             for a, b in zip(ref[1], traces):
                 np.testing.assert_array_equal(a, b)
+
+
+def test_graph_replay_equals_plain_launches(bmg, tmp_path, monkeypatch):
+    """Chunks captured as CUDA graphs (re-captured when the segment pattern
+    changes) give the same chains as plain launches."""
+    opt, packed, y, e = synth_case(bmg, tmp_path, "plain", n=700, p=2500, chains=2, iters=70, n_rao=3)
+    opt.graph_iters = 16
+    outs = []
+    for eager in ("1", "0"):
+        monkeypatch.setenv("BMG_EAGER", eager)
+        ctx, col = run_gpu(bmg, opt, packed, y, e, 70)
+        outs.append(([col.chain(c) for c in range(opt.n_chains)],
+                     [ctx.rao(c)[0] for c in range(opt.n_chains)], ctx.launch_count()))
+        ctx.close()
+    (ta, ra, na), (tb, rb, nb) = outs
+    for c in range(opt.n_chains):
+        for key in H.INT_KEYS + H.FLOAT_KEYS:
+            np.testing.assert_array_equal(ta[c][key], tb[c][key], err_msg=key)
+        np.testing.assert_array_equal(ra[c], rb[c])
+    assert na == nb > 0
