@@ -55,6 +55,8 @@ def lib():
         L.bmg_precompute.argtypes = [vp]
         L.bmg_get_precomputed.argtypes = [vp, vp, C.POINTER(u32)]
         L.bmg_scan.argtypes = [vp, vp, vp]
+        L.bmg_scan_logodds.argtypes = [vp, vp]
+        L.bmg_scan_schur.argtypes = [vp, vp]
         L.bmg_run.argtypes = [vp, u64, C.POINTER(abi.TraceSink)]
         L.bmg_get_state.argtypes = [vp, u32, C.POINTER(abi.ChainState), vp, vp, u32]
         L.bmg_get_rao.argtypes = [vp, u32, vp, vp]
@@ -136,6 +138,11 @@ class Context:
         self.m_g = int(opt.m_g)
         self.n_types = int(opt.n_types)
         self.n_chains = int(opt.n_chains)
+        terms = set()
+        for i in range(int(opt.n_types)):
+            t = int(opt.types[i])
+            terms.update((0, 1) if t == 4 else (t,))
+        self.n_terms = len(terms)
         h = C.c_void_p()
         rc = lib().bmg_create(C.byref(opt), C.byref(h))
         if rc != 0:
@@ -198,6 +205,21 @@ class Context:
         if prt is not None:
             prt = prt.reshape(self.n_chains, self.m_g, self.n_types)
         return pr, prt
+
+    def scan_logodds(self):
+        """(chains, m_g) per-SNP log posterior odds of inclusion of an RB scan
+        of every chain's current state."""
+        lo = np.zeros(self.n_chains * self.m_g)
+        self._check(lib().bmg_scan_logodds(self.h, _ptr(lo)))
+        return lo.reshape(self.n_chains, self.m_g)
+
+    def scan_schur(self):
+        """(chains, m_g, terms) exact change of each chain's log marginal
+        likelihood from adding each single term of each SNP outside its model."""
+        nt = self.n_terms
+        out = np.zeros(self.n_chains * self.m_g * nt)
+        self._check(lib().bmg_scan_schur(self.h, _ptr(out)))
+        return out.reshape(self.n_chains, self.m_g, nt)
 
     def state(self, chain=0, cap=4096):
         st = abi.ChainState()

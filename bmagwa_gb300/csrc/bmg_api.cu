@@ -42,6 +42,8 @@ extern "C" cudaError_t bmg_move_configure(size_t* smem_bytes);
 // tensor-core scan (scan_tc.cu)
 extern "C" int bmg_scan_tc_launch(const DevConst* K, cudaStream_t stream, int variant);
 extern "C" int bmg_scan_tc_variants();
+extern "C" int bmg_schur_launch(const DevConst* K, const int* xcols, uint16_t** bm, size_t* bm_cap, double* out,
+                                cudaStream_t stream);
 extern "C" void bmg_scan_tc_variant_name(int v, char* buf, size_t len);
 extern "C" int bmg_scan_tc_supported(const DevConst* K);
 
@@ -114,6 +116,10 @@ struct bmg_ctx {
   cudaGraphExec_t graph_exec = nullptr;        // the captured chunk
   std::vector<Segment> graph_segs;             // ... and its segment pattern
   uint64_t graph_launches = 0;                 // kernels in the captured chunk
+  double* lml_buf = nullptr;                   // bmg_scan_logodds output on the device
+  double* schur_out = nullptr;                 // bmg_scan_schur output on the device
+  uint16_t* schur_bm = nullptr;                // its B operand (model columns), grown on demand
+  size_t schur_bm_cap = 0;
   int tc_forced = -1;      // BMG_SCAN_VARIANT
   int tc_variant = -1;     // chosen shape (-1 while tuning)
   int tc_tuned = 0;        // tuning scans issued
@@ -148,6 +154,7 @@ struct bmg_ctx {
     for (cudaEvent_t e : tc_ev)
       if (e) cudaEventDestroy(e);
     for (cudaEvent_t e : seg_ev) cudaEventDestroy(e);
+    if (schur_bm) cudaFree(schur_bm);
     if (graph_exec) cudaGraphExecDestroy(graph_exec);
     for (void* a : allocs) cudaFree(a);
     if (stream) cudaStreamDestroy(stream);
@@ -1145,6 +1152,58 @@ extern "C" bmg_status bmg_scan(bmg_ctx* ctx, double* p_r, double* p_r_types)
   if (p_r) CK(cudaMemcpyAsync(p_r, K.p_r, 8 * pc, cudaMemcpyDeviceToHost, ctx->stream));
   if (p_r_types && ctx->opt.n_types > 1)
     CK(cudaMemcpyAsync(p_r_types, K.p_r_types, 8 * pc * ctx->opt.n_types, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  device_error_check(ctx);
+  return BMG_OK;
+  API_END
+}
+
+extern "C" bmg_status bmg_scan_logodds(bmg_ctx* ctx, double* logodds)
+{
+  if (!ctx || !logodds) return BMG_EINVAL;
+  API_BEGIN
+  check_ready(ctx);
+  DevConst& K = ctx->K;
+  const size_t pc = (size_t)ctx->p * ctx->C;
+  if (!ctx->lml_buf) ctx->lml_buf = ctx->dalloc<double>(pc, false);
+  K.p_lml = ctx->lml_buf;
+  try {
+    bmg_rbprep_kernel<<<ctx->C, BMG_MOVE_THREADS, ctx->move_smem, ctx->stream>>>(K);
+    LAUNCHED(ctx, "bmg_rbprep_kernel");
+    launch_scan(ctx);
+  } catch (...) {
+    K.p_lml = nullptr;
+    throw;
+  }
+  K.p_lml = nullptr;
+  CK(cudaMemcpyAsync(logodds, ctx->lml_buf, 8 * pc, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  device_error_check(ctx);
+  return BMG_OK;
+  API_END
+}
+
+extern "C" bmg_status bmg_scan_schur(bmg_ctx* ctx, double* dlml)
+{
+  if (!ctx || !dlml) return BMG_EINVAL;
+  API_BEGIN
+  check_ready(ctx);
+  const uint32_t C = ctx->C;
+  const size_t out_n = (size_t)C * ctx->p * ctx->K.n_terms;
+  if (!ctx->schur_out) ctx->schur_out = ctx->dalloc<double>(out_n, false);
+  std::vector<DevModel> mods(C);
+  CK(cudaMemcpyAsync(mods.data(), ctx->K.cur, sizeof(DevModel) * C, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  std::vector<int> xcols(C);
+  for (uint32_t c = 0; c < C; ++c) xcols[c] = mods[c].xcols;
+  const int rc = bmg_schur_launch(&ctx->K, xcols.data(), &ctx->schur_bm, &ctx->schur_bm_cap, ctx->schur_out,
+                                  ctx->stream);
+  if (rc == 100) throw bmg_error(BMG_EUNSUPPORTED, "the Schur scan supports models of at most 128 columns");
+  if (rc != 0)
+    throw bmg_error(BMG_ECUDA, "Schur scan launch failed (step " + std::to_string(rc) +
+                                   "): " + cudaGetErrorString(cudaGetLastError()));
+  LAUNCHED(ctx, "bmg_schur_tc_kernel");
+  CK(cudaMemcpyAsync(dlml, ctx->schur_out, 8 * out_n, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   device_error_check(ctx);
   return BMG_OK;

@@ -22,8 +22,9 @@ static __device__ __forceinline__ bool rb_fast_ok(const DevConst& K)
   return !K.use_individual_tau2 && K.n_types == 1 && K.types[0] != 4;
 }
 
-// p_r of (SNP j, chain c) from the exact product xi = x_t(j)' R_c
-static __device__ __forceinline__ double rb_fast_pr(const DevConst& K, int c, uint64_t j, long long xi)
+// p_r of (SNP j, chain c) from the exact product xi = x_t(j)' R_c; *lo gets
+// the log posterior odds of inclusion
+static __device__ __forceinline__ double rb_fast_pr(const DevConst& K, int c, uint64_t j, long long xi, double* lo)
 {
   const RbParams& rp = K.rb[c];
   const int type = K.types[0];
@@ -35,17 +36,19 @@ static __device__ __forceinline__ double rb_fast_pr(const DevConst& K, int c, ui
   const double rx = xr - pre[off] * rp.mr;
   const double et = (rx * rx) / det;
   const double p = et * rp.inv_2s2 - 0.5 * (log(det) + slq) + rp.lmp_add[type];
+  *lo = p;
   const double e = exp(p);
   return isfinite(e) ? e / (1 + e) : 1;
 }
 
 // p_r and the running means of one (SNP, chain) with one effect type
 // (src/sampler.cpp:739-776)
-static __device__ __forceinline__ void rb_store1(const DevConst& K, int c, uint64_t j, double pr)
+static __device__ __forceinline__ void rb_store1(const DevConst& K, int c, uint64_t j, double pr, double lo)
 {
   const RbParams& rp = K.rb[c];
   const size_t cj = (size_t)c * K.p + j;
   if (K.p_r) K.p_r[cj] = pr;
+  if (K.p_lml) K.p_lml[cj] = lo;
   if (rp.acc_rao) K.p_rao[cj] = rp.rao_z2 * K.p_rao[cj] + pr / rp.rao_z1;
   if (rp.adapt) {
     const size_t q = (size_t)c * K.p + K.pos[j];
@@ -109,7 +112,7 @@ static __device__ __noinline__ void rb_epilogue(const DevConst& K, int c, uint64
   const int nt = K.n_types;
   const bool ut = nt > 1;
   double pt[5];
-  double pr = 0;
+  double pr = 0, lo = 0;
   double maxt = -INFINITY;
   for (int t = 0; t < nt; ++t) {
     int type = K.types[t];
@@ -136,6 +139,7 @@ static __device__ __noinline__ void rb_epilogue(const DevConst& K, int c, uint64
       if (p > maxt) maxt = p;
       pt[t] = p;
     } else {
+      lo = p;
       double e = exp(p);
       pr = isfinite(e) ? e / (1 + e) : 1;
     }
@@ -152,15 +156,18 @@ static __device__ __noinline__ void rb_epilogue(const DevConst& K, int c, uint64
         pr = 0;
       }
       if (isnan(maxt)) atomicExch(&K.ch[c].error, BMG_DERR_NAN);
+      lo = maxt;
     } else {
       double st = 0;
       for (int t = 0; t < nt; ++t) { pt[t] = exp(pt[t] - maxt); st += pt[t]; }
       for (int t = 0; t < nt; ++t) pt[t] /= st;
+      lo = log(st) + maxt;
       st = exp(log(st) + maxt);
       pr = isfinite(st) ? st / (1 + st) : 1;
     }
   }
   const size_t cj = (size_t)c * K.p + j;
+  if (K.p_lml) K.p_lml[cj] = lo;
   if (K.p_r) {
     K.p_r[cj] = pr;
     if (ut)

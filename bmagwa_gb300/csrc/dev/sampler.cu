@@ -1752,7 +1752,7 @@ __device__ void prep_rb(Warp& W, bool scan_only)
   }
   // many pending flips make every proposal draw slower: ask the rebuild
   // that follows the scan for a fresh prefix
-  if (W.lane == 0 && W.s.n_pend > BMG_PEND_REBUILD) ch->rebuild = 1;
+  if (!scan_only && W.lane == 0 && W.s.n_pend > BMG_PEND_REBUILD) ch->rebuild = 1;
   if (W.lane == 0) ch->rb_pending = do_scan || adapt;
   __syncwarp();
 }

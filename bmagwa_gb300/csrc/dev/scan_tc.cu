@@ -25,6 +25,7 @@
 #include <cstdio>
 
 #include "rb_epilogue.cuh"
+#include "tc_mainloop.cuh"
 
 namespace {
 
@@ -34,125 +35,6 @@ template <int EPI>
 struct TcShape {
   static constexpr int threads = 192 + 32 * EPI;
 };
-constexpr int TC_MAX_STAGES = 4;
-constexpr int TC_BM = 128;          // rows of D per tile
-constexpr int TC_BK = 64;           // individuals per stage (128 bytes of bf16)
-constexpr uint32_t TC_ACC_COLS = 256;  // columns of one accumulator
-constexpr uint32_t TC_TMEM_COLS = 512; // two accumulators
-constexpr uint32_t WAIT_LIMIT = 1u << 24;
-
-struct TcParams {
-  uint32_t tpad;           // rows per SNP (terms rounded up to 1, 2 or 4)
-  uint32_t snps_per_tile;  // TC_BM / tpad
-  uint32_t chains_tile;    // chains per N tile
-  uint32_t n_mma;          // N of the MMA (chains_tile * L rounded up to 16)
-  uint32_t k_chunks;       // n_pad / TC_BK
-  uint32_t stages;         // pipeline depth (2..TC_MAX_STAGES)
-  uint32_t m_tiles, n_tiles, tiles;
-  uint32_t xr_bytes;       // TC_BM x chains_tile int64 sums
-  uint32_t stage_bytes;
-  uint32_t b_bytes, a_bytes, pk_bytes;
-  int32_t term_of_row[4];  // term of row u of a SNP (-1: unused)
-};
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p)
-{
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
-{
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
-}
-
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar)
-{
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive_tx(uint64_t* bar, uint32_t bytes)
-{
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-               : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity)
-{
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-// bounded wait: false after WAIT_LIMIT polls
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity)
-{
-  for (uint32_t it = 0; it < WAIT_LIMIT; ++it)
-    if (mbar_try(bar, parity)) return true;
-  return false;
-}
-
-__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y)
-{
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
-      ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
-      : "memory");
-}
-
-// shared-memory matrix descriptor, K-major, 128-byte swizzle, 8-row atoms of 1024 B
-__device__ __forceinline__ uint64_t smem_desc(const void* p)
-{
-  uint64_t addr = smem_u32(p);
-  uint64_t d = 0;
-  d |= (addr >> 4) & 0x3FFFull;            // start address
-  d |= (uint64_t)1 << 16;                  // leading byte offset (unused for this layout)
-  d |= (uint64_t)(1024 >> 4) << 32;        // stride byte offset: next 8-row atom
-  d |= (uint64_t)1 << 46;                  // descriptor version
-  d |= (uint64_t)2 << 61;                  // 128-byte swizzle
-  return d;
-}
-
-__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc)
-{
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
-      "l"(a), "l"(b), "r"(idesc), "r"(acc)
-      : "memory");
-}
-
-__device__ __forceinline__ void mma_commit(uint64_t* bar)
-{
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
-               : "memory");
-}
-
-__device__ __forceinline__ void named_bar_sync(uint32_t id, uint32_t threads)
-{
-  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(threads) : "memory");
-}
-
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v)
-{
-  uint32_t r[32];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
-        "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
-        "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
-        "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
-}
-
 }  // namespace
 
 template <int TC_EPI_WARPS>
@@ -165,131 +47,18 @@ bmg_scan_tc_kernel(DevConst K, TcParams P, const __grid_constant__ CUtensorMap m
   // 1024-byte aligned base for the swizzled tiles; the int64 sums follow the stages
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   long long* xr_s = reinterpret_cast<long long*>(smem + P.stages * P.stage_bytes);
-  __shared__ uint64_t full_bar[TC_MAX_STAGES], aready_bar[TC_MAX_STAGES], empty_bar[TC_MAX_STAGES];
-  __shared__ uint64_t acc_full[2], acc_empty[2], drain_bar;
-  __shared__ uint32_t tmem_base_sh;
-  __shared__ volatile int abort_flag;
+  __shared__ TcCtl ctl;
   __shared__ int epi_ok;
   __shared__ uint2 lut[4][256];  // per term: byte -> 4 bf16 values
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t L = K.limbs_n;
-  const uint32_t nk = P.k_chunks, S = P.stages;
   const uint32_t ct = P.chains_tile;
   const uint32_t my_tiles = (P.tiles > blockIdx.x) ? (P.tiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
+  const uint32_t tmem = tc_setup(P, ctl, lut, TC_THREADS, TC_EPI_WARPS);
 
-  // decode tables: bf16 bit patterns of 0, 1, 2 are 0x0000, 0x3F80, 0x4000
-  for (int e = tid; e < 4 * 256; e += TC_THREADS) {
-    int term = e >> 8, byte = e & 255;
-    uint16_t h[4];
-    for (int q = 0; q < 4; ++q) {
-      int code = (byte >> (2 * q)) & 3;
-      int v = term_value(code, term);
-      h[q] = v == 0 ? 0 : (v == 1 ? 0x3F80 : 0x4000);
-    }
-    lut[term][byte] = make_uint2((uint32_t)h[0] | ((uint32_t)h[1] << 16), (uint32_t)h[2] | ((uint32_t)h[3] << 16));
-  }
-  if (tid == 0) {
-    for (uint32_t st = 0; st < S; ++st) {
-      mbar_init(&full_bar[st], 1);
-      mbar_init(&aready_bar[st], 4);
-      mbar_init(&empty_bar[st], 1);
-    }
-    for (int b = 0; b < 2; ++b) {
-      mbar_init(&acc_full[b], 1);
-      mbar_init(&acc_empty[b], TC_EPI_WARPS);
-    }
-    mbar_init(&drain_bar, 1);
-    abort_flag = 0;
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  if (warp == 5) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_sh)),
-                 "r"(TC_TMEM_COLS));
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-  }
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-  __syncthreads();
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  const uint32_t tmem = tmem_base_sh;
-
-  if (warp == 4) {
-    if (lane == 0) {
-      // TMA producer: packed genotype rows and residual digits of each stage
-      uint32_t issued = 0;
-      for (uint32_t i = 0; i < my_tiles && !abort_flag; ++i) {
-        const uint32_t tile = blockIdx.x + i * gridDim.x;
-        const uint32_t snp0 = (tile % P.m_tiles) * P.snps_per_tile;
-        const uint32_t chain0 = (tile / P.m_tiles) * ct;
-        for (uint32_t k = 0; k < nk; ++k) {
-          const uint32_t g = i * nk + k, st = g % S;
-          if (g >= S && !mbar_wait(&empty_bar[st], ((g / S) - 1) & 1)) { abort_flag = 1; break; }
-          uint8_t* sp = smem + st * P.stage_bytes;
-          mbar_arrive_tx(&full_bar[st], P.b_bytes + P.pk_bytes);
-          tma_load_2d(sp, &map_b, &full_bar[st], (int)(k * TC_BK), (int)(chain0 * L));
-          tma_load_2d(sp + P.b_bytes + P.a_bytes, &map_g, &full_bar[st], (int)(k * (TC_BK / 4)), (int)snp0);
-          ++issued;
-        }
-      }
-      // no load may still be landing in shared memory when the CTA exits:
-      // wait (bounded) for the last load of every stage
-      for (uint32_t g = issued > S ? issued - S : 0; g < issued; ++g) mbar_wait(&full_bar[g % S], (g / S) & 1);
-    }
-  } else if (warp == 5) {
-    if (lane == 0) {
-      // MMA issuer: tile i accumulates into buffer i & 1
-      const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((P.n_mma >> 3) << 17) | ((uint32_t)(TC_BM >> 4) << 24);
-      for (uint32_t i = 0; i < my_tiles && !abort_flag; ++i) {
-        const uint32_t b = i & 1, u = i >> 1;
-        if (u >= 1 && !mbar_wait(&acc_empty[b], (u - 1) & 1)) { abort_flag = 1; break; }
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t d = tmem + b * TC_ACC_COLS;
-        bool ok = true;
-        for (uint32_t k = 0; k < nk; ++k) {
-          const uint32_t g = i * nk + k, st = g % S, par = (g / S) & 1;
-          if (!mbar_wait(&full_bar[st], par) || !mbar_wait(&aready_bar[st], par)) { ok = false; break; }
-          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-          uint8_t* sp = smem + st * P.stage_bytes;
-          uint64_t bdesc = smem_desc(sp), adesc = smem_desc(sp + P.b_bytes);
-#pragma unroll
-          for (int kk = 0; kk < TC_BK / 16; ++kk)  // 16 bf16 = 32 bytes = 2 descriptor units
-            mma_bf16(d, adesc + 2 * kk, bdesc + 2 * kk, idesc, (k | kk) != 0);
-          mma_commit(&empty_bar[st]);
-        }
-        if (!ok) { abort_flag = 1; break; }
-        mma_commit(&acc_full[b]);
-      }
-      // every MMA issued has completed before tensor memory is freed
-      mma_commit(&drain_bar);
-      if (!mbar_wait(&drain_bar, 0)) abort_flag = 1;
-    }
-  } else if (warp < 4) {
-    // decode warps: packed 2-bit codes -> bf16 rows of the swizzled A tile
-    const uint32_t row = tid;  // 0..127
-    const uint32_t sl = row / P.tpad, u = row % P.tpad;
-    const int term = P.term_of_row[u];
-    const uint32_t total = my_tiles * nk;
-    for (uint32_t g = 0; g < total; ++g) {
-      if (abort_flag) break;
-      const uint32_t st = g % S, par = (g / S) & 1;
-      if (!mbar_wait(&full_bar[st], par)) { abort_flag = 1; break; }
-      uint8_t* sp = smem + st * P.stage_bytes;
-      uint8_t* a = sp + P.b_bytes;
-      const uint8_t* pk = sp + P.b_bytes + P.a_bytes + sl * 16;
-      uint4 bytes = *reinterpret_cast<const uint4*>(pk);
-      uint32_t w[4] = {bytes.x, bytes.y, bytes.z, bytes.w};
-#pragma unroll
-      for (int c = 0; c < 8; ++c) {
-        uint32_t two = (w[c >> 1] >> ((c & 1) * 16)) & 0xFFFF;
-        uint2 lo = (term >= 0) ? lut[term][two & 255] : make_uint2(0, 0);
-        uint2 hi = (term >= 0) ? lut[term][two >> 8] : make_uint2(0, 0);
-        uint4 v = make_uint4(lo.x, lo.y, hi.x, hi.y);
-        *reinterpret_cast<uint4*>(a + row * 128 + ((c ^ (row & 7)) << 4)) = v;
-      }
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&aready_bar[st]);
-    }
+  if (warp < 6) {
+    tc_main_roles(P, ctl, lut, smem, tmem, my_tiles, map_b, map_g);
   } else {
     // epilogue warps: warp w reads TMEM lanes 32 (w % 4) .. +31 (the rows of
     // the tile); the TC_EPI_WARPS / 4 warps of a quarter split the chains
@@ -309,11 +78,11 @@ bmg_scan_tc_kernel(DevConst K, TcParams P, const __grid_constant__ CUtensorMap m
       // the same number of named-barrier steps
       if (e == 0) {
         bool ok = false;
-        if (lane == 0) ok = !abort_flag && mbar_wait(&acc_full[b], u & 1);
+        if (lane == 0) ok = !ctl.abort_flag && mbar_wait(&ctl.acc_full[b], u & 1);
         ok = __shfl_sync(0xffffffffu, ok, 0);
         if (lane == 0) {
           epi_ok = ok;
-          if (!ok) abort_flag = 1;
+          if (!ok) ctl.abort_flag = 1;
         }
       }
       named_bar_sync(1, ethreads);
@@ -343,7 +112,7 @@ bmg_scan_tc_kernel(DevConst K, TcParams P, const __grid_constant__ CUtensorMap m
       }
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       __syncwarp();
-      if (lane == 0) mbar_arrive(&acc_empty[b]);
+      if (lane == 0) mbar_arrive(&ctl.acc_empty[b]);
       named_bar_sync(1, ethreads);
       // one unit per (SNP, chain), SNPs fastest so that a warp's stores to
       // the chain-major running means are contiguous; two units per step
@@ -365,14 +134,15 @@ bmg_scan_tc_kernel(DevConst K, TcParams P, const __grid_constant__ CUtensorMap m
         }
         if (fast) {
           const long long xa = xr_s[sl[0] * ct + cl[0]], xb = xr_s[sl[1] * ct + cl[1]];
-          const double pa = rb_fast_pr(K, (int)c[0], j[0], xa);
-          const double pb = rb_fast_pr(K, (int)c[1], j[1], xb);
-          const double pr[2] = {pa, pb};
+          double la, lb;
+          const double pa = rb_fast_pr(K, (int)c[0], j[0], xa, &la);
+          const double pb = rb_fast_pr(K, (int)c[1], j[1], xb, &lb);
+          const double pr[2] = {pa, pb}, lo[2] = {la, lb};
           const long long xi[2] = {xa, xb};
           for (int h = 0; h < 2; ++h) {
             if (!live[h]) continue;
             if (!in_model(K, (int)c[h], j[h])) {
-              rb_store1(K, (int)c[h], j[h], pr[h]);
+              rb_store1(K, (int)c[h], j[h], pr[h], lo[h]);
             } else {
               long long xr[4] = {0, 0, 0, 0};
               xr[K.types[0]] = xi[h];
@@ -395,29 +165,11 @@ bmg_scan_tc_kernel(DevConst K, TcParams P, const __grid_constant__ CUtensorMap m
     }
   }
 
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-  __syncthreads();
-  if (tid == 0 && abort_flag) atomicExch(&K.ch[0].error, BMG_DERR_TIMEOUT);
-  if (warp == 5) {
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS));
-  }
+  if (tc_teardown(ctl, tmem) && tid == 0) atomicExch(&K.ch[0].error, BMG_DERR_TIMEOUT);
 }
 
 // ----------------------------------------------------------------- host side
 
-static PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
-{
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  if (!fn) {
-    cudaDriverEntryPointQueryResult q;
-    void* p = nullptr;
-    if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-  }
-  return fn;
-}
 
 // dynamic shared memory of a plan: the stage ring, the int64 sums, alignment slack
 static size_t tc_smem_bytes(const TcParams& P)
@@ -448,6 +200,7 @@ static bool tc_plan(const DevConst* K, TcParams* P, uint32_t ct_cap)
     P->b_bytes = P->n_mma * 128;
     P->stage_bytes = ((P->b_bytes + P->a_bytes + P->pk_bytes + 1023) / 1024) * 1024;
     P->xr_bytes = TC_BM * ct * 8;
+    P->b_rows_per_tile = ct * L;
     for (uint32_t st = TC_MAX_STAGES; st >= 2; --st) {
       P->stages = st;
       if (tc_smem_bytes(*P) <= TC_SMEM_LIMIT) {

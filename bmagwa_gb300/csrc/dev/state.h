@@ -236,6 +236,7 @@ struct DevConst {
   int64_t* cadd;        // chains x (p + 1) prefix of dd_add weights (x 2^qs) in in-order
   uint32_t* inbits;     // chains x ceil(p/32): SNP in current model
   uint32_t* basebits;   // chains x ceil(p/32): zeroed in the cadd base
+  double* p_lml;        // chains x p: log posterior odds of inclusion of the last scan, when requested (else null)
   int64_t* tile_sums;   // chains x ceil(p / BMG_REBUILD_TILE): rebuild pass 1
   int32_t* rebuild_active;  // chains: this rebuild covers the chain
   int32_t* model_inds;  // chains x p: current model's index or -1

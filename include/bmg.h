@@ -202,6 +202,26 @@ bmg_status bmg_get_precomputed(bmg_ctx* ctx, double* xx, uint32_t* offset);
  * p_r: n_chains x m_g; p_r_types: n_chains x m_g x n_types (may be NULL). */
 bmg_status bmg_scan(bmg_ctx* ctx, double* p_r, double* p_r_types);
 
+/* The same scan with the per-SNP log posterior odds of inclusion written to
+ * logodds (chains x m_g, chain-major): log of p_r / (1 - p_r), computed
+ * before the logistic, the per-SNP Bayes factor with its prior odds
+ * (src/sampler.cpp:193-195; with several effect types log sum_t exp,
+ * :241-255).  No
+ * counterpart entry point in the reference; its error against the FP64
+ * oracle is the one the parity tests bound. */
+bmg_status bmg_scan_logodds(bmg_ctx* ctx, double* logodds);
+
+/* The exact change of every chain's log marginal likelihood from adding each
+ * single term of each SNP outside its model (no counterpart entry point in
+ * the reference: Model::update_likelihood_on_add, src/model.hpp:432-506,
+ * evaluated for every candidate without changing the model).  dlml receives
+ * chains x m_g x terms doubles (terms: the allowed single codings A, H, D, R
+ * in that order; AH contributes A and H), NaN for SNPs in the model and -inf
+ * where the enlarged system is not positive definite.  The prior precision
+ * of a term is the chain's shared tau2 value.  Models of more than 128
+ * columns return BMG_EUNSUPPORTED. */
+bmg_status bmg_scan_schur(bmg_ctx* ctx, double* dlml);
+
 /* Advance every chain by n_iter MCMC iterations (replaces the main loop of
  * Sampler::sample, src/sampler.cpp:626-834).  Traces go to `sink` (may be
  * NULL) and, with opt.write_files, to the reference's files. */

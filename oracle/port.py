@@ -23,7 +23,9 @@ def build(verbose=False):
     """Compile the port (and nothing else) into oracle/_build."""
     os.makedirs(os.path.dirname(PORT_LIB), exist_ok=True)
     inc = os.path.join(HERE, "..", "include")
-    cmd = ["g++", "-std=c++17", "-O3", "-fPIC", "-shared", "-I" + inc,
+    # no FMA contraction: the same arithmetic on x86-64 and aarch64 (gcc
+    # contracts a*b+c by default where the target has FMA)
+    cmd = ["g++", "-std=c++17", "-O3", "-ffp-contract=off", "-fPIC", "-shared", "-I" + inc,
            "-I" + os.path.join(HERE, "port"), os.path.join(HERE, "port", "port.cpp"),
            "-x", "c", os.path.join(HERE, "linalg.c"), "-o", PORT_LIB, "-lpthread"]
     subprocess.run(cmd, check=True, capture_output=not verbose)
@@ -50,6 +52,8 @@ def lib():
                                      C.POINTER(C.c_void_p), C.c_char_p, C.c_size_t]
         L.bmgport_run.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32, C.POINTER(abi.TraceSink)]
         L.bmgport_scan.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]
+        L.bmgport_scan_logodds.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p]
+        L.bmgport_schur.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]
         L.bmgport_scan_yhat.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_double, C.c_void_p,
                                         C.c_void_p]
         L.bmgport_get_state.argtypes = [C.c_void_p, C.c_uint32, C.POINTER(abi.ChainState),
@@ -81,6 +85,11 @@ class Port:
         self.opt = opt
         self.m_g = int(opt.m_g)
         self.n_types = int(opt.n_types)
+        terms = set()
+        for i in range(self.n_types):
+            t = int(opt.types[i])
+            terms.update((0, 1) if t == 4 else (t,))
+        self.n_terms = len(terms)
         h = C.c_void_p()
         err = C.create_string_buffer(512)
         rc = lib().bmgport_create(C.byref(opt), _ptr(self._keep[0]), _ptr(self._keep[1]),
@@ -107,6 +116,24 @@ class Port:
         if lib().bmgport_scan(self.h, chain, _ptr(pr), _ptr(prt)) != 0:
             raise RuntimeError("oracle scan failed")
         return pr, (prt.reshape(self.m_g, self.n_types) if prt is not None else None)
+
+    def scan_logodds(self, chain=0):
+        """Per-SNP log posterior odds of inclusion from an RB scan of the
+        chain's current state."""
+        lo = np.zeros(self.m_g)
+        if lib().bmgport_scan_logodds(self.h, chain, _ptr(lo)) != 0:
+            raise RuntimeError("oracle scan failed")
+        return lo
+
+    def schur(self, chain=0):
+        """(p, terms) change of the model LML from adding each single term of
+        each SNP outside the model (NaN inside), and the 4 prior precisions."""
+        nt = self.n_terms
+        out = np.zeros(self.m_g * nt)
+        itv = np.zeros(4)
+        if lib().bmgport_schur(self.h, chain, _ptr(out), _ptr(itv)) != 0:
+            raise RuntimeError("oracle Schur scan failed")
+        return out.reshape(self.m_g, nt), itv
 
     def scan_yhat(self, y_hat, sigma2, chain=0):
         pr = np.zeros(self.m_g)

@@ -1176,6 +1176,8 @@ struct Sampler {
   }
 
   /* src/sampler.cpp:32-261 */
+  double* logodds_out = nullptr;  // when set: the log posterior odds of inclusion per SNP
+
   void p_raoblackwell(const std::vector<double>& y_hat, double* pr, double* prt)
   {
     const Model* cm = cur;
@@ -1274,6 +1276,7 @@ struct Sampler {
           if (p > max_types) max_types = p;
           prt[i * nt + t] = p;
         } else {
+          if (logodds_out) logodds_out[i] = p;
           p = exp(p);
           pr[i] = std::isfinite(p) ? p / (1 + p) : 1;
         }
@@ -1294,6 +1297,7 @@ struct Sampler {
             for (size_t t = 0; t < nt; ++t) prt[i * nt + t] = 1.0 / nt;
             pr[i] = 0;
           }
+          if (logodds_out) logodds_out[i] = max_types;
           continue;
         }
         double st = 0;
@@ -1302,8 +1306,53 @@ struct Sampler {
           st += prt[i * nt + t];
         }
         for (size_t t = 0; t < nt; ++t) prt[i * nt + t] /= st;
+        if (logodds_out) logodds_out[i] = log(st) + max_types;
         st = exp(log(st) + max_types);
         pr[i] = std::isfinite(st) ? st / (1 + st) : 1;
+      }
+    }
+  }
+
+  /* The exact change of the current model's log marginal likelihood from
+     adding single term t of SNP j, for every SNP outside the model and every
+     allowed single term (A, H, D, R in that order): the formulas of
+     Model::update_likelihood_on_add (src/model.hpp:432-506) evaluated on the
+     new column alone, with the chain's shared prior precision of the term;
+     the model is left unchanged.  NaN for SNPs in the model. */
+  void schur_scan(double* out, double* itv_out)
+  {
+    const Model* m = cur;
+    const size_t n = dm->n, k = m->xcols;
+    std::vector<int> terms;
+    for (int t = 0; t < 4; ++t)
+      if (dm->allow_terms(t)) terms.push_back(t);
+    std::vector<double> xcol(n), g(k > 0 ? k : 1);
+    for (int t = 0; t < 4; ++t) itv_out[t] = dm->allow_terms(t) ? prior->inv_tau2_alpha2[t] : NAN;
+    for (size_t j = 0; j < m_g; ++j) {
+      for (size_t u = 0; u < terms.size(); ++u) {
+        double& o = out[j * terms.size() + u];
+        if (m->model_inds[j] >= 0) {
+          o = NAN;
+          continue;
+        }
+        const int t = terms[u];
+        const double inv_val = prior->inv_tau2_alpha2[t];
+        dm->get_genotypes(t, j, xcol.data());
+        const double xy = ddot(n, xcol.data(), data->y.data());
+        const double xxc = ddot(n, xcol.data(), xcol.data());
+        cblas_dgemv(CblasColMajor, CblasTrans, (int)n, (int)k, 1.0, m->x.data(), (int)n, xcol.data(), 1, 0.0,
+                    g.data(), 1);
+        cblas_dtrsv(CblasColMajor, CblasUpper, CblasTrans, CblasNonUnit, (int)k, m->l.data(), (int)m->cap,
+                    g.data(), 1);
+        const double lmm2 = xxc + inv_val - ddot(k, g.data(), g.data());
+        if (lmm2 <= 0) {
+          o = -INFINITY;
+          continue;
+        }
+        const double lcc = sqrt(lmm2);
+        const double vc = (xy - ddot(k, g.data(), m->v.data())) / lcc;
+        const double syx2 = m->syx_plus_vs2 - vc * vc;
+        o = 0.5 * log(inv_val) - log(lcc) + prior->minus_n_plus_nu_2 * (log(syx2) - log(m->syx_plus_vs2));
       }
     }
   }
@@ -1965,6 +2014,32 @@ extern "C" int bmgport_scan(bmgport* P, uint32_t chain, double* p_r, double* p_r
     std::vector<double> prt(s->use_types ? s->m_g * s->n_types : 1);
     s->p_raoblackwell(s->cur->y_hat, p_r, prt.data());
     if (p_r_types && s->use_types) std::memcpy(p_r_types, prt.data(), prt.size() * sizeof(double));
+    return 0;
+  } catch (...) {
+    return 1;
+  }
+}
+
+// the RB scan of the current state with the per-SNP log posterior odds of
+// inclusion (the quantity the probabilities are the logistic of)
+extern "C" int bmgport_scan_logodds(bmgport* P, uint32_t chain, double* logodds)
+{
+  try {
+    Sampler* s = P->p.chains.at(chain);
+    std::vector<double> pr(s->m_g), prt(s->use_types ? s->m_g * s->n_types : 1);
+    s->logodds_out = logodds;
+    s->p_raoblackwell(s->cur->y_hat, pr.data(), prt.data());
+    s->logodds_out = nullptr;
+    return 0;
+  } catch (...) {
+    return 1;
+  }
+}
+
+extern "C" int bmgport_schur(bmgport* P, uint32_t chain, double* dlml, double* itv)
+{
+  try {
+    P->p.chains.at(chain)->schur_scan(dlml, itv);
     return 0;
   } catch (...) {
     return 1;

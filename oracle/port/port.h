@@ -33,6 +33,8 @@ int bmgport_run(bmgport* P, uint64_t n_iter, uint32_t n_threads,
                 const bmg_trace_sink* sink);
 /* RB scan of one chain against y - y_hat of its current model */
 int bmgport_scan(bmgport* P, uint32_t chain, double* p_r, double* p_r_types);
+int bmgport_scan_logodds(bmgport* P, uint32_t chain, double* logodds);
+int bmgport_schur(bmgport* P, uint32_t chain, double* dlml, double* itv);
 /* RB scan of one chain against y - y_hat with sigma2 replaced (known-answer tests) */
 int bmgport_scan_yhat(bmgport* P, uint32_t chain, const double* y_hat, double sigma2,
                       double* p_r, double* p_r_types);

@@ -207,3 +207,85 @@ def test_graph_replay_equals_plain_launches(bmg, tmp_path, monkeypatch):
             np.testing.assert_array_equal(ta[c][key], tb[c][key], err_msg=key)
         np.testing.assert_array_equal(ra[c], rb[c])
     assert na == nb > 0
+
+
+@pytest.mark.parametrize("case", [
+    dict(name="plain", n=900, p=3000, chains=2, n_rao=1),
+    dict(name="batched", n=1000, p=3000, chains=2, n_rao=5),
+], ids=["one_type", "A_AH"])
+def test_scan_log_odds_error_against_fp64_oracle(bmg, oracle, tmp_path, case):
+    """The per-SNP log posterior odds of the GPU scan (exact integer products,
+    FP64 epilogue) against the FP64 oracle's, after identical trajectories:
+    relative error at most 1e-9 (relative to max(|value|, 1)).  The move-size
+    tuning is off here: early in burn-in its criterion ties across the grid and
+    last-bit differences of exp between the GPU and the CPU can break the tie
+    differently, which would give the two sides different states to scan."""
+    iters = 100  # a multiple of thin: both sides scan the same fitted values
+    opt, packed, y, e = synth_case(bmg, tmp_path, iters=iters, **case)
+    opt.adapt_p_move_size = 0
+    port = oracle.Port(opt, packed, y, e)
+    colp = port.run(iters)
+    ctx, colg = run_gpu(bmg, opt, packed, y, e, iters)
+    for c in range(opt.n_chains):
+        a, b = colp.chain(c), colg.chain(c)
+        for key in H.INT_KEYS:
+            if len(a[key]) != len(b[key]) or np.any(a[key] != b[key]):
+                n = min(len(a[key]), len(b[key]))
+                first = int(np.argmax(a[key][:n] != b[key][:n])) if np.any(a[key][:n] != b[key][:n]) else n
+                print("chain", c, "trace", key, "differs first at", first, "of", n)
+                for k2 in ("move_type", "move_size", "jumpdistance"):
+                    print("  ", k2, "oracle", a[k2][max(0, first - 3):first + 3].tolist(),
+                          "gpu", b[k2][max(0, first - 3):first + 3].tolist())
+                break
+        ll_a, ll_b = np.asarray(a["log_likelihood"]), np.asarray(b["log_likelihood"])
+        n = min(len(ll_a), len(ll_b))
+        d = np.nonzero(np.abs(ll_a[:n] - ll_b[:n]) > 1e-9 * np.abs(ll_a[:n]))[0]
+        if len(d):
+            print("chain", c, "log_likelihood differs first at", int(d[0]), ll_a[d[0]], ll_b[d[0]])
+    lo = ctx.scan_logodds()
+    pr_gpu, _ = ctx.scan()
+    worst = 0.0
+    for c in range(opt.n_chains):
+        ref = port.scan_logodds(c)
+        pr_ref, _ = port.scan(c)
+        assert np.all(np.isfinite(ref))
+        rel = np.abs(lo[c] - ref) / np.maximum(np.abs(ref), 1.0)
+        if rel.max() > 1e-9:
+            bad = np.argsort(-rel)[:5]
+            st = ctx.state(c)[0]
+            print("chain", c, "model size", st.model_size, "worst SNPs", bad.tolist())
+            print(" gpu lo", lo[c][bad].tolist(), "ref lo", ref[bad].tolist())
+            print(" gpu pr", pr_gpu[c][bad].tolist(), "ref pr", pr_ref[bad].tolist())
+            print(" max |pr diff|", float(np.abs(pr_gpu[c] - pr_ref).max()))
+        worst = max(worst, float(rel.max()))
+    print("max relative error of the per-SNP log odds: %.3e" % worst)
+    assert worst <= 1e-9
+
+
+@pytest.mark.parametrize("case", [
+    dict(name="plain", n=900, p=2500, chains=3, n_rao=5),
+    dict(name="batched", n=1000, p=2500, chains=2, n_rao=5),
+], ids=["one_type", "A_AH"])
+def test_schur_scan_against_fp64_oracle(bmg, oracle, tmp_path, case):
+    """The exact per-SNP conditional LML change (tcgen05 X'X_gamma products,
+    FP64 Schur complement) against the FP64 oracle's update_likelihood_on_add
+    on every candidate, after identical trajectories: NaN for SNPs in the
+    model on both sides, relative error at most 1e-9 elsewhere."""
+    iters = 100
+    opt, packed, y, e = synth_case(bmg, tmp_path, iters=iters, **case)
+    opt.adapt_p_move_size = 0
+    port = oracle.Port(opt, packed, y, e)
+    port.run(iters)
+    ctx, _ = run_gpu(bmg, opt, packed, y, e, iters)
+    dl = ctx.scan_schur()
+    worst = 0.0
+    for c in range(opt.n_chains):
+        ref, _ = port.schur(c)
+        np.testing.assert_array_equal(np.isnan(dl[c]), np.isnan(ref))
+        m = ~np.isnan(ref)
+        assert np.all(np.isfinite(ref[m]))
+        rel = np.abs(dl[c][m] - ref[m]) / np.maximum(np.abs(ref[m]), 1.0)
+        worst = max(worst, float(rel.max()))
+        assert ctx.state(c)[0].model_size > 0
+    print("max relative error of the per-SNP LML change: %.3e" % worst)
+    assert worst <= 1e-9

@@ -181,3 +181,41 @@ def test_oracle_matches_reference_traces(bmg, oracle, tmp_path, name):
         assert np.array_equal(rao, ref["rao"])
         if raot is not None:
             assert np.array_equal(raot.reshape(-1), ref["rao_types"])
+
+
+def test_schur_scan_matches_dense_lml(bmg, oracle):
+    """The oracle's per-SNP Schur scan (update_likelihood_on_add's formulas on
+    each candidate column) equals LML(model + column) - LML(model) computed
+    densely with numpy, for a chain state reached by sampling."""
+    rng = np.random.default_rng(11)
+    n, p = 120, 60
+    g = rng.integers(0, 3, size=(p, n))
+    code = np.where(g == 0, 0, np.where(g == 1, 2, 3)).astype(np.uint8)
+    pad = np.zeros((p, (n + 3) // 4 * 4), dtype=np.uint8)
+    pad[:, :n] = code
+    pad = pad.reshape(p, -1, 4)
+    packed = (pad[..., 0] | pad[..., 1] << 2 | pad[..., 2] << 4 | pad[..., 3] << 6).astype(np.uint8)
+    y = 0.8 * H.coding(g[7], 0) - 0.6 * H.coding(g[21], 0) + rng.normal(size=n)
+    o = small_opts(bmg, n, p, [0], nu_sigma2=2, s2_sigma2=0.7, inv_tau2_e_const_val=0.01)
+    port = oracle.Port(o, packed.reshape(-1), y)
+    port.run(40)
+    st, loci, tinds = port.state(0)
+    assert len(loci) >= 1
+    dl, itv = port.schur(0)
+    cols, precs = [np.ones(n)], [0.01]
+    for s_ in loci:
+        cols.append(H.coding(g[s_], 0))
+        precs.append(itv[0])
+    X = np.stack(cols, 1)
+    base = H.lml_numpy(X, y, np.array(precs), 2 * 0.7 + y @ y, n + 2)
+    assert base == pytest.approx(st.log_likelihood, rel=1e-10)
+    checked = 0
+    for j in range(p):
+        if j in set(loci.tolist()):
+            assert np.isnan(dl[j, 0])
+            continue
+        Xj = np.column_stack([X, H.coding(g[j], 0)])
+        exp = H.lml_numpy(Xj, y, np.array(precs + [itv[0]]), 2 * 0.7 + y @ y, n + 2) - base
+        assert dl[j, 0] == pytest.approx(exp, rel=1e-9, abs=1e-9)
+        checked += 1
+    assert checked == p - len(loci)
