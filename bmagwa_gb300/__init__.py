@@ -57,6 +57,8 @@ def lib():
         L.bmg_scan.argtypes = [vp, vp, vp]
         L.bmg_scan_logodds.argtypes = [vp, vp]
         L.bmg_scan_schur.argtypes = [vp, vp]
+        L.bmg_learned_snapshot.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+        L.bmg_learned_grad.argtypes = [vp, vp, u32, vp]
         L.bmg_run.argtypes = [vp, u64, C.POINTER(abi.TraceSink)]
         L.bmg_get_state.argtypes = [vp, u32, C.POINTER(abi.ChainState), vp, vp, u32]
         L.bmg_get_rao.argtypes = [vp, u32, vp, vp]
@@ -220,6 +222,30 @@ class Context:
         out = np.zeros(self.n_chains * self.m_g * nt)
         self._check(lib().bmg_scan_schur(self.h, _ptr(out)))
         return out.reshape(self.n_chains, self.m_g, nt)
+
+    MLP_NPAR = 18817
+
+    def learned_snapshot(self, features=False):
+        """(theta, logits (chains, m_g), features (chains, m_g, 16) or None,
+        tables: list of (snps, weights) per chain) of the learned proposal."""
+        C_, p = self.n_chains, self.m_g
+        topk = int(self.opt.learned_topk)
+        th = np.zeros(self.MLP_NPAR, dtype=np.float32)
+        lg = np.zeros(C_ * p, dtype=np.float32)
+        ft = np.zeros(C_ * p * 16, dtype=np.float32) if features else None
+        ts = np.zeros(C_ * topk, dtype=np.uint32)
+        tw = np.zeros(C_ * topk)
+        tn = np.zeros(C_, dtype=np.uint32)
+        self._check(lib().bmg_learned_snapshot(self.h, _ptr(th), _ptr(lg), _ptr(ft), _ptr(ts), _ptr(tw), _ptr(tn)))
+        tables = [(ts[c * topk:c * topk + tn[c]].copy(), tw[c * topk:c * topk + tn[c]].copy()) for c in range(C_)]
+        return th, lg.reshape(C_, p), (ft.reshape(C_, p, 16) if features else None), tables
+
+    def learned_grad(self, rows):
+        """Gradient of the training loss over rows [(chain, snp), ...]."""
+        r = np.ascontiguousarray(np.asarray(rows, dtype=np.uint32).reshape(-1, 2))
+        g = np.zeros(self.MLP_NPAR, dtype=np.float32)
+        self._check(lib().bmg_learned_grad(self.h, _ptr(r), len(r), _ptr(g)))
+        return g
 
     def state(self, chain=0, cap=4096):
         st = abi.ChainState()

@@ -74,6 +74,11 @@ class Options(C.Structure):
         ("graph_iters", C.c_uint32),
         ("write_files", C.c_int32),
         ("quiet", C.c_int32),
+        ("learned_mix", C.c_double),
+        ("learned_topk", C.c_uint32),
+        ("learned_every", C.c_uint32),
+        ("learned_steps", C.c_uint32),
+        ("learned_lr", C.c_double),
     ]
 
 

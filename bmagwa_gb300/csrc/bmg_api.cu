@@ -42,6 +42,13 @@ extern "C" cudaError_t bmg_move_configure(size_t* smem_bytes);
 // tensor-core scan (scan_tc.cu)
 extern "C" int bmg_scan_tc_launch(const DevConst* K, cudaStream_t stream, int variant);
 extern "C" int bmg_scan_tc_variants();
+extern "C" cudaError_t bmg_mlp_init(const DevConst* K, int32_t* adam_t, cudaStream_t s);
+extern "C" cudaError_t bmg_mlp_refresh(const DevConst* K, uint32_t km, int steps, float lr, int32_t* adam_t,
+                                       cudaStream_t s);
+extern "C" cudaError_t bmg_mlp_features(const DevConst* K, float* out, cudaStream_t s);
+extern "C" cudaError_t bmg_mlp_forward(const DevConst* K, cudaStream_t s);
+extern "C" cudaError_t bmg_mlp_grad(const DevConst* K, const int32_t* adam_t, const uint32_t* rows, uint32_t n,
+                                    cudaStream_t s);
 extern "C" int bmg_schur_launch(const DevConst* K, const int* xcols, uint16_t** bm, size_t* bm_cap, double* out,
                                 cudaStream_t stream);
 extern "C" void bmg_scan_tc_variant_name(int v, char* buf, size_t len);
@@ -83,7 +90,8 @@ const char* kTypeName[5] = {"A", "H", "D", "R", "AH"};
 struct Segment {
   uint64_t iters;
   bool rb;
-  bool operator==(const Segment& o) const { return iters == o.iters && rb == o.rb; }
+  bool refresh;  // learned proposal refreshed after the RB step
+  bool operator==(const Segment& o) const { return iters == o.iters && rb == o.rb && refresh == o.refresh; }
 };
 
 struct bmg_ctx {
@@ -116,7 +124,9 @@ struct bmg_ctx {
   cudaGraphExec_t graph_exec = nullptr;        // the captured chunk
   std::vector<Segment> graph_segs;             // ... and its segment pattern
   uint64_t graph_launches = 0;                 // kernels in the captured chunk
-  double* lml_buf = nullptr;                   // bmg_scan_logodds output on the device
+  double* lml_buf = nullptr;                   // per-SNP log odds of the scans (bmg_scan_logodds, learned proposal)
+  int32_t* adam_t = nullptr;                   // learned proposal: optimiser step counter (device)
+  uint64_t rb_steps = 0;                       // RB steps issued by bmg_run
   double* schur_out = nullptr;                 // bmg_scan_schur output on the device
   uint16_t* schur_bm = nullptr;                // its B operand (model columns), grown on demand
   size_t schur_bm_cap = 0;
@@ -260,6 +270,12 @@ extern "C" bmg_status bmg_create(const bmg_options* opt, bmg_ctx** out)
       throw bmg_error(BMG_EUNSUPPORTED, "only the PMV sampler runs on the GPU path");
     if (opt->delay_rejection != 0)
       throw bmg_error(BMG_EUNSUPPORTED, "delayed rejection is not on the GPU path (set delay_rejection = 0)");
+    if (opt->proposal != BMG_PROPOSAL_ADAPTIVE && opt->proposal != BMG_PROPOSAL_LEARNED)
+      throw bmg_error(BMG_EINVAL, "proposal must be BMG_PROPOSAL_ADAPTIVE or BMG_PROPOSAL_LEARNED");
+    if (opt->proposal == BMG_PROPOSAL_LEARNED &&
+        (!(opt->learned_mix >= 0 && opt->learned_mix < 1) || opt->learned_topk == 0 || opt->learned_topk > 65536 ||
+         opt->learned_every == 0 || !(opt->learned_lr > 0)))
+      throw bmg_error(BMG_EINVAL, "learned proposal: mix in [0, 1), topk in 1..65536, every >= 1, lr > 0");
     if (opt->n == 0 || opt->m_g == 0) throw bmg_error(BMG_EINVAL, "n and m_g must be positive");
     if (opt->n_types == 0 || opt->n_types > 5) throw bmg_error(BMG_EINVAL, "types");
     if (opt->thin == 0 || opt->n_rao == 0 || opt->n_sample_tau2_and_missing == 0)
@@ -719,6 +735,30 @@ extern "C" bmg_status bmg_precompute(bmg_ctx* ctx)
   K.basebits = ctx->dalloc<uint32_t>(words * C);
   K.tile_sums = ctx->dalloc<int64_t>((size_t)C * ((p + BMG_REBUILD_TILE - 1) / BMG_REBUILD_TILE));
   K.rebuild_active = ctx->dalloc<int32_t>(C);
+  // learned proposal: candidate tables, features, MLP parameters
+  K.lrn.on = o.proposal == BMG_PROPOSAL_LEARNED;
+  if (K.lrn.on) {
+    DevLearned& L = K.lrn;
+    L.mix = o.learned_mix;
+    L.topk = o.learned_topk;
+    L.t_snp = ctx->dalloc<uint32_t>((size_t)C * L.topk);
+    L.t_s = ctx->dalloc<double>((size_t)C * L.topk);
+    L.t_sum = ctx->dalloc<double>(C);
+    L.t_n = ctx->dalloc<uint32_t>(C);
+    L.maxcorr = ctx->dalloc<float>((size_t)C * p);
+    L.logit = ctx->dalloc<float>((size_t)C * p);
+    L.theta = ctx->dalloc<float>(MLP_NPAR);
+    L.grad = ctx->dalloc<float>(MLP_NPAR);
+    L.adam_m = ctx->dalloc<float>(MLP_NPAR);
+    L.adam_v = ctx->dalloc<float>(MLP_NPAR);
+    L.w1b = ctx->dalloc<uint16_t>(MLP_H * MLP_F);
+    L.w2b = ctx->dalloc<uint16_t>(MLP_H * MLP_H);
+    ctx->adam_t = ctx->dalloc<int32_t>(1);
+    // the scans keep the per-SNP log odds, the first feature
+    if (!ctx->lml_buf) ctx->lml_buf = ctx->dalloc<double>((size_t)C * p);
+    K.p_lml = ctx->lml_buf;
+    CK(bmg_mlp_init(&K, ctx->adam_t, ctx->stream));
+  }
   K.model_inds = ctx->dalloc<int32_t>(pc, false);
   CK(cudaMemsetAsync(K.model_inds, 0xff, 4 * pc, ctx->stream));
   K.n_pad = ctx->n_pad;
@@ -1014,16 +1054,24 @@ static void drain_traces(bmg_ctx* ctx, uint64_t iter0, const bmg_trace_sink* sin
   }
 }
 
-static std::vector<Segment> plan_chunk(uint64_t first_iter, uint64_t chunk, uint64_t n_rao)
+// learned: the RB step with this index (from 0) refreshes the MLP part when
+// the proposal still adapts and the index is a multiple of `every`
+static std::vector<Segment> plan_chunk(uint64_t first_iter, uint64_t chunk, uint64_t n_rao, uint64_t rb0,
+                                       bool learned, uint64_t adapt_rb, bool always, uint64_t every)
 {
   std::vector<Segment> segs;
-  uint64_t t = first_iter, i = 0;
+  uint64_t t = first_iter, i = 0, rb = rb0;
   while (i < chunk) {
     const uint64_t next_rb = ((t / n_rao) + 1) * n_rao - 1;  // first iter >= t with (iter+1) % n_rao == 0
     const uint64_t seg = std::min<uint64_t>(chunk - i, next_rb - t + 1);
     t += seg;
     i += seg;
-    segs.push_back({seg, t - 1 == next_rb});
+    const bool is_rb = t - 1 == next_rb;
+    // the adaptive proposal's last adaptation is RB step adapt_rb - 2
+    // (src/sampler.cpp:739-760); the MLP part follows the same rule
+    const bool refresh = learned && is_rb && (always || rb + 1 < adapt_rb) && rb % every == 0;
+    segs.push_back({seg, is_rb, refresh});
+    if (is_rb) ++rb;
   }
   return segs;
 }
@@ -1046,6 +1094,15 @@ static void issue_chunk(bmg_ctx* ctx, const std::vector<Segment>& segs)
       launch_scan(ctx);
       CK(cudaEventRecordWithFlags(ev[2], ctx->stream, rec));
       launch_rebuild(ctx, 0);
+      if (segs[q].refresh) {
+        CK(bmg_mlp_refresh(&K, ctx->km, (int)ctx->opt.learned_steps, (float)ctx->opt.learned_lr, ctx->adam_t,
+                           ctx->stream));
+        // LD feature, per step training + Adam + counter, forward pass, tables
+        const uint64_t n = 4 + 3ull * ctx->opt.learned_steps;
+        if (ctx->capturing) ctx->graph_launches += n;
+        else ctx->n_launches += n;
+        if (ctx->sync_check) CK(cudaStreamSynchronize(ctx->stream));
+      }
       CK(cudaEventRecordWithFlags(ev[3], ctx->stream, rec));
     }
   }
@@ -1068,7 +1125,9 @@ extern "C" bmg_status bmg_run(bmg_ctx* ctx, uint64_t n_iter, const bmg_trace_sin
   while (done < n_iter) {
     const uint64_t chunk = std::min<uint64_t>(n_iter - done, gi);
     const uint64_t iter0 = ctx->n_iter;
-    const std::vector<Segment> segs = plan_chunk(iter0, chunk, n_rao);
+    const std::vector<Segment> segs =
+        plan_chunk(iter0, chunk, n_rao, ctx->rb_steps, ctx->K.lrn.on != 0, ctx->opt.n_rao_burnin,
+                   ctx->opt.adaptation != 0, ctx->opt.learned_every ? ctx->opt.learned_every : 1);
     while (ctx->seg_ev.size() < 4 * segs.size()) {
       cudaEvent_t e;
       CK(cudaEventCreate(&e));
@@ -1123,6 +1182,7 @@ extern "C" bmg_status bmg_run(bmg_ctx* ctx, uint64_t n_iter, const bmg_trace_sin
         ctx->n_scans++;
       }
       ctx->n_iter += segs[q].iters;
+      if (segs[q].rb) ++ctx->rb_steps;
     }
     drain_traces(ctx, iter0, sink);
     device_error_check(ctx);
@@ -1166,16 +1226,17 @@ extern "C" bmg_status bmg_scan_logodds(bmg_ctx* ctx, double* logodds)
   DevConst& K = ctx->K;
   const size_t pc = (size_t)ctx->p * ctx->C;
   if (!ctx->lml_buf) ctx->lml_buf = ctx->dalloc<double>(pc, false);
+  double* const before = K.p_lml;
   K.p_lml = ctx->lml_buf;
   try {
     bmg_rbprep_kernel<<<ctx->C, BMG_MOVE_THREADS, ctx->move_smem, ctx->stream>>>(K);
     LAUNCHED(ctx, "bmg_rbprep_kernel");
     launch_scan(ctx);
   } catch (...) {
-    K.p_lml = nullptr;
+    K.p_lml = before;
     throw;
   }
-  K.p_lml = nullptr;
+  K.p_lml = before;
   CK(cudaMemcpyAsync(logodds, ctx->lml_buf, 8 * pc, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   device_error_check(ctx);
@@ -1206,6 +1267,56 @@ extern "C" bmg_status bmg_scan_schur(bmg_ctx* ctx, double* dlml)
   CK(cudaMemcpyAsync(dlml, ctx->schur_out, 8 * out_n, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   device_error_check(ctx);
+  return BMG_OK;
+  API_END
+}
+
+extern "C" bmg_status bmg_learned_snapshot(bmg_ctx* ctx, float* theta, float* logit, float* features,
+                                           uint32_t* t_snp, double* t_s, uint32_t* t_n)
+{
+  if (!ctx) return BMG_EINVAL;
+  API_BEGIN
+  check_ready(ctx);
+  const DevLearned& L = ctx->K.lrn;
+  if (!L.on) throw bmg_error(BMG_EINVAL, "the learned proposal is not on");
+  const size_t pc = (size_t)ctx->p * ctx->C;
+  // logits of the current parameters at the current state (the candidate
+  // tables are left as the last refresh made them)
+  if (logit) CK(bmg_mlp_forward(&ctx->K, ctx->stream));
+  if (theta) CK(cudaMemcpyAsync(theta, L.theta, sizeof(float) * MLP_NPAR, cudaMemcpyDeviceToHost, ctx->stream));
+  if (logit) CK(cudaMemcpyAsync(logit, L.logit, sizeof(float) * pc, cudaMemcpyDeviceToHost, ctx->stream));
+  if (t_snp) CK(cudaMemcpyAsync(t_snp, L.t_snp, 4 * (size_t)ctx->C * L.topk, cudaMemcpyDeviceToHost, ctx->stream));
+  if (t_s) CK(cudaMemcpyAsync(t_s, L.t_s, 8 * (size_t)ctx->C * L.topk, cudaMemcpyDeviceToHost, ctx->stream));
+  if (t_n) CK(cudaMemcpyAsync(t_n, L.t_n, 4 * (size_t)ctx->C, cudaMemcpyDeviceToHost, ctx->stream));
+  if (features) {
+    float* d = nullptr;
+    CK(cudaMallocAsync(&d, sizeof(float) * pc * MLP_F, ctx->stream));
+    cudaError_t e = bmg_mlp_features(&ctx->K, d, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(features, d, sizeof(float) * pc * MLP_F, cudaMemcpyDeviceToHost, ctx->stream);
+    cudaFreeAsync(d, ctx->stream);
+    CK(e);
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  return BMG_OK;
+  API_END
+}
+
+extern "C" bmg_status bmg_learned_grad(bmg_ctx* ctx, const uint32_t* rows, uint32_t n_rows, float* grad)
+{
+  if (!ctx || !rows || !grad || n_rows == 0) return BMG_EINVAL;
+  API_BEGIN
+  check_ready(ctx);
+  if (!ctx->K.lrn.on) throw bmg_error(BMG_EINVAL, "the learned proposal is not on");
+  uint32_t* d = nullptr;
+  CK(cudaMallocAsync(&d, 8 * (size_t)n_rows, ctx->stream));
+  cudaError_t e = cudaMemcpyAsync(d, rows, 8 * (size_t)n_rows, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) e = bmg_mlp_grad(&ctx->K, ctx->adam_t, d, n_rows, ctx->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(grad, ctx->K.lrn.grad, sizeof(float) * MLP_NPAR, cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ctx->K.lrn.grad, 0, sizeof(float) * MLP_NPAR, ctx->stream);
+  cudaFreeAsync(d, ctx->stream);
+  CK(e);
+  CK(cudaStreamSynchronize(ctx->stream));
   return BMG_OK;
   API_END
 }

@@ -45,6 +45,7 @@ struct MoveShared {
   double tv[2][SMK];    // work vectors for beta and its mean
   double cs[SMK], sn[SMK];  // Givens rotations of a downdate
   int l_smem[2];        // factor and v of model i are in shared memory
+  long long w_m;        // learned proposal: weight of the candidates outside the zero set (x 2^40)
   uint32_t move_inds[BMG_MAX_MS + 1];
   uint32_t move_add[BMG_MAX_MS + 1];
   uint32_t move_rem[BMG_MAX_MS + 1];
@@ -904,6 +905,11 @@ struct Warp {
     bool in_list = pend_find(snp, &at);
     bool zeroed = base_zero(snp) != in_list;
     if (zeroed == zero) return;
+    if (K.lrn.on) {
+      const long long wm = mlp_wint(snp);
+      __syncwarp();
+      if (lane == 0) s.w_m += zero ? -wm : wm;
+    }
     if (in_list) {
       int last = s.n_pend - 1;
       __syncwarp();
@@ -934,6 +940,70 @@ struct Warp {
     return ch->cadd_total + warp_sum_ll(t);
   }
   __device__ double add_total() { return (double)add_total_int() * ldexp(1.0, -K.qs); }
+
+  // ---- learned part of the add proposal: candidate weights in fixed point
+  // (x 2^40, exact sums), zero for SNPs outside the chain's candidate table
+  __device__ long long mlp_wint(uint32_t snp) const
+  {
+    const uint32_t T = K.lrn.topk, n = K.lrn.t_n[c];
+    const uint32_t* ts = K.lrn.t_snp + (size_t)c * T;
+    uint32_t lo = 0, hi = n;
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (ts[mid] < snp) lo = mid + 1;
+      else hi = mid;
+    }
+    return (lo < n && ts[lo] == snp) ? __double2ll_rn(K.lrn.t_s[(size_t)c * T + lo] * 0x1p40) : 0ll;
+  }
+  // at a launch's start the zero set is the current model
+  __device__ void mlp_init_total()
+  {
+    const uint32_t T = K.lrn.topk, n = K.lrn.t_n[c];
+    long long w = 0;
+    for (uint32_t i = lane; i < n; i += 32) w += __double2ll_rn(K.lrn.t_s[(size_t)c * T + i] * 0x1p40);
+    w = warp_sum_ll(w);
+    for (int i = 0; i < cur->k; ++i) w -= mlp_wint(cur->loci[i]);
+    __syncwarp();
+    if (lane == 0) s.w_m = w;
+    __syncwarp();
+  }
+  __device__ bool pend_has(uint32_t snp) const
+  {
+    for (int i = 0; i < s.n_pend; ++i)
+      if (s.pend_snp[i] == (int)snp) return true;
+    return false;
+  }
+  // a candidate outside the zero set, with probability proportional to its weight
+  __device__ uint32_t mlp_sample(long long wm)
+  {
+    long long target = (long long)floor(u01() * (double)wm);
+    if (target >= wm) target = wm - 1;
+    const uint32_t T = K.lrn.topk, n = K.lrn.t_n[c];
+    const uint32_t* ts = K.lrn.t_snp + (size_t)c * T;
+    const uint32_t per = (n + 31) / 32, i0 = min(n, lane * per), i1 = min(n, i0 + per);
+    long long mine = 0;
+    for (uint32_t i = i0; i < i1; ++i)
+      if (base_zero(ts[i]) == pend_has(ts[i])) mine += __double2ll_rn(K.lrn.t_s[(size_t)c * T + i] * 0x1p40);
+    long long incl = mine;
+    for (int o = 1; o < 32; o <<= 1) {
+      const long long v = __shfl_up_sync(FULL_MASK, incl, o);
+      if (lane >= o) incl += v;
+    }
+    const unsigned hit = __ballot_sync(FULL_MASK, incl > target);
+    const int src = hit ? __ffs(hit) - 1 : 31;
+    uint32_t pick = 0xFFFFFFFFu, last = 0xFFFFFFFFu;
+    if (lane == src) {
+      long long run = incl - mine;
+      for (uint32_t i = i0; i < i1; ++i) {
+        if (base_zero(ts[i]) != pend_has(ts[i])) continue;
+        last = ts[i];
+        run += __double2ll_rn(K.lrn.t_s[(size_t)c * T + i] * 0x1p40);
+        if (run > target) { pick = ts[i]; break; }
+      }
+      if (pick == 0xFFFFFFFFu) pick = last;
+    }
+    return __shfl_sync(FULL_MASK, pick, src);
+  }
 
   // C'(q): weight of in-order positions < q after the pending flips
   __device__ long long cum_at(long long q) const
@@ -1098,8 +1168,19 @@ struct Warp {
       if (add) {
         --max_adds;
         double tot = add_total();
-        ind = add_sample();
-        lqf += log(qadd(ind)) - log(tot);
+        if (K.lrn.on) {
+          // mixture of the adaptive proposal and the learned candidates
+          const long long wm = s.w_m;
+          const double eps = wm > 0 ? K.lrn.mix : 0.0;
+          const bool learned = eps > 0 && u01() < eps;
+          ind = learned ? mlp_sample(wm) : add_sample();
+          double q = (1.0 - eps) * qadd(ind) / tot;
+          if (eps > 0) q += eps * (double)mlp_wint(ind) / (double)wm;
+          lqf += log(q);
+        } else {
+          ind = add_sample();
+          lqf += log(qadd(ind)) - log(tot);
+        }
         add_set_zero(ind, true);
         if (lane == 0) { s.move_isadd[i] = 1; s.move_inds[i] = ind; s.move_map[i] = ind; }
       } else {
@@ -1161,6 +1242,7 @@ struct Warp {
   {
     long long max_adds = (long long)K.p - nm->k, max_rems = nm->k;
     double w_add = add_total(), w_rem = rs_total();
+    long long wmb = s.w_m;
     int last_rem = ms - 1;
     for (int i = 0; i < ms; ++i) {
       if (max_adds > 0 && max_rems > 0) lqb += LOG_HALF_D;
@@ -1177,7 +1259,16 @@ struct Warp {
         --max_adds;
         ind = (uint32_t)s.move_map[i];
         double q = qadd(ind);
-        lqb += log(q) - log(w_add);
+        if (K.lrn.on) {
+          const double eps = wmb > 0 ? K.lrn.mix : 0.0;
+          const long long wi = mlp_wint(ind);
+          double qm = (1.0 - eps) * q / w_add;
+          if (eps > 0) qm += eps * (double)wi / (double)wmb;
+          lqb += log(qm);
+          wmb -= wi;
+        } else {
+          lqb += log(q) - log(w_add);
+        }
         w_add -= q;
       }
     }
@@ -1319,7 +1410,11 @@ struct Warp {
     int ms = sample_naive(K.q_nbc + (size_t)c * 256, (int)mms) + 1;
     if (lane == 0) ch->movesize = ms;
     __syncwarp();
-    long long nbh = min((long long)K.max_nbh, (long long)K.p / 2);
+    // the reference takes min(max_nbh, m_g / 2); when 2 nbh + 1 exceeds m_g
+    // its wrapped index goes below zero (a size_t out-of-bounds read, UB), so
+    // the window is capped at (m_g - 1) / 2 each side, which changes nothing
+    // for m_g > 2 max_nbh
+    long long nbh = min((long long)K.max_nbh, ((long long)K.p - 1) / 2);
     int mic = (int)floor(u01() * nm->k);
     long long ind_c = nm->loci[mic];
     // the permutation of 2*nbh neighbours is kept in move_map
@@ -1889,6 +1984,7 @@ bmg_move_kernel(DevConst K, int max_iters)
 
   // warp 0 keeps the sampler context (and its random stream) in registers
   Warp W(K, c, s);
+  if (K.lrn.on && tid < 32) W.mlp_init_total();
   double* cs_buf = K.scratch + (size_t)c * 2 * K.km;
   double* sn_buf = cs_buf + K.km;
 

@@ -142,6 +142,38 @@ struct DevTrace {
 };
 
 // Read-only context constants.
+// The learned part of the add proposal (no reference counterpart): a
+// 16 -> 128 -> 128 -> 1 MLP shared by the chains, its per-chain candidate
+// tables and the buffers of its features.  FP32 master parameters in one
+// array (W1 128x16, b1, W2 128x128, b2, w3, b3), bf16 copies of W1 and W2 for
+// the tensor-core forward pass.
+#define MLP_F 16
+#define MLP_H 128
+#define MLP_OW1 0
+#define MLP_OB1 (MLP_OW1 + MLP_H * MLP_F)
+#define MLP_OW2 (MLP_OB1 + MLP_H)
+#define MLP_OB2 (MLP_OW2 + MLP_H * MLP_H)
+#define MLP_OW3 (MLP_OB2 + MLP_H)
+#define MLP_OB3 (MLP_OW3 + MLP_H)
+#define MLP_NPAR (MLP_OB3 + 1)
+struct DevLearned {
+  int on;               // BMG_PROPOSAL_LEARNED
+  double mix;           // weight of the MLP part
+  uint32_t topk;        // candidate table size per chain
+  uint32_t* t_snp;      // chains x topk: candidates in ascending SNP order
+  double* t_s;          // chains x topk: their weights (predicted inclusion probability)
+  double* t_sum;        // chains: sum of the weights
+  uint32_t* t_n;        // chains: candidates in the table
+  float* maxcorr;       // chains x p: max |corr| to the model's SNPs within the LD window
+  float* logit;         // chains x p: MLP output of the last refresh
+  float* theta;         // MLP_NPAR parameters
+  float* grad;          // MLP_NPAR gradient accumulator
+  float* adam_m;
+  float* adam_v;
+  uint16_t* w1b;        // bf16 W1 (128 x 16)
+  uint16_t* w2b;        // bf16 W2 (128 x 128)
+};
+
 struct DevConst {
   // sizes
   uint64_t n;           // individuals
@@ -236,6 +268,7 @@ struct DevConst {
   int64_t* cadd;        // chains x (p + 1) prefix of dd_add weights (x 2^qs) in in-order
   uint32_t* inbits;     // chains x ceil(p/32): SNP in current model
   uint32_t* basebits;   // chains x ceil(p/32): zeroed in the cadd base
+  DevLearned lrn;
   double* p_lml;        // chains x p: log posterior odds of inclusion of the last scan, when requested (else null)
   int64_t* tile_sums;   // chains x ceil(p / BMG_REBUILD_TILE): rebuild pass 1
   int32_t* rebuild_active;  // chains: this rebuild covers the chain

@@ -232,6 +232,8 @@ static void copy_path(char* dst, const std::string& src)
 
 using namespace bmg_host;
 
+extern "C" size_t bmg_options_size(void) { return sizeof(bmg_options); }
+
 extern "C" bmg_status bmg_options_default(bmg_options* o)
 {
   if (!o) return BMG_EINVAL;
@@ -258,6 +260,11 @@ extern "C" bmg_status bmg_options_default(bmg_options* o)
   o->graph_iters = 64;
   o->write_files = 0;
   o->quiet = 0;
+  o->learned_mix = 0.3;
+  o->learned_topk = 1024;
+  o->learned_every = 10;
+  o->learned_steps = 4;
+  o->learned_lr = 1e-3;
   return BMG_OK;
 }
 

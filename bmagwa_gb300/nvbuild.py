@@ -20,7 +20,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 INC = ["-I" + os.path.join(ROOT, "include"), "-I" + CSRC, "-I" + os.path.join(CSRC, "dev")]
 
 CU = ["bmg_api.cu", "dev/sampler.cu", "dev/scan.cu", "dev/prep.cu", "dev/scan_tc.cu", "dev/schur_tc.cu",
-      "dev/noalloc.cu"]
+      "dev/learned.cu", "dev/noalloc.cu"]
 CPP = ["host/options.cpp", "host/plink.cpp"]
 
 

@@ -115,6 +115,12 @@ typedef struct bmg_options {
   uint32_t graph_iters;     /* iterations captured per CUDA graph chunk */
   int32_t write_files;      /* 1: bmg_run writes the reference's trace files */
   int32_t quiet;            /* 1: no console warnings */
+  /* learned proposal (BMG_PROPOSAL_LEARNED; no reference counterpart) */
+  double learned_mix;       /* weight of the MLP part of the add proposal (default 0.3) */
+  uint32_t learned_topk;    /* candidate SNPs per chain of the MLP part (default 1024) */
+  uint32_t learned_every;   /* RB steps between MLP refreshes during burn-in (default 10) */
+  uint32_t learned_steps;   /* optimiser steps per refresh (default 4) */
+  double learned_lr;        /* Adam step size (default 1e-3) */
 } bmg_options;
 
 /* Trace of a chain over a run chunk, in the reference's file layouts
@@ -148,6 +154,10 @@ typedef struct bmg_trace_sink {
 } bmg_trace_sink;
 
 typedef struct bmg_ctx bmg_ctx;
+
+/* sizeof(bmg_options) as compiled into the library, for bindings that mirror
+ * the struct (no reference counterpart). */
+size_t bmg_options_size(void);
 
 /* Reference defaults of every optional key (src/options.hpp:138-321). */
 bmg_status bmg_options_default(bmg_options* opt);
@@ -221,6 +231,21 @@ bmg_status bmg_scan_logodds(bmg_ctx* ctx, double* logodds);
  * of a term is the chain's shared tau2 value.  Models of more than 128
  * columns return BMG_EUNSUPPORTED. */
 bmg_status bmg_scan_schur(bmg_ctx* ctx, double* dlml);
+
+/* Learned proposal (BMG_PROPOSAL_LEARNED; no reference counterpart).
+ * Snapshot: the MLP's MLP_NPAR = 18817 FP32 parameters (W1 128x16, b1 128,
+ * W2 128x128, b2 128, w3 128, b3), its logits at the current state
+ * (chains x m_g), the features of the current state (chains x m_g x 16), and
+ * the candidate tables (chains x topk SNPs and weights, chains counts); any
+ * pointer may be NULL. */
+bmg_status bmg_learned_snapshot(bmg_ctx* ctx, float* theta, float* logit, float* features, uint32_t* t_snp,
+                                double* t_s, uint32_t* t_n);
+
+/* The gradient of the training loss (mean binary cross-entropy of the MLP's
+ * output against the chain's p_proposal) over an explicit list of rows
+ * (n_rows pairs chain, SNP) at the current parameters, written to grad
+ * (18817 floats); the parameters do not change. */
+bmg_status bmg_learned_grad(bmg_ctx* ctx, const uint32_t* rows, uint32_t n_rows, float* grad);
 
 /* Advance every chain by n_iter MCMC iterations (replaces the main loop of
  * Sampler::sample, src/sampler.cpp:626-834).  Traces go to `sink` (may be

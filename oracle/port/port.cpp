@@ -1674,7 +1674,9 @@ struct Sampler {
   {
     size_t mms = std::min(max_nbh * 2, std::min(m_g - 1, (size_t)max_move_size));
     movesize = (unsigned char)(sample_discrete_naive(q_p_move_size_nbc.data(), (int)mms, rng) + 1);
-    size_t nbh = std::min(max_nbh, m_g / 2);
+    // src/sampler.hpp:1441 takes min(max_nbh, m_g / 2), which wraps below
+    // index 0 (UB) when 2 nbh + 1 > m_g; capped at (m_g - 1) / 2 as on the GPU
+    size_t nbh = std::min(max_nbh, (m_g - 1) / 2);
     size_t mic = (size_t)std::floor(rng.rand_01() * nm->size());
     size_t ind_c = nm->loci[mic];
     std::vector<size_t> perm(2 * nbh);

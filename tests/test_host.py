@@ -212,3 +212,12 @@ def test_create_rejects_unsupported_options_before_touching_the_device(tmp_path)
         L.bmg_status_string.restype = C.c_char_p
         assert L.bmg_status_string(rc).decode() == status, field
         setattr(o, field, old)
+
+
+def test_options_struct_matches_the_library():
+    L = bg.lib()
+    L.bmg_options_size.restype = C.c_size_t
+    from bmagwa_gb300 import abi
+    assert L.bmg_options_size() == C.sizeof(abi.Options)
+    o = bg.default_options()
+    assert o.learned_topk == 1024 and o.learned_mix == pytest.approx(0.3)
