@@ -33,6 +33,9 @@ WORKLOADS = {
     "scan": dict(n=10000, p=500000, chains=32, n_rao=1, ld_block=50, causal=30, types="A"),
     "batched": dict(n=5000, p=50000, chains=8, n_rao=500, ld_block=50, causal=20, types="A,AH"),
     "plain": dict(n=1000, p=5000, chains=1, n_rao=500, ld_block=0, causal=10, types="A"),
+    # the learned proposal against the plain adaptive one (inclusion ESS/s)
+    "learned": dict(n=10000, p=200000, chains=16, n_rao=1, ld_block=100, causal=50, types="A,AH", dominance=10,
+                    burnin=600, sample=1500),
 }
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM = 6800.0
@@ -73,7 +76,7 @@ def options(bg, wl, seed0, iters):
 def make_data(wl, seed, device):
     from bmagwa_gb300 import synth
     counts, _ = synth.genotypes(wl["n"], wl["p"], wl["ld_block"], seed, device=device)
-    y, _, _ = synth.phenotype(counts, wl["causal"], 0.2, 0, seed, device=device)
+    y, _, _ = synth.phenotype(counts, wl["causal"], 0.2, wl.get("dominance", 0), seed, device=device)
     packed = synth.pack(counts).cpu().numpy().reshape(-1)
     del counts
     return packed, y
@@ -286,6 +289,50 @@ def run_gb300(args, wl):
         dist.destroy_process_group()
 
 
+def run_learned_compare(args, wl):
+    """Inclusion-indicator ESS per second of the sampling phase (after the
+    same burn-in) with the plain adaptive add proposal and with the learned
+    mixture; one JSON line with both."""
+    import torch
+    import bmagwa_gb300 as bg
+    from bmagwa_gb300 import ess
+    torch.cuda.set_device(0)
+    bg.build()
+    seed = 11
+    packed, y = make_data(wl, seed, "cuda")
+    burn, samp = wl["burnin"], wl["sample"]
+    out = {}
+    for name, mode in (("plain", 0), ("learned", 1)):
+        o = options(bg, wl, seed, burn + samp)
+        o.n_rao_burnin = burn // wl["n_rao"]
+        o.proposal = mode
+        ctx = bg.Context(o)
+        ctx.load_bed(packed)
+        ctx.set_phenotypes(y)
+        ctx.set_covariates(None)
+        ctx.precompute()
+        ctx.run(burn, collect=False)
+        torch.cuda.synchronize()
+        ctx.reset_timings()
+        col = ctx.run(samp, collect=True)
+        sec = ctx.timings()[3] / 1000.0
+        chains = [col.chain(c) for c in range(wl["chains"])]
+        e = ess.summarize([(t["modelsize"], t["loci"]) for t in chains], sec)
+        acc = [ctx.state(c)[0].n_accepted / max(1, ctx.state(c)[0].n_iter) for c in range(wl["chains"])]
+        out[name] = dict(e, iter_per_s=samp * wl["chains"] / sec, seconds=sec,
+                         mean_model_size=float(np.mean([len(t["loci"]) / max(1, len(t["modelsize"])) for t in chains])),
+                         acceptance=float(np.mean(acc)))
+        ctx.close()
+    ratio = (out["learned"]["per_s"] / out["plain"]["per_s"]) if out["plain"]["per_s"] else None
+    print(json.dumps({"metric": "inclusion-indicator ESS/s, learned vs plain adaptive add proposal",
+                      "value": ratio, "unit": "ratio", "n_gpus": 1, "higher_is_better": True,
+                      "data": "synthetic (seeded LD-block genotypes, 50 causal SNPs, 10 in dominance coding)",
+                      "config": {"workload": "learned", "n": wl["n"], "p": wl["p"], "chains": wl["chains"],
+                                 "types": wl["types"], "n_rao": wl["n_rao"], "burnin_iters": burn,
+                                 "sample_iters": samp},
+                      "plain": out["plain"], "learned": out["learned"]}))
+
+
 def run_reference(args, wl):
     rank, world, _ = env_rank()
     if rank != 0:
@@ -348,6 +395,8 @@ def main():
             wl[key] = getattr(args, key)
     if args.impl == "reference":
         run_reference(args, wl)
+    elif args.workload == "learned":
+        run_learned_compare(args, wl)
     else:
         run_gb300(args, wl)
 
