@@ -8,6 +8,7 @@
 // is the same for every chain, so it is known on the host; the launches of a
 // chunk are captured once in a CUDA graph and replayed.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -29,6 +30,10 @@
 extern "C" __global__ void bmg_prep_kernel(uint8_t* geno, uint64_t n, uint64_t p, uint32_t gs,
                                            int recode, int32_t* cnt, int32_t* missing);
 extern "C" __global__ void bmg_trace_reset_kernel(DevChain* ch, int n_chains);
+extern "C" __global__ void bmg_mask_counts_kernel(const uint8_t* geno, uint32_t gs, uint64_t p, const uint64_t* mask2,
+                                                  uint32_t n_samples, int32_t* cnt);
+extern "C" __global__ void bmg_pre_kernel(const int32_t* cnt, uint64_t p, uint32_t n_samples, const double* n_of,
+                                          int allow_mask, int ah, int offset, double* pre);
 extern "C" __global__ void bmg_gsum_kernel(const uint8_t* geno, uint64_t n, uint64_t p, uint32_t gs,
                                            const int64_t* yint, const int64_t* eint, uint32_t nv, int64_t* gsum);
 extern "C" __global__ void bmg_init_kernel(DevConst K);
@@ -104,6 +109,14 @@ struct bmg_ctx {
   std::vector<int32_t> cnt_h;
   std::vector<double> y_h, e_h, pre_h;
   double var_x = 0, mean_x = 0, var_y = 0, yy = 0;
+  // several phenotypes (one chain each): per sample the individuals, values
+  // (zero outside), and sums; record k of K.ph is built from these
+  bool multi = false;
+  std::vector<uint8_t> ph_mask;        // n_pheno x n: 1 = in the sample
+  std::vector<double> ph_n, ph_yy, ph_var_y, ph_amax, ph_ysum;
+  std::vector<int32_t> ph_sy;
+  double* ph_y_dev = nullptr;          // n_pheno x n
+  int64_t* ph_yint_dev = nullptr;      // n_pheno x n
   double g_a = 0, g_b = 0, s2_sigma2 = 0, s2_tau2[4] = {0, 0, 0, 0};
   std::vector<void*> allocs;
   DevConst K;
@@ -400,10 +413,69 @@ extern "C" bmg_status bmg_set_phenotypes(bmg_ctx* ctx, const double* y, const ui
 {
   if (!ctx) return BMG_EINVAL;
   API_BEGIN
-  if (!y) throw bmg_error(BMG_EINVAL, "null phenotypes");
-  if (n_pheno != 1 || mask)
-    throw bmg_error(BMG_EUNSUPPORTED, "one phenotype without mask per context on this path");
+  if (!y || n_pheno == 0) throw bmg_error(BMG_EINVAL, "null phenotypes");
   const uint64_t n = ctx->n;
+  if (n_pheno > 1 || mask) {
+    // one chain per phenotype, each fitted to the individuals its mask keeps
+    // (the reference runs one process per phenotype on a subset .bed)
+    if (n_pheno != ctx->C)
+      throw bmg_error(BMG_EUNSUPPORTED, "several phenotypes need one chain per phenotype (n_threads = phenotypes)");
+    if (ctx->opt.m_e != 0) throw bmg_error(BMG_EUNSUPPORTED, "covariates are not supported with several phenotypes");
+    if (ctx->opt.recode_g_to_minor_allele_count)
+      throw bmg_error(BMG_EUNSUPPORTED, "the minor-allele recode would differ per sample; recode the .bed first");
+    ctx->multi = true;
+    ctx->ph_mask.assign((size_t)n_pheno * n, 1);
+    if (mask)
+      for (size_t q = 0; q < (size_t)n_pheno * n; ++q) ctx->ph_mask[q] = mask[q] ? 1 : 0;
+    const uint32_t P = n_pheno;
+    ctx->ph_n.assign(P, 0);
+    ctx->ph_yy.assign(P, 0);
+    ctx->ph_var_y.assign(P, 0);
+    ctx->ph_amax.assign(P, 0);
+    ctx->ph_ysum.assign(P, 0);
+    ctx->ph_sy.assign(P, 0);
+    std::vector<double> yall((size_t)P * n, 0.0);
+    std::vector<int64_t> yint((size_t)P * n, 0);
+    for (uint32_t k = 0; k < P; ++k) {
+      const double* yk = y + (size_t)k * n;
+      const uint8_t* mk = &ctx->ph_mask[(size_t)k * n];
+      double cnt = 0, yy = 0, s = 0, amax = 0;
+      for (uint64_t i = 0; i < n; ++i) {
+        if (!mk[i]) continue;
+        if (!std::isfinite(yk[i])) throw bmg_error(BMG_EINVAL, "non-finite phenotype");
+        cnt += 1;
+        yy += yk[i] * yk[i];
+        s += yk[i];
+        amax = std::max(amax, std::fabs(yk[i]));
+        yall[(size_t)k * n + i] = yk[i];
+      }
+      if (cnt < 2) throw bmg_error(BMG_EINVAL, "a sample needs at least two individuals");
+      ctx->ph_n[k] = cnt;
+      ctx->ph_yy[k] = yy;
+      ctx->ph_var_y[k] = (yy - s * s / cnt) / (cnt - 1);
+      ctx->ph_amax[k] = amax;
+      ctx->ph_ysum[k] = s;
+      const int sy = fixed_exponent(amax, (uint64_t)cnt);
+      ctx->ph_sy[k] = sy;
+      for (uint64_t i = 0; i < n; ++i)
+        if (mk[i]) yint[(size_t)k * n + i] = (int64_t)std::llrint(std::ldexp(yk[i], sy));
+    }
+    ctx->ph_y_dev = ctx->dalloc<double>((size_t)P * n, false);
+    ctx->ph_yint_dev = ctx->dalloc<int64_t>((size_t)P * n, false);
+    CK(cudaMemcpyAsync(ctx->ph_y_dev, yall.data(), 8 * yall.size(), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->ph_yint_dev, yint.data(), 8 * yint.size(), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    // the single-sample fields hold sample 0 (read by what reports one sample)
+    ctx->y_h.assign(yall.begin(), yall.begin() + n);
+    ctx->yy = ctx->ph_yy[0];
+    ctx->var_y = ctx->ph_var_y[0];
+    ctx->K.y = ctx->ph_y_dev;
+    ctx->K.yint = ctx->ph_yint_dev;
+    ctx->K.sy = ctx->ph_sy[0];
+    ctx->K.y_absmax = ctx->ph_amax[0];
+    ctx->have_y = true;
+    return BMG_OK;
+  }
   ctx->y_h.assign(y, y + n);
   double yy = 0, sq = 0, s = 0, amax = 0;
   for (uint64_t i = 0; i < n; ++i) {
@@ -648,6 +720,124 @@ extern "C" bmg_status bmg_precompute(bmg_ctx* ctx)
   K.n_plus_nu = (double)n + o.nu_sigma2;
   K.minus_n_plus_nu_2 = -0.5 * K.n_plus_nu;
   K.nus2_plus_yy = o.nu_sigma2 * s2s + ctx->yy;
+  // the samples the chains are fitted to: one record for all chains, or one
+  // per phenotype; per chain the covariate block and the initial precisions
+  std::vector<DevPheno> recs;
+  std::vector<uint32_t> pheno_of(C, 0);
+  std::vector<double> chain_ee0(C, ee[0]), chain_ey0(C, ey[0]);
+  std::vector<std::array<double, 4>> chain_inv0(C);
+  for (uint32_t c = 0; c < C; ++c)
+    for (int t = 0; t < 4; ++t) chain_inv0[c][t] = inv0[t];
+  if (!ctx->multi) {
+    DevPheno r;
+    std::memset(&r, 0, sizeof(r));
+    r.n = (double)n;
+    r.n_plus_nu = K.n_plus_nu;
+    r.minus_n_plus_nu_2 = K.minus_n_plus_nu_2;
+    r.nus2_plus_yy = K.nus2_plus_yy;
+    r.rng_nu = (double)n + o.nu_sigma2;
+    for (int t = 0; t < 4; ++t) r.nus2_tau2[t] = K.nus2_tau2[t];
+    r.y_absmax = K.y_absmax;
+    r.sy = K.sy;
+    r.y = K.y;
+    r.yint = K.yint;
+    r.mask2 = nullptr;
+    r.cnt = K.cnt;
+    r.pre = K.pre;
+    r.gsum = K.gsum;
+    recs.push_back(r);
+  } else {
+    const uint32_t P = C;
+    const size_t nw64 = ctx->gs / 8;
+    std::vector<uint64_t> m2((size_t)P * nw64, 0);
+    for (uint32_t k = 0; k < P; ++k)
+      for (uint64_t i = 0; i < n; ++i)
+        if (ctx->ph_mask[(size_t)k * n + i]) m2[(size_t)k * nw64 + (i >> 5)] |= 1ull << (2 * (i & 31));
+    uint64_t* dm2 = ctx->dalloc<uint64_t>(m2.size(), false);
+    int32_t* dcnt = ctx->dalloc<int32_t>((size_t)P * p * 2, false);
+    double* dpre = ctx->dalloc<double>((size_t)P * p * offset, false);
+    double* dn = ctx->dalloc<double>(P, false);
+    CK(cudaMemcpyAsync(dm2, m2.data(), 8 * m2.size(), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(dn, ctx->ph_n.data(), 8 * P, cudaMemcpyHostToDevice, ctx->stream));
+    const uint64_t warps = (uint64_t)P * p;
+    bmg_mask_counts_kernel<<<(unsigned)std::min<uint64_t>((warps + 7) / 8, 152 * 16), 256, 0, ctx->stream>>>(
+        K.geno, ctx->gs, p, dm2, P, dcnt);
+    LAUNCHED(ctx, "bmg_mask_counts_kernel");
+    int amask = 0;
+    for (int t = 0; t < 4; ++t) amask |= allow_terms[t] ? (1 << t) : 0;
+    bmg_pre_kernel<<<1024, 256, 0, ctx->stream>>>(dcnt, p, P, dn, amask, ah ? 1 : 0, offset, dpre);
+    LAUNCHED(ctx, "bmg_pre_kernel");
+    // var_x and mean_x of a sample (src/data.cpp:403-434) enter only where the
+    // term precision's scale comes from eh_tau2
+    bool need_x = false;
+    for (int t = 0; t < 4; ++t) need_x = need_x || (allow_terms[t] && !(o.s2_tau2[t] > 0));
+    std::vector<int32_t> hc;
+    if (need_x) {
+      hc.resize((size_t)P * p * 2);
+      CK(cudaMemcpyAsync(hc.data(), dcnt, 4 * hc.size(), cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    for (uint32_t k = 0; k < P; ++k) {
+      const double nk = ctx->ph_n[k];
+      double vx = 0, mx = 0;
+      if (need_x) {
+        double tv = 0, tm = 0;
+        for (uint64_t j = 0; j < p; ++j) {
+          const double n1 = hc[((size_t)k * p + j) * 2], n2 = hc[((size_t)k * p + j) * 2 + 1];
+          const double sq = n1 + 4.0 * n2, sm = n1 + 2.0 * n2;
+          tm += sm / nk;
+          tv += (sq - sm * sm / nk) / (nk - 1);
+        }
+        vx = tv / p;
+        mx = tm / p;
+      }
+      const double s2s_k = (o.s2_sigma2 > 0) ? o.s2_sigma2
+                                             : ctx->ph_var_y[k] * (1 - o.R2mode_sigma2) * (o.nu_sigma2 + 2) / o.nu_sigma2;
+      if (s2s_k <= 0) throw bmg_error(BMG_EINVAL, "Prior specification error: s2_sigma2 is not positive (sample " +
+                                                      std::to_string(k) + ")");
+      DevPheno r;
+      std::memset(&r, 0, sizeof(r));
+      r.n = nk;
+      r.n_plus_nu = nk + o.nu_sigma2;
+      r.minus_n_plus_nu_2 = -0.5 * r.n_plus_nu;
+      r.nus2_plus_yy = o.nu_sigma2 * s2s_k + ctx->ph_yy[k];
+      r.rng_nu = nk + o.nu_sigma2;
+      for (int t = 0; t < 4; ++t) {
+        if (!allow_terms[t]) {
+          r.nus2_tau2[t] = NAN;
+          chain_inv0[k][t] = NAN;
+          continue;
+        }
+        const double s2t_k = (o.s2_tau2[t] > 0) ? o.s2_tau2[t]
+                                                : o.eh_tau2[t] * (o.nu_tau2[t] - 2) /
+                                                      (o.nu_tau2[t] * (vx + mx * mx) * (1 - o.R2mode_sigma2));
+        if (!(s2t_k > 0)) throw bmg_error(BMG_EINVAL, "Prior specification error: s2_tau2 is not positive");
+        r.nus2_tau2[t] = o.nu_tau2[t] * s2t_k;
+        chain_inv0[k][t] = 1.0 / (alpha2 * (r.nus2_tau2[t] / std::max(0.1, (o.nu_tau2[t] - 2))));
+      }
+      r.y_absmax = ctx->ph_amax[k];
+      r.sy = ctx->ph_sy[k];
+      r.y = ctx->ph_y_dev + (size_t)k * n;
+      r.yint = ctx->ph_yint_dev + (size_t)k * n;
+      r.mask2 = dm2 + (size_t)k * nw64;
+      r.cnt = dcnt + (size_t)k * p * 2;
+      r.pre = dpre + (size_t)k * p * offset;
+      r.gsum = nullptr;
+      recs.push_back(r);
+      pheno_of[k] = k;
+      chain_ee0[k] = nk;
+      chain_ey0[k] = ctx->ph_ysum[k];
+    }
+  }
+  {
+    DevPheno* dph = ctx->dalloc<DevPheno>(recs.size(), false);
+    uint32_t* dpo = ctx->dalloc<uint32_t>(C, false);
+    CK(cudaMemcpyAsync(dph, recs.data(), sizeof(DevPheno) * recs.size(), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(dpo, pheno_of.data(), 4 * C, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    K.ph = dph;
+    K.pheno_of = dpo;
+  }
   K.mu_alpha = o.mu_alpha;
   K.use_individual_tau2 = o.use_individual_tau2;
   K.rng_nu = (double)n + o.nu_sigma2;
@@ -812,11 +1002,15 @@ extern "C" bmg_status bmg_precompute(bmg_ctx* ctx)
     M.llen = M.vlen = M.blen = (int)me;
     M.ll = NAN;
     // covariate block (src/model.hpp:92-105)
-    std::vector<double> xx((size_t)me * km, 0.0);
+    std::vector<double> xx((size_t)me * km, 0.0), xy0(ey);
     for (uint32_t j = 0; j < me; ++j)
       for (uint32_t i = 0; i <= j; ++i) xx[(size_t)j * km + i] = ee[(size_t)j * me + i];
+    if (ctx->multi) {  // the constant column of this chain's sample
+      xx[0] = chain_ee0[c % C];
+      xy0[0] = chain_ey0[c % C];
+    }
     CK(cudaMemcpyAsync(M.xx, xx.data(), 8 * xx.size(), cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(M.xy, ey.data(), 8 * me, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(M.xy, xy0.data(), 8 * me, cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaMemcpyAsync(M.inv, ite.data(), 8 * me, cudaMemcpyHostToDevice, ctx->stream));
     std::vector<int32_t> xt(me, 4);
     CK(cudaMemcpyAsync(M.xc_type, xt.data(), 4 * me, cudaMemcpyHostToDevice, ctx->stream));
@@ -837,7 +1031,7 @@ extern "C" bmg_status bmg_precompute(bmg_ctx* ctx)
     h.n_acpt[0] = h.n_acpt[1] = h.n_acpt[2] = 1;
     h.alpha = alpha0;
     h.alpha2 = alpha2;
-    for (int t = 0; t < 4; ++t) h.inv_t2a2[t] = inv0[t];
+    for (int t = 0; t < 4; ++t) h.inv_t2a2[t] = chain_inv0[c][t];
     h.p_move_size = o.p_move_size;
     h.k_move_size = 1000.0 / (double)o.n_rao_burnin;
     geometric_cdf(ctx->max_ms, o.p_move_size, &qms[(size_t)c * 256]);
@@ -1249,6 +1443,7 @@ extern "C" bmg_status bmg_scan_schur(bmg_ctx* ctx, double* dlml)
   if (!ctx || !dlml) return BMG_EINVAL;
   API_BEGIN
   check_ready(ctx);
+  if (ctx->multi) throw bmg_error(BMG_EUNSUPPORTED, "the Schur scan needs one phenotype per context");
   const uint32_t C = ctx->C;
   const size_t out_n = (size_t)C * ctx->p * ctx->K.n_terms;
   if (!ctx->schur_out) ctx->schur_out = ctx->dalloc<double>(out_n, false);

@@ -42,8 +42,9 @@ __device__ __forceinline__ void mlp_features(const DevConst& K, uint32_t c, uint
   float l = (float)(lo * (1.0 / 16.0));
   l = fminf(fmaxf(l, -4.0f), 4.0f);
   const bool in = (K.inbits[(size_t)c * ((K.p + 31) / 32) + (j >> 5)] >> (j & 31)) & 1u;
-  const float n = (float)K.n;
-  const float n1 = (float)K.cnt[2 * j], n2 = (float)K.cnt[2 * j + 1];
+  const DevPheno& P = K.ph[K.pheno_of[c]];
+  const float n = (float)P.n;
+  const float n1 = (float)P.cnt[2 * j], n2 = (float)P.cnt[2 * j + 1];
   const float af = (n1 + 2.0f * n2) / (2.0f * n);
   f[0] = l;
   f[1] = in ? 1.0f : 0.0f;
@@ -111,8 +112,10 @@ extern "C" __global__ void __launch_bounds__(128) bmg_mlp_ld_kernel(DevConst K)
   if ((int)mi >= M.k) return;
   const uint64_t m = M.loci[mi];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const double n = (double)K.n;
-  const double sm = K.cnt[2 * m] + 2.0 * K.cnt[2 * m + 1], qm = K.cnt[2 * m] + 4.0 * K.cnt[2 * m + 1];
+  const DevPheno& P = K.ph[K.pheno_of[c]];
+  const int32_t* cnt = P.cnt;
+  const double n = P.n;
+  const double sm = cnt[2 * m] + 2.0 * cnt[2 * m + 1], qm = cnt[2 * m] + 4.0 * cnt[2 * m + 1];
   const double vm = qm / n - (sm / n) * (sm / n);
   const uint64_t* rm = reinterpret_cast<const uint64_t*>(K.geno + m * K.gs);
   const unsigned nw64 = K.gs / 8;
@@ -124,13 +127,14 @@ extern "C" __global__ void __launch_bounds__(128) bmg_mlp_ld_kernel(DevConst K)
     long long xy = 0;
     for (unsigned w = lane; w < nw64; w += 32) {
       const uint64_t x = rm[w], y = rs[w];
-      const uint64_t xh = (x >> 1) & m5, xl = x & m5, yh = (y >> 1) & m5, yl = y & m5;
+      const uint64_t mk = P.mask2 ? P.mask2[w] : m5;
+      const uint64_t xh = (x >> 1) & mk, xl = x & m5, yh = (y >> 1) & mk, yl = y & m5;
       const uint64_t Hx = xh & ~xl, Rx = xh & xl, Hy = yh & ~yl, Ry = yh & yl;
       xy += __popcll(Hx & Hy) + 2 * __popcll(Hx & Ry) + 2 * __popcll(Rx & Hy) + 4 * __popcll(Rx & Ry);
     }
     xy = warp_sum_ll(xy);
     if (lane == 0) {
-      const double ss = K.cnt[2 * s] + 2.0 * K.cnt[2 * s + 1], qs = K.cnt[2 * s] + 4.0 * K.cnt[2 * s + 1];
+      const double ss = cnt[2 * s] + 2.0 * cnt[2 * s + 1], qs = cnt[2 * s] + 4.0 * cnt[2 * s + 1];
       const double vs = qs / n - (ss / n) * (ss / n);
       const double cov = (double)xy / n - (sm / n) * (ss / n);
       const float r = (vm > 0 && vs > 0) ? (float)fabs(cov / sqrt(vm * vs)) : 0.0f;

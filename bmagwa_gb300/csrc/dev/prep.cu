@@ -119,3 +119,59 @@ bmg_gsum_kernel(const uint8_t* geno, uint64_t n, uint64_t p, uint32_t gs, const 
     }
   }
 }
+
+// Several phenotypes: #het and #hom-alt of every SNP among the individuals of
+// every sample (mask2: 01 in the 2-bit slot of each individual of sample k),
+// cnt[(k p + j) 2 + {0, 1}].  One warp per (SNP, sample).
+extern "C" __global__ void __launch_bounds__(256)
+bmg_mask_counts_kernel(const uint8_t* geno, uint32_t gs, uint64_t p, const uint64_t* mask2, uint32_t n_samples,
+                       int32_t* cnt)
+{
+  const int lane = threadIdx.x & 31;
+  const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+  const uint64_t nw64 = gs / 8;
+  for (uint64_t t = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); t < p * n_samples; t += warps) {
+    const uint64_t j = t % p, k = t / p;
+    const uint64_t* row = reinterpret_cast<const uint64_t*>(geno + j * gs);
+    const uint64_t* mk = mask2 + k * nw64;
+    unsigned h = 0, r = 0;
+    for (uint64_t w = lane; w < nw64; w += 32) {
+      const uint64_t x = row[w], m = mk[w];
+      const uint64_t hi = (x >> 1) & m, lo = x & m;
+      h += __popcll(hi & ~lo);
+      r += __popcll(hi & lo);
+    }
+    h = (unsigned)warp_sum_i((int)h);
+    r = (unsigned)warp_sum_i((int)r);
+    if (lane == 0) {
+      cnt[t * 2] = (int32_t)h;
+      cnt[t * 2 + 1] = (int32_t)r;
+    }
+  }
+}
+
+// The precomputed sums of every SNP within every sample from its counts
+// (src/precomputed_snp_covariances.hpp:95-131; the same expressions as the
+// single-sample host pass), pre[(k p + j) offset + .].
+extern "C" __global__ void bmg_pre_kernel(const int32_t* cnt, uint64_t p, uint32_t n_samples, const double* n_of,
+                                          int allow_mask, int ah, int offset, double* pre)
+{
+  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < p * n_samples;
+       t += (uint64_t)gridDim.x * blockDim.x) {
+    const double n = n_of[t / p];
+    const double n1 = cnt[2 * t], n2 = cnt[2 * t + 1];
+    double* loc = pre + t * (uint64_t)offset;
+    for (int u = 0; u < 4; ++u) {
+      if (!((allow_mask >> u) & 1)) continue;
+      const double ch = (u == 3) ? 0 : 1, cr = (u == 0) ? 2 : (u == 1 ? 0 : 1);
+      const double xs = ch * n1 + cr * n2;
+      const double xx = ch * ch * n1 + cr * cr * n2;
+      *loc++ = xs;
+      *loc++ = xx - xs * xs / n;
+    }
+    if (ah) {
+      const double as = n1 + 2 * n2, hs = n1;
+      *loc = n1 - as * hs / n;
+    }
+  }
+}

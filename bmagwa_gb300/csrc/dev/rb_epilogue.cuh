@@ -28,7 +28,7 @@ static __device__ __forceinline__ double rb_fast_pr(const DevConst& K, int c, ui
 {
   const RbParams& rp = K.rb[c];
   const int type = K.types[0];
-  const double* pre = K.pre + j * (size_t)K.offset;
+  const double* pre = K.ph[K.pheno_of[c]].pre + j * (size_t)K.offset;
   const int off = K.offset_type[type];
   const double xr = (double)xi * rp.scale;
   const double det = pre[off + 1] + rp.itv[type];
@@ -61,7 +61,8 @@ static __device__ __forceinline__ void rb_store1(const DevConst& K, int c, uint6
 static __device__ __noinline__ void rb_epilogue(const DevConst& K, int c, uint64_t j, const long long* xr_by_type)
 {
   const RbParams& rp = K.rb[c];
-  const double n = (double)K.n;
+  const DevPheno& P = K.ph[K.pheno_of[c]];
+  const double n = P.n;
   double xr[4];
   for (int t = 0; t < 4; ++t) xr[t] = K.allow_terms[t] ? (double)xr_by_type[t] * rp.scale : 0.0;
   double mr = rp.mr;
@@ -94,21 +95,21 @@ static __device__ __noinline__ void rb_epilogue(const DevConst& K, int c, uint64
       else itv[type] = M.inv[x1];
     }
     // r_om = r + x_j beta_j: products and mean from the genotype counts
-    double msum = b1 * (double)term_sum(K.cnt, j, t1);
+    double msum = b1 * (double)term_sum(P.cnt, j, t1);
     for (int t = 0; t < 4; ++t)
-      if (K.allow_terms[t]) xr[t] += b1 * (double)term_cross_same(K.cnt, j, t, t1);
+      if (K.allow_terms[t]) xr[t] += b1 * (double)term_cross_same(P.cnt, j, t, t1);
     if (type == 4) {
       int x2 = M.x_ind2[mi];
       int t2 = M.xc_type[x2];
       double b2 = M.beta[x2];
-      msum += b2 * (double)term_sum(K.cnt, j, t2);
+      msum += b2 * (double)term_sum(P.cnt, j, t2);
       for (int t = 0; t < 4; ++t)
-        if (K.allow_terms[t]) xr[t] += b2 * (double)term_cross_same(K.cnt, j, t, t2);
+        if (K.allow_terms[t]) xr[t] += b2 * (double)term_cross_same(P.cnt, j, t, t2);
     }
     mr = mr + msum / n;
     lmp = rp.lmp_rem[type];
   }
-  const double* pre = K.pre + j * (size_t)K.offset;
+  const double* pre = P.pre + j * (size_t)K.offset;
   const int nt = K.n_types;
   const bool ut = nt > 1;
   double pt[5];

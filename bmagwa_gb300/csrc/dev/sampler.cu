@@ -40,6 +40,7 @@
 struct MoveShared {
   DevModel mod[2];      // current (0) and proposed (1) model headers
   DevChain chs;         // the chain's dynamic state
+  DevPheno phs;         // the chain's sample
   double Ls[2][SM_TRI];
   double vs[2][SMK];
   double tv[2][SMK];    // work vectors for beta and its mean
@@ -91,6 +92,7 @@ struct BulkCols {
 
 struct Warp {
   const DevConst& K;
+  const DevPheno& P;    // the chain's sample (shared-memory copy)
   int c;
   DevChain* ch;
   DevModel* cur;
@@ -101,7 +103,7 @@ struct Warp {
   unsigned km;
 
   __device__ Warp(const DevConst& k, int chain, MoveShared& sh)
-  : K(k), c(chain), ch(&sh.chs), cur(&sh.mod[0]), nm(&sh.mod[1]), s(sh),
+  : K(k), P(sh.phs), c(chain), ch(&sh.chs), cur(&sh.mod[0]), nm(&sh.mod[1]), s(sh),
     lane(threadIdx.x & 31), km(k.km)
   {
     rng = sh.chs.rng;
@@ -120,9 +122,9 @@ struct Warp {
   __device__ double sinvchi2(double s2)
   {
     for (int t = 0; t < 64; ++t) {
-      double g = bmg_gamma(&rng, 0.5 * K.rng_nu);
+      double g = bmg_gamma(&rng, 0.5 * P.rng_nu);
       if (isnan(g)) { fail(BMG_DERR_RNG); return 1.0; }
-      double val = K.rng_nu * s2 / (2.0 * g);
+      double val = P.rng_nu * s2 / (2.0 * g);
       if (val > 0 && isfinite(val)) return val;
     }
     fail(BMG_DERR_RNG);
@@ -389,12 +391,12 @@ struct Warp {
     double vv = dot(vb, vb, m);
     double ldqx = 0;
     for (int i = 0; i < m; ++i) ldqx += log(lb[TRI(i, i)]);
-    double syx = K.nus2_plus_yy - vv;
+    double syx = P.nus2_plus_yy - vv;
     if (lane == 0) {
       M->vlen = m;
       M->syx = syx;
       M->ldqx = ldqx;
-      M->ll = ldq - ldqx + K.minus_n_plus_nu_2 * log(syx);
+      M->ll = ldq - ldqx + P.minus_n_plus_nu_2 * log(syx);
       M->mu_beta_computed = 0;
     }
     __syncwarp();
@@ -405,14 +407,30 @@ struct Warp {
   // vector's fixed point, from the per-SNP H and R sums
   __device__ long long geno_dot_fixed(uint32_t snp, int term, int v)
   {
-    const size_t nv = K.m_e > 1 ? K.m_e : 1;
-    const int64_t* g = K.gsum + ((size_t)snp * nv + v) * 2;
-    return (long long)coefH(term) * g[0] + (long long)coefR(term) * g[1];
+    if (P.gsum) {
+      const size_t nv = K.m_e > 1 ? K.m_e : 1;
+      const int64_t* g = P.gsum + ((size_t)snp * nv + v) * 2;
+      return (long long)coefH(term) * g[0] + (long long)coefR(term) * g[1];
+    }
+    // the phenotype from the codes (no covariates in this case): 16
+    // individuals per 32-bit word, the phenotype is zero outside the sample
+    const uint32_t* row = reinterpret_cast<const uint32_t*>(K.geno + (size_t)snp * K.gs);
+    const long long cH = coefH(term), cR = coefR(term);
+    long long acc = 0;
+    for (uint32_t w = lane; w < (uint32_t)(K.gs / 4); w += 32) {
+      const uint32_t code = row[w];
+      if (!code) continue;
+      for (int q = 0; q < 16; ++q) {
+        const uint32_t c2 = (code >> (2 * q)) & 3u;
+        if (c2 >= 2u) acc += (c2 == 2u ? cH : cR) * P.yint[(size_t)16 * w + q];
+      }
+    }
+    return warp_sum_ll(acc);
   }
   // exact sum_i x_t(g_a,i) x_u(g_b,i) from the 2-bit codes
   __device__ long long geno_cross(uint32_t a, int t, uint32_t b, int u)
   {
-    if (a == b) return term_cross_same(K.cnt, a, t, u);
+    if (a == b) return term_cross_same(P.cnt, a, t, u);
     const uint64_t* ra = (const uint64_t*)(K.geno + (size_t)a * K.gs);
     const uint64_t* rb = (const uint64_t*)(K.geno + (size_t)b * K.gs);
     unsigned nw64 = K.gs / 8;
@@ -420,7 +438,8 @@ struct Warp {
     const uint64_t m5 = 0x5555555555555555ull;
     for (unsigned w = lane; w < nw64; w += 32) {
       uint64_t x = ra[w], y = rb[w];
-      uint64_t xh = (x >> 1) & m5, xl = x & m5, yh = (y >> 1) & m5, yl = y & m5;
+      const uint64_t mk = P.mask2 ? P.mask2[w] : m5;
+      uint64_t xh = (x >> 1) & mk, xl = x & m5, yh = (y >> 1) & mk, yl = y & m5;
       uint64_t Hx = xh & ~xl, Rx = xh & xl, Hy = yh & ~yl, Ry = yh & yl;
       hh += __popcll(Hx & Hy);
       hr += __popcll(Hx & Ry);
@@ -435,7 +454,7 @@ struct Warp {
   __device__ double cross_col(const DevModel* M, int r, uint32_t snp, int term)
   {
     if (r < (int)K.m_e) {
-      if (r == 0) return (double)term_sum(K.cnt, snp, term);
+      if (r == 0) return (double)term_sum(P.cnt, snp, term);
       long long acc = geno_dot_fixed(snp, term, r);
       return (double)acc * ldexp(1.0, -K.se[r]);
     }
@@ -465,7 +484,7 @@ struct Warp {
 #pragma unroll 4
       for (unsigned w = lane; w < nw64; w += 32) {
         const uint64_t y = rb[w];
-        const uint64_t yh = (y >> 1) & m5, yl = y & m5;
+        const uint64_t yh = (y >> 1) & (P.mask2 ? P.mask2[w] : m5), yl = y & m5;
         const uint64_t Hy = yh & ~yl, Ry = yh & yl;
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
@@ -508,7 +527,7 @@ struct Warp {
       M->inv[col] = invv;
     }
     long long xyi = geno_dot_fixed(snp, term, 0);
-    double xyc = (double)xyi * ldexp(1.0, -K.sy);
+    double xyc = (double)xyi * ldexp(1.0, -P.sy);
     __syncwarp();
     if (lane == 0) M->xy[col] = xyc;
     double* xxcol = &M->xx[(size_t)col * km];
@@ -518,7 +537,7 @@ struct Warp {
       if (lane == 0) xxcol[r] = v;
     }
     cross_cols(M, me, col, snp, term, xxcol);
-    if (lane == 0) xxcol[col] = (double)term_cross_same(K.cnt, snp, term, term);
+    if (lane == 0) xxcol[col] = (double)term_cross_same(P.cnt, snp, term, term);
     __syncwarp();
     if (!update) {
       if (lane == 0) { M->llen = col + 1; M->vlen = col + 1; }
@@ -558,7 +577,7 @@ struct Warp {
       M->syx = syx;
       M->ldq = ldq;
       M->ldqx = ldqx;
-      M->ll = ldq - ldqx + K.minus_n_plus_nu_2 * log(syx);
+      M->ll = ldq - ldqx + P.minus_n_plus_nu_2 * log(syx);
     }
     __syncwarp();
   }
@@ -702,7 +721,7 @@ struct Warp {
       trsv_T(M, vb, nl);
       double ldqx = 0;
       for (int i = 0; i < nl; ++i) ldqx += log(L(M, i, i));
-      double syx = K.nus2_plus_yy - dot(vb, vb, xc);
+      double syx = P.nus2_plus_yy - dot(vb, vb, xc);
       if (lane == 0) {
         M->llen = nl;
         M->vlen = xc;
@@ -712,7 +731,7 @@ struct Warp {
       __syncwarp();
     }
     double ldq = M->ldq - 0.5 * log(invv);
-    double ll = ldq - M->ldqx + K.minus_n_plus_nu_2 * log(M->syx);
+    double ll = ldq - M->ldqx + P.minus_n_plus_nu_2 * log(M->syx);
     __syncwarp();
     if (lane == 0) {
       M->ldq = ldq;
@@ -766,7 +785,7 @@ struct Warp {
   /* src/model.hpp:314-342, src/rand.hpp:144-168 */
   __device__ void sample_beta_sigma2(DevModel* M)
   {
-    double s2 = sinvchi2(M->syx / K.n_plus_nu);
+    double s2 = sinvchi2(M->syx / P.n_plus_nu);
     int len = M->vlen;
     // the triangular solves run on shared copies when the model fits
     const bool on_chip = len <= SMK && M->llen <= SMK;
@@ -808,7 +827,7 @@ struct Warp {
         int t = M->xc_type[i];
         double nu = K.nu_tau2[t] + 1.0;
         double b = M->beta[i];
-        double s2 = (K.nus2_tau2[t] + b * b / a2s2) / nu;
+        double s2 = (P.nus2_tau2[t] + b * b / a2s2) / nu;
         double v = 1.0 / (ch->alpha2 * sinvchi2(nu, s2));
         __syncwarp();
         if (lane == 0) M->inv[i] = v;
@@ -826,7 +845,7 @@ struct Warp {
         it[t] = ch->inv_t2a2[t];
         if (!K.allow_terms[t]) continue;
         double nu = K.nu_tau2[t] + mt[t];
-        double s2 = (K.nus2_tau2[t] + b2s[t] / a2s2) / nu;
+        double s2 = (P.nus2_tau2[t] + b2s[t] / a2s2) / nu;
         it[t] = 1.0 / (ch->alpha2 * sinvchi2(nu, s2));
       }
       __syncwarp();
@@ -1583,6 +1602,7 @@ struct Warp {
 
 __device__ void bulk_phase(const DevConst& K, int c, MoveShared& s, BulkCols& bc)
 {
+  const DevPheno& P = s.phs;
   const int tid = threadIdx.x, nth = blockDim.x;
   const int mode = s.bulk_mode, nt = s.bulk_nterm, sh = s.bulk_s;
   const int me = K.m_e;
@@ -1596,7 +1616,7 @@ __device__ void bulk_phase(const DevConst& K, int c, MoveShared& s, BulkCols& bc
   // (src/sampler.cpp:735).  The same update is reproduced here.
   const bool stale = (nt == 0) && (me > 1);
   double* yhat = K.yhat + (size_t)c * K.n;
-  const int dsh = K.sy - sh;
+  const int dsh = P.sy - sh;
   // a thread takes 16 individuals at a time: one 32-bit word of every model
   // column's packed codes, so each column costs one coalesced load per word
   const uint32_t words = (uint32_t)(K.n_pad / 16);
@@ -1620,7 +1640,8 @@ __device__ void bulk_phase(const DevConst& K, int c, MoveShared& s, BulkCols& bc
 #pragma unroll
     for (int q = 0; q < 16; ++q) {
       const uint64_t i = (uint64_t)16 * w + q;
-      const bool live = i < K.n;
+      // individuals outside the chain's sample have no residual
+      const bool live = i < K.n && (!P.mask2 || ((P.mask2[i >> 5] >> (2 * (i & 31))) & 1ull));
       const long long yg = yg16[q];
       double ye = 0;
       if (live) {
@@ -1642,7 +1663,7 @@ __device__ void bulk_phase(const DevConst& K, int c, MoveShared& s, BulkCols& bc
         s2g += ygd * ygd;
         if (mode & BULK_ALPHA) {
           // eb = E beta_E - y, xb = fitted genotype part
-          s1e += (ye - K.y[i]) * ygd;
+          s1e += (ye - P.y[i]) * ygd;
         } else {
           s1e += ye;
           s2e += ye * ye;
@@ -1653,7 +1674,7 @@ __device__ void bulk_phase(const DevConst& K, int c, MoveShared& s, BulkCols& bc
       }
       long long R = 0;
       if (live && (mode & BULK_RESID)) {
-        const long long Y = K.yint[i];
+        const long long Y = P.yint[i];
         const long long Ys = (dsh > 0) ? ((Y + (1ll << (dsh - 1))) >> dsh) : (Y << (-dsh));
         if (stale) {
           const double yv = (mode & BULK_PVE) ? yh : yhat[i];
@@ -1732,7 +1753,7 @@ __device__ void bulk_setup(Warp& W, BulkCols& bc, int mode)
     // hold |R| < 2^(8L-1)
     double eb = 0;
     for (int e = 0; e < me && e < bl; ++e) eb += K.e_absmax[e] * fabs(M->beta[e]);
-    double tot = bound + K.y_absmax + eb + 1e-300;
+    double tot = bound + W.P.y_absmax + eb + 1e-300;
     if (nt == 0 && me > 1) tot += W.ch->yhat_absmax;  // the accumulated y_hat
     int e2 = (int)ceil(log2(tot));
     sh = (int)(8 * K.limbs_n - 3) - e2;
@@ -1810,7 +1831,7 @@ __device__ void prep_rb(Warp& W, bool scan_only)
     rp->prop_z2 = pz2;
     rp->inv_2s2 = 1.0 / (2 * M->sigma2);
     rp->scale = ldexp(1.0, -W.s.bulk_s);
-    rp->mr = (double)W.s.bsuml[0] * ldexp(1.0, -W.s.bulk_s) / (double)K.n;
+    rp->mr = (double)W.s.bsuml[0] * ldexp(1.0, -W.s.bulk_s) / W.P.n;
     for (int t = 0; t < 4; ++t) {
       rp->itv[t] = ch->inv_t2a2[t];
       rp->nlog_itv[t] = -log(ch->inv_t2a2[t]);
@@ -1883,6 +1904,7 @@ __device__ void load_state(const DevConst& K, int c, MoveShared& s)
   block_copy(&s.chs, K.ch + c);
   block_copy(&s.mod[0], K.cur + c);
   block_copy(&s.mod[1], K.nm + c);
+  block_copy(&s.phs, K.ph + K.pheno_of[c]);
   __syncthreads();
   for (int i = 0; i < 2; ++i) {
     const DevModel& M = s.mod[i];
@@ -2083,7 +2105,7 @@ bmg_move_kernel(DevConst K, int max_iters)
       if (tid < 32) {
         /* src/sampler.cpp:691-727, src/model.hpp:345-392 */
         DevModel* M = W.cur;
-        const double n = (double)K.n;
+        const double n = s.phs.n;
         const bool ce = K.m_e > 1, cg = M->k > 0;
         double pv[3];
         double vg = (s.bsum[1] - s.bsum[0] * s.bsum[0] / n) / (n - 1);

@@ -57,17 +57,18 @@ __device__ double schur_unit(const DevConst& K, int c, uint64_t j, int term, dou
     uu += g[i] * g[i];
     uv += g[i] * M.v[i];
   }
+  const DevPheno& P = K.ph[K.pheno_of[c]];
   const double inv_t = K.ch[c].inv_t2a2[term];
-  const double xxc = (double)term_cross_same(K.cnt, j, term, term);
+  const double xxc = (double)term_cross_same(P.cnt, j, term, term);
   const size_t nv = K.m_e > 1 ? K.m_e : 1;
-  const int64_t* gs = K.gsum + (size_t)j * nv * 2;
-  const double xy = (double)((long long)coefH(term) * gs[0] + (long long)coefR(term) * gs[1]) * ldexp(1.0, -K.sy);
+  const int64_t* gs = P.gsum + (size_t)j * nv * 2;
+  const double xy = (double)((long long)coefH(term) * gs[0] + (long long)coefR(term) * gs[1]) * ldexp(1.0, -P.sy);
   const double d2 = xxc + inv_t - uu;
   if (!(d2 > 0)) return -INFINITY;
   const double lcc = sqrt(d2);
   const double w = (xy - uv) / lcc;
   const double S = M.syx;
-  return 0.5 * log(inv_t) - log(lcc) + K.minus_n_plus_nu_2 * (log(S - w * w) - log(S));
+  return 0.5 * log(inv_t) - log(lcc) + P.minus_n_plus_nu_2 * (log(S - w * w) - log(S));
 }
 
 }  // namespace
@@ -162,9 +163,10 @@ bmg_schur_tc_kernel(DevConst K, TcParams P, uint32_t KB, uint32_t n_terms, doubl
         }
         // covariate entries: the constant from the counts, the others from
         // the fixed-point sums
-        g[0] = (double)term_sum(K.cnt, j, term);
+        const DevPheno& P = K.ph[K.pheno_of[c]];
+        g[0] = (double)term_sum(P.cnt, j, term);
         for (int r = 1; r < me; ++r) {
-          const int64_t* gs = K.gsum + ((size_t)j * me + r) * 2;
+          const int64_t* gs = P.gsum + ((size_t)j * me + r) * 2;
           g[r] = (double)((long long)coefH(term) * gs[0] + (long long)coefR(term) * gs[1]) * ldexp(1.0, -K.se[r]);
         }
         o = schur_unit(K, (int)c, j, term, g);

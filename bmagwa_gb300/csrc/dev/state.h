@@ -142,6 +142,25 @@ struct DevTrace {
 };
 
 // Read-only context constants.
+// The sample a chain is fitted to: one phenotype and the individuals it has
+// a value for.  All chains of a context share one record unless the context
+// holds several phenotypes (then chain c uses record c).  Counts, sums and
+// the fixed-point phenotype are over the sample only; the phenotype is zero
+// outside it, so products with it need no mask.
+struct DevPheno {
+  double n;              // individuals in the sample
+  double n_plus_nu, minus_n_plus_nu_2, nus2_plus_yy, rng_nu;
+  double nus2_tau2[4];   // nu_t s2_t of the term precisions' prior
+  double y_absmax;
+  int32_t sy;            // fixed-point exponent of y
+  const double* y;       // n entries (0 outside the sample)
+  const int64_t* yint;   // n entries, y 2^sy rounded
+  const uint64_t* mask2; // gs / 8 words: 01 in the 2-bit slot of each individual in the sample; null: all
+  const int32_t* cnt;    // p x 2: #het, #hom-alt within the sample
+  const double* pre;     // p x offset: the precomputed sums within the sample
+  const int64_t* gsum;   // p x nv x 2 fixed-point sums of y and covariates, or null (X'y from the codes)
+};
+
 // The learned part of the add proposal (no reference counterpart): a
 // 16 -> 128 -> 128 -> 1 MLP shared by the chains, its per-chain candidate
 // tables and the buffers of its features.  FP32 master parameters in one
@@ -269,6 +288,8 @@ struct DevConst {
   uint32_t* inbits;     // chains x ceil(p/32): SNP in current model
   uint32_t* basebits;   // chains x ceil(p/32): zeroed in the cadd base
   DevLearned lrn;
+  const DevPheno* ph;         // phenotype records
+  const uint32_t* pheno_of;   // chains: record of the chain
   double* p_lml;        // chains x p: log posterior odds of inclusion of the last scan, when requested (else null)
   int64_t* tile_sums;   // chains x ceil(p / BMG_REBUILD_TILE): rebuild pass 1
   int32_t* rebuild_active;  // chains: this rebuild covers the chain

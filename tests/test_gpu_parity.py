@@ -289,3 +289,49 @@ def test_schur_scan_against_fp64_oracle(bmg, oracle, tmp_path, case):
         assert ctx.state(c)[0].model_size > 0
     print("max relative error of the per-SNP LML change: %.3e" % worst)
     assert worst <= 1e-9
+
+
+def test_several_phenotypes_match_the_oracle_on_their_samples(bmg, oracle, tmp_path):
+    """One chain per phenotype, each fitted to the individuals its mask keeps,
+    all in one context: chain k equals the oracle run on the subset .bed of
+    phenotype k with the same seed (the reference's one-process-per-phenotype
+    baseline)."""
+    import torch
+    from bmagwa_gb300 import synth
+    iters = 200
+    ini = synth.make_dataset("plain", str(tmp_path), n=700, p=2500, chains=3, iters=iters, n_rao=2)
+    opt = bmg.options_from_ini(ini)
+    opt.adapt_p_move_size = 0  # early tuning ties break on last bits of exp
+    packed, y, e = bmg.read_plink(opt)
+    n, p = int(opt.n), int(opt.m_g)
+    rng = np.random.default_rng(4)
+    Y = np.stack([y, 0.6 * y + rng.normal(size=n), rng.normal(size=n)])
+    masks = (rng.random((3, n)) < np.array([[0.6], [0.85], [1.0]])).astype(np.uint8)
+    ctx = bmg.Context(opt)
+    ctx.load_bed(packed)
+    ctx.set_phenotypes(Y, masks)
+    ctx.set_covariates(None)
+    ctx.precompute()
+    colg = ctx.run(iters)
+    G = H.decode(packed, n, p)
+    seeds = [int(opt.seeds[c]) for c in range(3)]
+    for k in range(3):
+        keep = np.nonzero(masks[k])[0]
+        pk = synth.pack(torch.as_tensor(G[:, keep].astype(np.uint8))).numpy().reshape(-1)
+        ok = bmg.options_from_ini(ini)
+        ok.adapt_p_move_size = 0
+        ok.n = len(keep)
+        bmg.set_seeds(ok, [seeds[k]])
+        port = oracle.Port(ok, pk, Y[k][keep])
+        colp = port.run(iters)
+        a, b = colp.chain(0), colg.chain(k)
+        d = np.nonzero(a["jumpdistance"] != b["jumpdistance"])[0]
+        if len(d):
+            i = int(d[0])
+            print("phenotype", k, "first difference at", i, "moves", a["move_type"][i - 2:i + 2].tolist(),
+                  b["move_type"][i - 2:i + 2].tolist(), "sizes", a["move_size"][i - 2:i + 2].tolist(),
+                  b["move_size"][i - 2:i + 2].tolist(), "ll", a["log_likelihood"][max(0, i // 2 - 2):i // 2 + 2].tolist(),
+                  b["log_likelihood"][max(0, i // 2 - 2):i // 2 + 2].tolist())
+        H.compare(a, b, rtol=RTOL, label="phenotype %d" % k)
+        np.testing.assert_allclose(ctx.rao(k)[0], port.rao(0)[0], rtol=RTOL, atol=1e-12)
+    ctx.close()
