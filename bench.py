@@ -185,7 +185,7 @@ def run_gb300(args, wl):
     # the scan's launch-shape tuner times its candidates on the first scans;
     # finish it before the timed region
     extra = 0
-    while ctx.scan_shape()[0] < 0 and extra < 16:
+    while ctx.scan_shape()[0] < 0 and extra < 40:
         ctx.run(1, collect=False)
         extra += 1
     torch.cuda.synchronize()
@@ -202,6 +202,7 @@ def run_gb300(args, wl):
     ms = ctx.timings()
     launches = ctx.launch_count()
     scan_shape = ctx.scan_shape()[1]
+    scan_tuning = ctx.scan_tuning()
     n_scans = ctx.reset_timings()
     dev_s = ms[3] / 1000.0
     from bmagwa_gb300 import replicas
@@ -265,7 +266,7 @@ def run_gb300(args, wl):
                    "types": wl["types"], "parallelism": "replicas" if world > 1 else "single",
                    "l2": "inputs larger than L2 (%.2f GB packed genotypes)" % (packed.nbytes / 1e9),
                    "scan_impl": "tcgen05" if args.scan == 0 else "simt",
-                   "scan_shape": scan_shape},
+                   "scan_shape": scan_shape, "scan_tuning_ms": scan_tuning},
         "e2e": e2e,
         "gpu_launches": launches,
         "phase_ms": {"move": ms[0], "scan": ms[1], "rebuild": ms[2], "total": ms[3],

@@ -72,7 +72,13 @@ def lib():
         L.bmg_get_last_scan.argtypes = [vp, u32, vp, vp]
         L.bmg_get_data_stats.argtypes = [vp, vp]
         L.bmg_get_launch_count.argtypes = [vp, C.POINTER(u64)]
+        L.bmg_selftest_exp.argtypes = [vp, vp, C.c_size_t]
+        L.bmg_selftest_exp.restype = C.c_int
         L.bmg_get_scan_shape.argtypes = [vp, C.POINTER(C.c_int32), C.c_char_p, C.c_size_t]
+        L.bmg_get_scan_tuning.argtypes = [vp, vp, C.c_int32, C.POINTER(C.c_int32)]
+        L.bmg_get_scan_tuning.restype = C.c_int
+        L.bmg_get_scan_shape_name.argtypes = [C.c_int32, C.c_char_p, C.c_size_t]
+        L.bmg_get_scan_shape_name.restype = C.c_int
         L.bmg_last_error.argtypes = [vp]
         L.bmg_last_error.restype = C.c_char_p
         L.bmg_status_string.argtypes = [C.c_int]
@@ -296,6 +302,19 @@ class Context:
         self._check(lib().bmg_get_scan_shape(self.h, C.byref(v), buf, 128))
         return int(v.value), buf.value.decode()
 
+    def scan_tuning(self):
+        """{shape description: fastest tuning scan in ms} of the scan's tuner."""
+        n = C.c_int32(0)
+        self._check(lib().bmg_get_scan_tuning(self.h, None, 0, C.byref(n)))
+        ms = np.zeros(n.value, dtype=np.float32)
+        self._check(lib().bmg_get_scan_tuning(self.h, _ptr(ms), n.value, None))
+        out = {}
+        for i in range(n.value):
+            buf = C.create_string_buffer(128)
+            self._check(lib().bmg_get_scan_shape_name(i, buf, 128))
+            out[buf.value.decode()] = round(float(ms[i]), 4)
+        return out
+
     def reset_timings(self):
         n = C.c_uint64()
         self._check(lib().bmg_reset_timings(self.h, C.byref(n)))
@@ -315,6 +334,25 @@ def precompute_noalloc(d_packed, n, p, recode, types, d_out, d_flag, stream=None
     if rc != 0:
         raise BmgError(rc, "bmg_precompute_noalloc failed")
     return off.value
+
+
+def scan_shapes():
+    """Descriptions of the tensor-core scan's launch shapes, in shape order."""
+    out = []
+    buf = C.create_string_buffer(128)
+    while lib().bmg_get_scan_shape_name(len(out), buf, 128) == 0:
+        out.append(buf.value.decode())
+    return out
+
+
+def selftest_exp(a):
+    """The scan's table-driven exp of each |a| <= 700 (bmg_selftest_exp)."""
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    out = np.empty_like(a)
+    rc = lib().bmg_selftest_exp(_ptr(a), _ptr(out), a.size)
+    if rc != 0:
+        raise BmgError(rc, "bmg_selftest_exp failed")
+    return out
 
 
 def run_ini(path, n_iter=None, write_files=True):

@@ -7,6 +7,7 @@
 #include <math.h>
 
 #include "common.cuh"
+#include "exp_table.h"
 
 static __device__ __forceinline__ bool in_model(const DevConst& K, int c, uint64_t j)
 {
@@ -22,8 +23,30 @@ static __device__ __forceinline__ bool rb_fast_ok(const DevConst& K)
   return !K.use_individual_tau2 && K.n_types == 1 && K.types[0] != 4;
 }
 
+// exp(a) for |a| <= 700 by Tang's table-driven method (P. T. P. Tang,
+// "Table-driven implementation of the exponential function in IEEE
+// floating-point arithmetic", ACM TOMS 15(2), 1989).  a = k ln2/256 + r with
+// k = 256 m + i and |r| <= ln2/512, so exp(a) = 2^m 2^(i/256) exp(r).  The
+// reduction splits ln2/256 into a 34-bit head (k head exact for |k| < 2^19)
+// and a tail; exp(r) is its Taylor series to r^4 (truncation below 4e-17
+// relative).  Nine FP64 instructions; the 2^m scaling is an integer add to the
+// exponent field, valid because the result stays a normal number.
+static __device__ __forceinline__ double bmg_exp_tab(double a)
+{
+  const double shift = 0x1.8p52;  // adding it rounds a 256/ln2 to an integer in the low word
+  const double ks = fma(a, 0x1.71547652b82fep+8, shift);
+  const int k = __double2loint(ks);
+  const double kd = ks - shift;
+  double r = fma(-kd, 0x1.62e42fef80000p-9, a);
+  r = fma(-kd, 0x1.1cf79abc9e3b4p-44, r);
+  const double q = fma(fma(fma(1.0 / 24, r, 1.0 / 6), r, 0.5), r, 1.0);  // (exp(r) - 1) / r
+  const double t = __ldg(&kExp2Tab[k & 255]);
+  const double y = fma(t, r * q, t);
+  return __hiloint2double(__double2hiint(y) + ((k >> 8) << 20), __double2loint(y));
+}
+
 // p_r of (SNP j, chain c) from the exact product xi = x_t(j)' R_c; *lo gets
-// the log posterior odds of inclusion
+// the log posterior odds of inclusion when the scan keeps them (K.p_lml).
 static __device__ __forceinline__ double rb_fast_pr(const DevConst& K, int c, uint64_t j, long long xi, double* lo)
 {
   const RbParams& rp = K.rb[c];
@@ -32,13 +55,32 @@ static __device__ __forceinline__ double rb_fast_pr(const DevConst& K, int c, ui
   const int off = K.offset_type[type];
   const double xr = (double)xi * rp.scale;
   const double det = pre[off + 1] + rp.itv[type];
-  const double slq = rp.nlog_itv[type];
   const double rx = xr - pre[off] * rp.mr;
-  const double et = (rx * rx) / det;
-  const double p = et * rp.inv_2s2 - 0.5 * (log(det) + slq) + rp.lmp_add[type];
-  *lo = p;
-  const double e = exp(p);
-  return isfinite(e) ? e / (1 + e) : 1;
+  if (K.p_lml) {
+    // the reference's expression term by term, log odds kept
+    const double slq = rp.nlog_itv[type];
+    const double et = (rx * rx) / det;
+    const double p = et * rp.inv_2s2 - 0.5 * (log(det) + slq) + rp.lmp_add[type];
+    *lo = p;
+    const double e = exp(p);
+    return isfinite(e) ? e / (1 + e) : 1;
+  }
+  // the same odds without the log: with s = det^-1/2, rx^2/det = (rx s)^2 and
+  // exp(p) = exp(et/(2 sigma2) + lmp - slq/2) s.  Odds above 2^54 round
+  // p_r to 1 (a > 700 included, with NaN as the reference maps it); a < -700
+  // takes the library exp.
+  *lo = 0;
+  const double s = rsqrt(det);
+  const double t = rx * s;
+  const double a = fma(t * t, rp.inv_2s2, rp.cadd[type]);
+  if (!(a <= 700.0)) return 1;
+  double ea;
+  if (a >= -700.0)
+    ea = bmg_exp_tab(a);
+  else
+    ea = exp(a);
+  const double e = ea * s;
+  return e / (1 + e);
 }
 
 // p_r and the running means of one (SNP, chain) with one effect type
@@ -49,10 +91,10 @@ static __device__ __forceinline__ void rb_store1(const DevConst& K, int c, uint6
   const size_t cj = (size_t)c * K.p + j;
   if (K.p_r) K.p_r[cj] = pr;
   if (K.p_lml) K.p_lml[cj] = lo;
-  if (rp.acc_rao) K.p_rao[cj] = rp.rao_z2 * K.p_rao[cj] + pr / rp.rao_z1;
+  if (rp.acc_rao) K.p_rao[cj] = fma(rp.rao_z2, K.p_rao[cj], pr * rp.rao_iz1);
   if (rp.adapt) {
     const size_t q = (size_t)c * K.p + K.pos[j];
-    K.p_prop[q] = rp.prop_z2 * K.p_prop[q] + pr / rp.prop_z1;
+    K.p_prop[q] = fma(rp.prop_z2, K.p_prop[q], pr * rp.prop_iz1);
   }
 }
 
@@ -175,17 +217,17 @@ static __device__ __noinline__ void rb_epilogue(const DevConst& K, int c, uint64
       for (int t = 0; t < nt; ++t) K.p_r_types[cj * nt + t] = pt[t];
   }
   if (rp.acc_rao) {
-    K.p_rao[cj] = rp.rao_z2 * K.p_rao[cj] + pr / rp.rao_z1;
+    K.p_rao[cj] = fma(rp.rao_z2, K.p_rao[cj], pr * rp.rao_iz1);
     if (ut)
       for (int t = 0; t < nt; ++t)
-        K.p_rao_types[cj * nt + t] = rp.rao_z2 * K.p_rao_types[cj * nt + t] + pt[t] / rp.rao_z1;
+        K.p_rao_types[cj * nt + t] = fma(rp.rao_z2, K.p_rao_types[cj * nt + t], pt[t] * rp.rao_iz1);
   }
   if (rp.adapt) {
     size_t q = (size_t)c * K.p + K.pos[j];
-    K.p_prop[q] = rp.prop_z2 * K.p_prop[q] + pr / rp.prop_z1;
+    K.p_prop[q] = fma(rp.prop_z2, K.p_prop[q], pr * rp.prop_iz1);
     if (ut)
       for (int t = 0; t < nt; ++t)
-        K.p_prop_types[cj * nt + t] = rp.prop_z2 * K.p_prop_types[cj * nt + t] + pt[t] / rp.prop_z1;
+        K.p_prop_types[cj * nt + t] = fma(rp.prop_z2, K.p_prop_types[cj * nt + t], pt[t] * rp.prop_iz1);
   }
 }
 

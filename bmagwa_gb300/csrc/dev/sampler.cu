@@ -1825,9 +1825,9 @@ __device__ void prep_rb(Warp& W, bool scan_only)
     rp->do_scan = do_scan;
     rp->acc_rao = acc_rao;
     rp->adapt = adapt && !K.flat_proposal_dist;
-    rp->rao_z1 = rz1;
+    rp->rao_iz1 = rz1 > 0 ? 1.0 / rz1 : 0.0;
     rp->rao_z2 = rz2;
-    rp->prop_z1 = pz1;
+    rp->prop_iz1 = pz1 > 0 ? 1.0 / pz1 : 0.0;
     rp->prop_z2 = pz2;
     rp->inv_2s2 = 1.0 / (2 * M->sigma2);
     rp->scale = ldexp(1.0, -W.s.bulk_s);
@@ -1845,7 +1845,10 @@ __device__ void prep_rb(Warp& W, bool scan_only)
     if (!K.allow_types[t]) continue;
     double la = 0;
     if ((uint64_t)(Ns[t] + 1) <= K.p) la = W.lchange_add(Ns, nl, t);
-    if (W.lane == 0) rp->lmp_add[t] = la;
+    if (W.lane == 0) {
+      rp->lmp_add[t] = la;
+      if (t < 4) rp->cadd[t] = la - 0.5 * rp->nlog_itv[t];
+    }
     Ns[t]--;
     nl--;
     if (Ns[t] >= 0) {

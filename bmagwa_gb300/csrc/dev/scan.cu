@@ -50,6 +50,13 @@ bmg_scan_simt_kernel(DevConst K, const int64_t* resid_t)
   }
 }
 
+// out[i] = the scan's table-driven exp of a[i], |a[i]| <= 700 (self-test).
+extern "C" __global__ void bmg_exp_selftest_kernel(const double* a, double* out, uint64_t n)
+{
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    out[i] = bmg_exp_tab(a[i]);
+}
+
 // Transpose the move kernel's residuals (chains x n_pad) to individual-major.
 extern "C" __global__ void bmg_resid_transpose_kernel(DevConst K, int64_t* resid_t)
 {

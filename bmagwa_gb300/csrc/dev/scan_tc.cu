@@ -49,11 +49,12 @@ bmg_scan_tc_kernel(DevConst K, TcParams P, const __grid_constant__ CUtensorMap m
   long long* xr_s = reinterpret_cast<long long*>(smem + P.stages * P.stage_bytes);
   __shared__ TcCtl ctl;
   __shared__ int epi_ok;
-  __shared__ uint2 lut[4][256];  // per term: byte -> 4 bf16 values
+  __shared__ TcLut lut;  // per term: nibble -> 2 bf16 values
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t L = K.limbs_n;
   const uint32_t ct = P.chains_tile;
+  const uint32_t xs = ct + 1;  // row stride of the sums: odd, so rows fall in distinct banks
   const uint32_t my_tiles = (P.tiles > blockIdx.x) ? (P.tiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
   const uint32_t tmem = tc_setup(P, ctl, lut, TC_THREADS, TC_EPI_WARPS);
 
@@ -94,7 +95,7 @@ bmg_scan_tc_kernel(DevConst K, TcParams P, const __grid_constant__ CUtensorMap m
         long long acc = 0;
         for (uint32_t chunk = col_lo & ~31u; chunk < col_hi; chunk += 32) {
           float v[32];
-          tmem_ld32(tmem + ((quarter * 32) << 16) + b * TC_ACC_COLS + chunk, v);
+          tmem_ld32(tmem + ((quarter * 32) << 16) + b * P.acc_cols + chunk, v);
 #pragma unroll
           for (uint32_t q = 0; q < 32; ++q) {
             const uint32_t col = chunk + q;
@@ -102,7 +103,7 @@ bmg_scan_tc_kernel(DevConst K, TcParams P, const __grid_constant__ CUtensorMap m
             // |D| < 2^24: an exact float integer, converted through int32
             acc += (long long)__float2int_rn(v[q]) * (1ll << (8 * limb));
             if (++limb == L) {
-              xr_s[row * ct + chain] = acc;
+              xr_s[row * xs + chain] = acc;
               acc = 0;
               limb = 0;
               ++chain;
@@ -133,7 +134,7 @@ bmg_scan_tc_kernel(DevConst K, TcParams P, const __grid_constant__ CUtensorMap m
           if (j[h] >= K.p) j[h] = snp0;  // a valid address for the unused half
         }
         if (fast) {
-          const long long xa = xr_s[sl[0] * ct + cl[0]], xb = xr_s[sl[1] * ct + cl[1]];
+          const long long xa = xr_s[sl[0] * xs + cl[0]], xb = xr_s[sl[1] * xs + cl[1]];
           double la, lb;
           const double pa = rb_fast_pr(K, (int)c[0], j[0], xa, &la);
           const double pb = rb_fast_pr(K, (int)c[1], j[1], xb, &lb);
@@ -155,7 +156,7 @@ bmg_scan_tc_kernel(DevConst K, TcParams P, const __grid_constant__ CUtensorMap m
             long long xr[4] = {0, 0, 0, 0};
             for (uint32_t q = 0; q < P.tpad; ++q) {
               const int term = P.term_of_row[q];
-              if (term >= 0) xr[term] = xr_s[(sl[h] * P.tpad + q) * ct + cl[h]];
+              if (term >= 0) xr[term] = xr_s[(sl[h] * P.tpad + q) * xs + cl[h]];
             }
             rb_epilogue(K, (int)c[h], j[h], xr);
           }
@@ -177,10 +178,10 @@ static size_t tc_smem_bytes(const TcParams& P)
   return (size_t)P.stages * P.stage_bytes + P.xr_bytes + 1024;
 }
 
-// static shared memory of the kernel (decode tables and barriers) is below 9 KB
-constexpr size_t TC_SMEM_LIMIT = 227 * 1024 - 9 * 1024;
+// static shared memory of the kernel (decode tables and barriers) is below 2 KB
+constexpr size_t TC_SMEM_LIMIT = 227 * 1024 - 2 * 1024;
 
-static bool tc_plan(const DevConst* K, TcParams* P, uint32_t ct_cap)
+static bool tc_plan(const DevConst* K, TcParams* P, uint32_t ct_cap, uint32_t stages_cap)
 {
   uint32_t T = K->n_terms;
   P->tpad = T <= 1 ? 1 : (T <= 2 ? 2 : 4);
@@ -189,7 +190,6 @@ static bool tc_plan(const DevConst* K, TcParams* P, uint32_t ct_cap)
   const uint32_t L = K->limbs_n;
   if (K->n_pad % TC_BK != 0 || K->n >= 65536) return false;  // exact FP32 sums need n < 2^16
   P->k_chunks = K->n_pad / TC_BK;
-  P->a_bytes = TC_BM * 128;
   P->pk_bytes = P->snps_per_tile * 16;
   // widest chain tile whose accumulator fits one TMEM buffer and whose stages
   // (at least two) and sums fit shared memory
@@ -198,11 +198,14 @@ static bool tc_plan(const DevConst* K, TcParams* P, uint32_t ct_cap)
     P->n_mma = ((ct * L + 15) / 16) * 16;
     if (P->n_mma > TC_ACC_COLS || P->n_mma < 16) continue;
     P->b_bytes = P->n_mma * 128;
+    tc_place_a(*P);
     P->stage_bytes = ((P->b_bytes + P->a_bytes + P->pk_bytes + 1023) / 1024) * 1024;
-    P->xr_bytes = TC_BM * ct * 8;
+    P->xr_bytes = TC_BM * (ct + 1) * 8;
     P->b_rows_per_tile = ct * L;
-    for (uint32_t st = TC_MAX_STAGES; st >= 2; --st) {
+    const uint32_t st_max = stages_cap >= 2 && stages_cap < (uint32_t)TC_MAX_STAGES ? stages_cap : TC_MAX_STAGES;
+    for (uint32_t st = st_max; st >= 2; --st) {
       P->stages = st;
+      if (!P->a_tmem) P->a_stages = st;
       if (tc_smem_bytes(*P) <= TC_SMEM_LIMIT) {
         P->m_tiles = (uint32_t)((K->p + P->snps_per_tile - 1) / P->snps_per_tile);
         P->n_tiles = (K->n_chains + ct - 1) / ct;
@@ -214,14 +217,17 @@ static bool tc_plan(const DevConst* K, TcParams* P, uint32_t ct_cap)
   return false;
 }
 
-// Launch shapes the autotuner chooses between: epilogue warps and a cap on
-// the chains of one N tile (0: as many as one accumulator holds).  All of
-// them compute the same exact sums and the same posterior, bit for bit.
+// Launch shapes the autotuner chooses between: epilogue warps, a cap on the
+// chains of one N tile, and a cap on the depth of the shared-memory ring (a
+// deeper ring hides more TMA latency but leaves less of the SM's L1 to the
+// epilogue's loads).  All of them compute the same exact sums and the same
+// posterior, bit for bit.
 struct TcVariant {
   int epi;
-  int ct_div;  // chains per tile = ceil(chains / ct_div)
+  int ct_div;      // chains per tile = ceil(chains / ct_div)
+  int stages_cap;  // 0: as many stages as shared memory holds
 };
-static const TcVariant kTcVariants[] = {{12, 1}, {8, 1}, {12, 2}, {8, 2}};
+static const TcVariant kTcVariants[] = {{12, 1, 0}, {8, 1, 0}, {12, 2, 0}, {8, 2, 0}, {12, 1, 4}, {8, 1, 4}};
 constexpr int kTcVariantCount = sizeof(kTcVariants) / sizeof(kTcVariants[0]);
 
 extern "C" int bmg_scan_tc_variants() { return kTcVariantCount; }
@@ -229,7 +235,8 @@ extern "C" int bmg_scan_tc_variants() { return kTcVariantCount; }
 extern "C" void bmg_scan_tc_variant_name(int v, char* buf, size_t len)
 {
   if (v < 0 || v >= kTcVariantCount) v = 0;
-  snprintf(buf, len, "epilogue_warps=%d chains_per_tile=1/%d", kTcVariants[v].epi, kTcVariants[v].ct_div);
+  snprintf(buf, len, "epilogue_warps=%d chains_per_tile=1/%d ring=%s", kTcVariants[v].epi, kTcVariants[v].ct_div,
+           kTcVariants[v].stages_cap ? "4" : "max");
 }
 
 static uint32_t tc_cap(const DevConst* K, int v)
@@ -241,7 +248,7 @@ static uint32_t tc_cap(const DevConst* K, int v)
 extern "C" int bmg_scan_tc_supported(const DevConst* K)
 {
   TcParams P;
-  if (!tc_plan(K, &P, K->n_chains) || !encode_fn()) return 0;
+  if (!tc_plan(K, &P, K->n_chains, 0) || !encode_fn()) return 0;
   int dev = 0, major = 0, minor = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
@@ -277,7 +284,7 @@ extern "C" int bmg_scan_tc_launch(const DevConst* K, cudaStream_t stream, int va
 {
   if (variant < 0 || variant >= kTcVariantCount) variant = 0;
   TcParams P;
-  if (!tc_plan(K, &P, tc_cap(K, variant))) return 1;
+  if (!tc_plan(K, &P, tc_cap(K, variant), (uint32_t)kTcVariants[variant].stages_cap)) return 1;
   auto enc = encode_fn();
   if (!enc) return 2;
   CUtensorMap mb, mg;

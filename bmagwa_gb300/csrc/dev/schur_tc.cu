@@ -104,7 +104,7 @@ bmg_schur_tc_kernel(DevConst K, TcParams P, uint32_t KB, uint32_t n_terms, doubl
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   __shared__ TcCtl ctl;
   __shared__ int epi_ok;
-  __shared__ uint2 lut[4][256];
+  __shared__ TcLut lut;  // per term: nibble -> 2 bf16 values
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t ct = P.chains_tile;
   const uint32_t my_tiles = (P.tiles > blockIdx.x) ? (P.tiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
@@ -200,7 +200,10 @@ extern "C" int bmg_schur_launch(const DevConst* K, const int* xcols, uint16_t** 
   P.snps_per_tile = TC_BM / P.tpad;
   for (uint32_t u = 0; u < 4; ++u) P.term_of_row[u] = (u < T) ? K->term_of[u] : -1;
   P.k_chunks = K->n_pad / TC_BK;
-  P.a_bytes = TC_BM * 128;
+  P.a_bytes = TC_BM * 128;  // A in shared memory: the accumulators may take all 512 columns
+  P.a_tmem = 0;
+  P.a_stages = 0;
+  P.acc_cols = TC_ACC_COLS;
   P.pk_bytes = P.snps_per_tile * 16;
   P.chains_tile = std::max(1u, std::min(C, TC_ACC_COLS / KB));
   P.n_mma = P.chains_tile * KB;
@@ -212,6 +215,7 @@ extern "C" int bmg_schur_launch(const DevConst* K, const int* xcols, uint16_t** 
   for (uint32_t st = TC_MAX_STAGES; st >= 2 && !P.stages; --st)
     if ((size_t)st * P.stage_bytes + 1024 <= 227 * 1024 - 9 * 1024) P.stages = st;
   if (!P.stages) return 2;
+  P.a_stages = P.stages;
   P.m_tiles = (uint32_t)((K->p + P.snps_per_tile - 1) / P.snps_per_tile);
   P.n_tiles = (C + P.chains_tile - 1) / P.chains_tile;
   P.tiles = P.m_tiles * P.n_tiles;

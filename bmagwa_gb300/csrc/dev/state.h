@@ -111,10 +111,11 @@ struct RbParams {
   double scale;             // 2^-s of the fixed-point residual
   double itv[4];            // inv_tau2_alpha2 per term (shared tau2)
   double nlog_itv[4];       // -log(itv[t]), once per chain
+  double cadd[4];           // lmp_add[t] - nlog_itv[t] / 2: the odds' constant
   double lmp_add[5];
   double lmp_rem[5][5];
-  double rao_z1, rao_z2;    // running-mean weights of p_rao
-  double prop_z1, prop_z2;  // running-mean weights of p_proposal
+  double rao_iz1, rao_z2;   // running mean of p_rao: z2 old + p / z1, 1/z1 kept
+  double prop_iz1, prop_z2; // running mean of p_proposal, the same form
   double alpha2;            // Prior::alpha2_ for per-SNP tau2 draws
   uint64_t rng_slot;        // first stream slot of the per-SNP tau2 draws
   uint32_t key0, key1;      // chain stream key

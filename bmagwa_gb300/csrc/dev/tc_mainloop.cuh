@@ -4,13 +4,26 @@
 // residual digits of the RB scan, the model columns of the Schur scan).
 //
 // A persistent CTA walks the tiles (tile = blockIdx.x + i gridDim.x, m tile =
-// tile % m_tiles).  Warps 0-3 decode A into the 128-byte-swizzled stage
-// buffers, warp 4 issues the TMA loads of the packed rows and of B, warp 5
-// owns 512 TMEM columns and issues the MMAs of tile i into accumulator i & 1;
+// tile % m_tiles).  Warps 0-3 decode A, warp 4 issues the TMA loads of the
+// packed rows and of B, warp 5 owns 512 TMEM columns and issues the MMAs of
+// tile i into accumulator i & 1;
 // the kernel's own epilogue warps (from warp 6 on) drain the other one and
 // hand it back through acc_empty.  Every wait is bounded; a timeout sets
 // abort_flag and every role leaves its loop after draining its own
 // asynchronous work.
+//
+// A is staged in one of two places:
+//  - tensor memory (a_tmem): the decode warps write each stage's 128 x 64
+//    bf16 block into one of a_stages slots of 32 TMEM columns after the two
+//    accumulators, and the MMA reads A from there.  Shared memory then
+//    carries only B and the packed codes (the main loop is bound by
+//    shared-memory bandwidth and by the latency of the TMA loads), so its
+//    ring can be deeper than the TMEM ring.  Slot g % a_stages is free once
+//    the MMA of stage g - a_stages has completed: the decode waits for that
+//    stage's empty_bar phase, which cannot have moved on before stage g is
+//    decoded (a later phase needs the MMA of stage g - a_stages + stages);
+//  - shared memory, 128-byte swizzled, when the accumulators leave no room
+//    (more than 192 columns each, as in the Schur scan of large models).
 #ifndef BMG_TC_MAINLOOP_CUH_
 #define BMG_TC_MAINLOOP_CUH_
 
@@ -19,11 +32,13 @@
 
 namespace {
 
-constexpr int TC_MAX_STAGES = 4;
+constexpr int TC_MAX_STAGES = 8;    // shared-memory ring (B and packed codes)
+constexpr int TC_MAX_A_STAGES = 4;  // TMEM ring of A when A is in tensor memory
 constexpr int TC_BM = 128;          // rows of D per tile
 constexpr int TC_BK = 64;           // individuals per stage (128 bytes of bf16)
-constexpr uint32_t TC_ACC_COLS = 256;  // columns of one accumulator
-constexpr uint32_t TC_TMEM_COLS = 512; // two accumulators
+constexpr uint32_t TC_ACC_COLS = 256;  // widest accumulator
+constexpr uint32_t TC_TMEM_COLS = 512; // two accumulators (+ the A stages)
+constexpr uint32_t TC_A_COLS = TC_BK / 2;  // TMEM columns of one A stage
 
 struct TcParams {
   uint32_t tpad;           // rows per SNP (terms rounded up to 1, 2 or 4)
@@ -31,14 +46,38 @@ struct TcParams {
   uint32_t chains_tile;    // chains per N tile
   uint32_t n_mma;          // N of the MMA (chains_tile * L rounded up to 16)
   uint32_t k_chunks;       // n_pad / TC_BK
-  uint32_t stages;         // pipeline depth (2..TC_MAX_STAGES)
+  uint32_t stages;         // shared-memory ring depth (2..TC_MAX_STAGES)
+  uint32_t a_stages;       // A ring depth: TMEM slots (a_tmem), else = stages
   uint32_t m_tiles, n_tiles, tiles;
   uint32_t xr_bytes;       // epilogue shared memory after the stages
   uint32_t b_rows_per_tile;  // B rows between consecutive N tiles
   uint32_t stage_bytes;
-  uint32_t b_bytes, a_bytes, pk_bytes;
+  uint32_t b_bytes, a_bytes, pk_bytes;  // a_bytes = 0 when A is in TMEM
+  uint32_t acc_cols;       // TMEM column stride of the two accumulators
+  uint32_t a_tmem;         // 1: A stage st at TMEM column 2 acc_cols + st TC_A_COLS
   int32_t term_of_row[4];  // term of row u of a SNP (-1: unused)
 };
+
+// Where the accumulators and A go: A in TMEM when two accumulators of n_mma
+// columns (rounded up to 32) leave room for at least two A slots; else A in
+// shared memory (a_stages is then set to the ring depth by the caller).
+__host__ __device__ inline void tc_place_a(TcParams& P)
+{
+  const uint32_t acc = ((P.n_mma + 31) / 32) * 32;
+  const uint32_t room = TC_TMEM_COLS >= 2 * acc ? (TC_TMEM_COLS - 2 * acc) / TC_A_COLS : 0;
+  const uint32_t st = room < (uint32_t)TC_MAX_A_STAGES ? room : (uint32_t)TC_MAX_A_STAGES;
+  if (st >= 2) {
+    P.a_tmem = 1;
+    P.a_stages = st;
+    P.acc_cols = acc;
+    P.a_bytes = 0;
+  } else {
+    P.a_tmem = 0;
+    P.a_stages = 0;
+    P.acc_cols = TC_ACC_COLS;
+    P.a_bytes = TC_BM * 128;
+  }
+}
 
 
 // barriers and flags of one CTA
@@ -49,28 +88,33 @@ struct TcCtl {
   volatile int abort_flag;
 };
 
+// Decode table of one term: entry x (a nibble of packed codes, two
+// individuals) holds their bf16 values, the first in the low half.  16 entries
+// of 4 bytes sit in 16 distinct banks, so a warp's lookups never conflict.
+// Row TC_LUT_ZERO is all zeros (rows of a SNP beyond its terms).
+constexpr int TC_LUT_ZERO = 4;
+typedef uint32_t TcLut[TC_LUT_ZERO + 1][16];
+
 // All threads: decode tables, barriers, tensor memory.  Returns the TMEM base.
-__device__ __forceinline__ uint32_t tc_setup(const TcParams& P, TcCtl& ctl, uint2 (*lut)[256], int threads,
-                                             int epi_warps)
+__device__ __forceinline__ uint32_t tc_setup(const TcParams& P, TcCtl& ctl, TcLut& lut, int threads, int epi_warps)
 {
   const int tid = threadIdx.x, warp = tid >> 5;
-  // decode tables: bf16 bit patterns of 0, 1, 2 are 0x0000, 0x3F80, 0x4000
-  for (int e = tid; e < 4 * 256; e += threads) {
-    int term = e >> 8, byte = e & 255;
-    uint16_t h[4];
-    for (int q = 0; q < 4; ++q) {
-      int code = (byte >> (2 * q)) & 3;
-      int v = term_value(code, term);
+  // bf16 bit patterns of 0, 1, 2 are 0x0000, 0x3F80, 0x4000
+  for (int e = tid; e < (TC_LUT_ZERO + 1) * 16; e += threads) {
+    const int term = e >> 4, x = e & 15;
+    uint32_t h[2];
+    for (int q = 0; q < 2; ++q) {
+      const int v = term == TC_LUT_ZERO ? 0 : term_value((x >> (2 * q)) & 3, term);
       h[q] = v == 0 ? 0 : (v == 1 ? 0x3F80 : 0x4000);
     }
-    lut[term][byte] = make_uint2((uint32_t)h[0] | ((uint32_t)h[1] << 16), (uint32_t)h[2] | ((uint32_t)h[3] << 16));
+    lut[term][x] = h[0] | (h[1] << 16);
   }
   if (tid == 0) {
     for (uint32_t st = 0; st < P.stages; ++st) {
       mbar_init(&ctl.full_bar[st], 1);
-      mbar_init(&ctl.aready_bar[st], 4);
       mbar_init(&ctl.empty_bar[st], 1);
     }
+    for (uint32_t t = 0; t < P.a_stages; ++t) mbar_init(&ctl.aready_bar[t], 4);
     for (int b = 0; b < 2; ++b) {
       mbar_init(&ctl.acc_full[b], 1);
       mbar_init(&ctl.acc_empty[b], epi_warps);
@@ -91,12 +135,12 @@ __device__ __forceinline__ uint32_t tc_setup(const TcParams& P, TcCtl& ctl, uint
 }
 
 // Warps 0-5: the decode, TMA and MMA roles over this CTA's tiles.
-__device__ __forceinline__ void tc_main_roles(const TcParams& P, TcCtl& ctl, uint2 (*lut)[256], uint8_t* smem,
+__device__ __forceinline__ void tc_main_roles(const TcParams& P, TcCtl& ctl, const TcLut& lut, uint8_t* smem,
                                               uint32_t tmem, uint32_t my_tiles, const CUtensorMap& map_b,
                                               const CUtensorMap& map_g)
 {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const uint32_t nk = P.k_chunks, S = P.stages;
+  const uint32_t nk = P.k_chunks, S = P.stages, SA = P.a_stages;
   uint64_t* full_bar = ctl.full_bar;
   uint64_t* aready_bar = ctl.aready_bar;
   uint64_t* empty_bar = ctl.empty_bar;
@@ -130,17 +174,25 @@ __device__ __forceinline__ void tc_main_roles(const TcParams& P, TcCtl& ctl, uin
         const uint32_t b = i & 1, u = i >> 1;
         if (u >= 1 && !mbar_wait(&ctl.acc_empty[b], (u - 1) & 1)) { ctl.abort_flag = 1; break; }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t d = tmem + b * TC_ACC_COLS;
+        const uint32_t d = tmem + b * P.acc_cols;
         bool ok = true;
         for (uint32_t k = 0; k < nk; ++k) {
-          const uint32_t g = i * nk + k, st = g % S, par = (g / S) & 1;
-          if (!mbar_wait(&full_bar[st], par) || !mbar_wait(&aready_bar[st], par)) { ok = false; break; }
+          const uint32_t g = i * nk + k, st = g % S, par = (g / S) & 1, ta = g % SA;
+          if (!mbar_wait(&full_bar[st], par) || !mbar_wait(&aready_bar[ta], (g / SA) & 1)) { ok = false; break; }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           uint8_t* sp = smem + st * P.stage_bytes;
-          uint64_t bdesc = smem_desc(sp), adesc = smem_desc(sp + P.b_bytes);
+          const uint64_t bdesc = smem_desc(sp);
+          if (P.a_tmem) {
+            const uint32_t at = tmem + 2 * P.acc_cols + ta * TC_A_COLS;
 #pragma unroll
-          for (int kk = 0; kk < TC_BK / 16; ++kk)  // 16 bf16 = 32 bytes = 2 descriptor units
-            mma_bf16(d, adesc + 2 * kk, bdesc + 2 * kk, idesc, (k | kk) != 0);
+            for (int kk = 0; kk < TC_BK / 16; ++kk)  // 16 bf16: 8 TMEM columns of A, 2 descriptor units of B
+              mma_bf16_tmem_a(d, at + 8 * kk, bdesc + 2 * kk, idesc, (k | kk) != 0);
+          } else {
+            const uint64_t adesc = smem_desc(sp + P.b_bytes);
+#pragma unroll
+            for (int kk = 0; kk < TC_BK / 16; ++kk)  // 16 bf16 = 32 bytes = 2 descriptor units
+              mma_bf16(d, adesc + 2 * kk, bdesc + 2 * kk, idesc, (k | kk) != 0);
+          }
           mma_commit(&empty_bar[st]);
         }
         if (!ok) { ctl.abort_flag = 1; break; }
@@ -151,31 +203,47 @@ __device__ __forceinline__ void tc_main_roles(const TcParams& P, TcCtl& ctl, uin
       if (!mbar_wait(&ctl.drain_bar, 0)) ctl.abort_flag = 1;
     }
   } else if (warp < 4) {
-    // decode warps: packed 2-bit codes -> bf16 rows of the swizzled A tile
+    // decode warps: packed 2-bit codes -> bf16 rows of A; thread = row = TMEM lane
     const uint32_t row = tid;  // 0..127
     const uint32_t sl = row / P.tpad, u = row % P.tpad;
-    const int term = P.term_of_row[u];
+    const uint32_t* tl = lut[P.term_of_row[u] >= 0 ? P.term_of_row[u] : TC_LUT_ZERO];
     const uint32_t total = my_tiles * nk;
+    const uint32_t a_lane = tmem + ((uint32_t)(warp * 32) << 16) + 2 * P.acc_cols;
     for (uint32_t g = 0; g < total; ++g) {
-      if (ctl.abort_flag) break;
-      const uint32_t st = g % S, par = (g / S) & 1;
-      if (!mbar_wait(&full_bar[st], par)) { ctl.abort_flag = 1; break; }
+      const uint32_t st = g % S, par = (g / S) & 1, ta = g % SA;
+      // A in shared memory: the TMA of this stage was issued after the MMA of
+      // its previous round completed (empty_bar), so that MMA no longer reads
+      // the stage's A.  A in TMEM: slot ta is free after the MMA of stage
+      // g - SA.  The verdict is warp-uniform: the TMEM store is .sync.aligned.
+      const uint32_t gp = g - SA;
+      const bool ok = !ctl.abort_flag && mbar_wait(&full_bar[st], par) &&
+                      (!P.a_tmem || g < SA || mbar_wait(&empty_bar[gp % S], (gp / S) & 1));
+      if (!__all_sync(0xffffffffu, ok)) { ctl.abort_flag = 1; break; }
       uint8_t* sp = smem + st * P.stage_bytes;
-      uint8_t* a = sp + P.b_bytes;
       const uint8_t* pk = sp + P.b_bytes + P.a_bytes + sl * 16;
-      uint4 bytes = *reinterpret_cast<const uint4*>(pk);
-      uint32_t w[4] = {bytes.x, bytes.y, bytes.z, bytes.w};
+      const uint4 bytes = *reinterpret_cast<const uint4*>(pk);
+      const uint32_t w[4] = {bytes.x, bytes.y, bytes.z, bytes.w};
+      if (P.a_tmem) {
+        // 64 individuals = 32 columns, column q = individuals 2q, 2q + 1
+        uint32_t v[32];
 #pragma unroll
-      for (int c = 0; c < 8; ++c) {
-        uint32_t two = (w[c >> 1] >> ((c & 1) * 16)) & 0xFFFF;
-        uint2 lo = (term >= 0) ? lut[term][two & 255] : make_uint2(0, 0);
-        uint2 hi = (term >= 0) ? lut[term][two >> 8] : make_uint2(0, 0);
-        uint4 v = make_uint4(lo.x, lo.y, hi.x, hi.y);
-        *reinterpret_cast<uint4*>(a + row * 128 + ((c ^ (row & 7)) << 4)) = v;
+        for (int q = 0; q < 32; ++q) v[q] = tl[(w[q >> 3] >> (4 * (q & 7))) & 15];
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        tmem_st32(a_lane + ta * TC_A_COLS, v);
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      } else {
+        uint8_t* a = sp + P.b_bytes;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+          // 16-byte chunk c of the row: individuals 8c .. 8c + 7, 16 bits of codes
+          const uint32_t h = w[c >> 1] >> ((c & 1) * 16);
+          const uint4 v = make_uint4(tl[h & 15], tl[(h >> 4) & 15], tl[(h >> 8) & 15], tl[(h >> 12) & 15]);
+          *reinterpret_cast<uint4*>(a + row * 128 + ((c ^ (row & 7)) << 4)) = v;
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       }
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       __syncwarp();
-      if (lane == 0) mbar_arrive(&aready_bar[st]);
+      if (lane == 0) mbar_arrive(&aready_bar[ta]);
     }
   }
 }

@@ -302,11 +302,26 @@ bmg_status bmg_reset_timings(bmg_ctx* ctx, uint64_t* n_scans);
  * (no counterpart in the reference; a measurement aid). */
 bmg_status bmg_get_launch_count(bmg_ctx* ctx, uint64_t* n_launches);
 
+/* Self-test of the scan's table-driven exp (no counterpart in the reference):
+ * out[i] = exp(a[i]) as the posterior epilogue evaluates it, for host arrays
+ * of n arguments with |a[i]| <= 700 (others give BMG_EINVAL).  Uses the
+ * current CUDA device and allocates 16 n bytes there for the call. */
+bmg_status bmg_selftest_exp(const double* a, double* out, size_t n);
+
 /* Launch shape of the tensor-core scan (no counterpart in the reference).
  * The first scans of a context time each shape once and keep the fastest;
  * every shape gives the same results bit for bit.  variant is -1 while
  * tuning; BMG_SCAN_VARIANT=<i> in the environment at bmg_create fixes it. */
 bmg_status bmg_get_scan_shape(bmg_ctx* ctx, int32_t* variant, char* name, size_t name_len);
+
+/* The tuner's time of each launch shape (no counterpart in the reference):
+ * ms[i] = the fastest of its tuning scans in milliseconds, -1 if not timed
+ * (yet).  Writes min(n, shapes) entries; *n_shapes (may be NULL) receives
+ * the number of shapes. */
+bmg_status bmg_get_scan_tuning(bmg_ctx* ctx, float* ms, int32_t n, int32_t* n_shapes);
+
+/* Description of launch shape `shape` (0 .. n_shapes - 1). */
+bmg_status bmg_get_scan_shape_name(int32_t shape, char* name, size_t name_len);
 
 /* Per-SNP precomputed sums, allocating nothing (no counterpart in the
  * reference).  For callers that cannot call cudaMalloc, e.g. code running in

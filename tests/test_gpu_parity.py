@@ -163,10 +163,12 @@ def test_setup_is_ordered_against_a_busy_default_stream(bmg, tmp_path):
 @pytest.mark.parametrize("name,types", [("plain", None), ("batched", None)])
 def test_every_scan_shape_gives_the_same_results(bmg, tmp_path, monkeypatch, name, types):
     """The launch shapes the scan's autotuner chooses between (epilogue warps,
-    chains per tile) agree with each other and with the SIMT scan bit for bit."""
+    chains per tile, ring depth) agree with each other and with the SIMT scan
+    bit for bit."""
     opt, packed, y, e = synth_case(bmg, tmp_path, name, n=640, p=2000, chains=3, iters=40, n_rao=2)
     ref = None
-    shapes = list(range(4)) + ["simt"]
+    shapes = list(range(len(bmg.scan_shapes()))) + ["simt"]
+    assert len(shapes) >= 7
     for v in shapes:
         if v == "simt":
             monkeypatch.delenv("BMG_SCAN_VARIANT", raising=False)
@@ -335,3 +337,20 @@ def test_several_phenotypes_match_the_oracle_on_their_samples(bmg, oracle, tmp_p
         H.compare(a, b, rtol=RTOL, label="phenotype %d" % k)
         np.testing.assert_allclose(ctx.rao(k)[0], port.rao(0)[0], rtol=RTOL, atol=1e-12)
     ctx.close()
+
+
+def test_table_exp_of_the_scan_epilogue(bmg):
+    """The scan's table-driven exp (Tang's method, 256-entry table) against
+    the host's exp: within 4 ulp over [-700, 700], including the points next
+    to the table's break points."""
+    rng = np.random.default_rng(11)
+    step = np.log(2.0) / 256
+    k = rng.integers(-258000, 258000, 200000)
+    near = k * step + rng.uniform(-1, 1, k.size) * step * 1e-6
+    a = np.concatenate([rng.uniform(-700, 700, 300000), rng.uniform(-40, 40, 300000), near,
+                        np.linspace(-700, 700, 100001)])
+    a = a[np.abs(a) <= 700]
+    got = bmg.selftest_exp(a)
+    ref = np.exp(a)
+    ulp = np.abs(got - ref) / np.spacing(ref)
+    assert ulp.max() <= 4, (ulp.max(), a[np.argmax(ulp)])
