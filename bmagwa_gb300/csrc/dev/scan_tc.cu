@@ -74,7 +74,7 @@ bmg_scan_tc_kernel(DevConst K, TcParams P, const __grid_constant__ CUtensorMap m
       const uint32_t snp0 = (tile % P.m_tiles) * P.snps_per_tile;
       const uint32_t chain0 = (tile / P.m_tiles) * ct;
       const uint32_t chains_here = min(ct, K.n_chains - chain0);
-      const uint32_t b = i & 1, u = i >> 1;
+      const uint32_t b = i % P.n_acc, u = i / P.n_acc;
       // one warp waits; the verdict is shared so that all epilogue warps take
       // the same number of named-barrier steps
       if (e == 0) {
@@ -181,7 +181,7 @@ static size_t tc_smem_bytes(const TcParams& P)
 // static shared memory of the kernel (decode tables and barriers) is below 2 KB
 constexpr size_t TC_SMEM_LIMIT = 227 * 1024 - 2 * 1024;
 
-static bool tc_plan(const DevConst* K, TcParams* P, uint32_t ct_cap, uint32_t stages_cap)
+static bool tc_plan(const DevConst* K, TcParams* P, uint32_t ct_cap, uint32_t n_acc)
 {
   uint32_t T = K->n_terms;
   P->tpad = T <= 1 ? 1 : (T <= 2 ? 2 : 4);
@@ -190,22 +190,20 @@ static bool tc_plan(const DevConst* K, TcParams* P, uint32_t ct_cap, uint32_t st
   const uint32_t L = K->limbs_n;
   if (K->n_pad % TC_BK != 0 || K->n >= 65536) return false;  // exact FP32 sums need n < 2^16
   P->k_chunks = K->n_pad / TC_BK;
-  P->pk_bytes = P->snps_per_tile * 16;
+  P->pk_bytes = P->snps_per_tile * (TC_BK / 4);
   // widest chain tile whose accumulator fits one TMEM buffer and whose stages
   // (at least two) and sums fit shared memory
   for (uint32_t ct = std::min(std::min(K->n_chains, TC_ACC_COLS / L), std::max(1u, ct_cap)); ct >= 1; --ct) {
     P->chains_tile = ct;
     P->n_mma = ((ct * L + 15) / 16) * 16;
     if (P->n_mma > TC_ACC_COLS || P->n_mma < 16) continue;
-    P->b_bytes = P->n_mma * 128;
-    tc_place_a(*P);
+    P->b_bytes = P->n_mma * TC_BK * 2;  // two 128-byte-swizzled boxes of 64 individuals
+    tc_place_a(*P, n_acc);
     P->stage_bytes = ((P->b_bytes + P->a_bytes + P->pk_bytes + 1023) / 1024) * 1024;
     P->xr_bytes = TC_BM * (ct + 1) * 8;
     P->b_rows_per_tile = ct * L;
-    const uint32_t st_max = stages_cap >= 2 && stages_cap < (uint32_t)TC_MAX_STAGES ? stages_cap : TC_MAX_STAGES;
-    for (uint32_t st = st_max; st >= 2; --st) {
-      P->stages = st;
-      if (!P->a_tmem) P->a_stages = st;
+    for (uint32_t st = TC_MAX_STAGES; st >= 2; --st) {
+      tc_set_rings(*P, st);
       if (tc_smem_bytes(*P) <= TC_SMEM_LIMIT) {
         P->m_tiles = (uint32_t)((K->p + P->snps_per_tile - 1) / P->snps_per_tile);
         P->n_tiles = (K->n_chains + ct - 1) / ct;
@@ -218,16 +216,16 @@ static bool tc_plan(const DevConst* K, TcParams* P, uint32_t ct_cap, uint32_t st
 }
 
 // Launch shapes the autotuner chooses between: epilogue warps, a cap on the
-// chains of one N tile, and a cap on the depth of the shared-memory ring (a
-// deeper ring hides more TMA latency but leaves less of the SM's L1 to the
-// epilogue's loads).  All of them compute the same exact sums and the same
-// posterior, bit for bit.
+// chains of one N tile, and the number of TMEM accumulators (two overlap the
+// epilogue's copy-out with the next tile's MMAs; one leaves ten A slots
+// instead of four, a deeper decode ring).  All of them compute the same exact
+// sums and the same posterior, bit for bit.
 struct TcVariant {
   int epi;
-  int ct_div;      // chains per tile = ceil(chains / ct_div)
-  int stages_cap;  // 0: as many stages as shared memory holds
+  int ct_div;  // chains per tile = ceil(chains / ct_div)
+  int n_acc;   // TMEM accumulators
 };
-static const TcVariant kTcVariants[] = {{12, 1, 0}, {8, 1, 0}, {12, 2, 0}, {8, 2, 0}, {12, 1, 4}, {8, 1, 4}};
+static const TcVariant kTcVariants[] = {{12, 1, 2}, {8, 1, 2}, {12, 2, 2}, {8, 2, 2}, {12, 1, 1}, {8, 1, 1}};
 constexpr int kTcVariantCount = sizeof(kTcVariants) / sizeof(kTcVariants[0]);
 
 extern "C" int bmg_scan_tc_variants() { return kTcVariantCount; }
@@ -235,8 +233,8 @@ extern "C" int bmg_scan_tc_variants() { return kTcVariantCount; }
 extern "C" void bmg_scan_tc_variant_name(int v, char* buf, size_t len)
 {
   if (v < 0 || v >= kTcVariantCount) v = 0;
-  snprintf(buf, len, "epilogue_warps=%d chains_per_tile=1/%d ring=%s", kTcVariants[v].epi, kTcVariants[v].ct_div,
-           kTcVariants[v].stages_cap ? "4" : "max");
+  snprintf(buf, len, "epilogue_warps=%d chains_per_tile=1/%d accumulators=%d", kTcVariants[v].epi,
+           kTcVariants[v].ct_div, kTcVariants[v].n_acc);
 }
 
 static uint32_t tc_cap(const DevConst* K, int v)
@@ -248,7 +246,7 @@ static uint32_t tc_cap(const DevConst* K, int v)
 extern "C" int bmg_scan_tc_supported(const DevConst* K)
 {
   TcParams P;
-  if (!tc_plan(K, &P, K->n_chains, 0) || !encode_fn()) return 0;
+  if (!tc_plan(K, &P, K->n_chains, 2) || !encode_fn()) return 0;
   int dev = 0, major = 0, minor = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
@@ -284,14 +282,14 @@ extern "C" int bmg_scan_tc_launch(const DevConst* K, cudaStream_t stream, int va
 {
   if (variant < 0 || variant >= kTcVariantCount) variant = 0;
   TcParams P;
-  if (!tc_plan(K, &P, tc_cap(K, variant), (uint32_t)kTcVariants[variant].stages_cap)) return 1;
+  if (!tc_plan(K, &P, tc_cap(K, variant), (uint32_t)kTcVariants[variant].n_acc)) return 1;
   auto enc = encode_fn();
   if (!enc) return 2;
   CUtensorMap mb, mg;
   {
     cuuint64_t dims[2] = {K->n_pad, (cuuint64_t)K->n_chains * K->limbs_n};
     cuuint64_t strides[1] = {(cuuint64_t)K->n_pad * 2};
-    cuuint32_t box[2] = {TC_BK, P.n_mma};
+    cuuint32_t box[2] = {TC_BK_SUB, P.n_mma};
     cuuint32_t es[2] = {1, 1};
     if (enc(&mb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void*)K->limbs, dims, strides, box, es,
             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -301,7 +299,7 @@ extern "C" int bmg_scan_tc_launch(const DevConst* K, cudaStream_t stream, int va
   {
     cuuint64_t dims[2] = {K->gs, K->p};
     cuuint64_t strides[1] = {K->gs};
-    cuuint32_t box[2] = {16, P.snps_per_tile};
+    cuuint32_t box[2] = {TC_BK / 4, P.snps_per_tile};
     cuuint32_t es[2] = {1, 1};
     if (enc(&mg, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, (void*)K->geno, dims, strides, box, es,
             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,

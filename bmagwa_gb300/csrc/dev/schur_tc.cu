@@ -127,7 +127,7 @@ bmg_schur_tc_kernel(DevConst K, TcParams P, uint32_t KB, uint32_t n_terms, doubl
       const uint32_t tile = blockIdx.x + i * gridDim.x;
       const uint32_t snp0 = (tile % P.m_tiles) * P.snps_per_tile;
       const uint32_t chain0 = (tile / P.m_tiles) * ct;
-      const uint32_t b = i & 1, u = i >> 1;
+      const uint32_t b = i % P.n_acc, u = i / P.n_acc;
       if (e == 0) {
         bool ok = false;
         if (lane == 0) ok = !ctl.abort_flag && mbar_wait(&ctl.acc_full[b], u & 1);
@@ -200,14 +200,15 @@ extern "C" int bmg_schur_launch(const DevConst* K, const int* xcols, uint16_t** 
   P.snps_per_tile = TC_BM / P.tpad;
   for (uint32_t u = 0; u < 4; ++u) P.term_of_row[u] = (u < T) ? K->term_of[u] : -1;
   P.k_chunks = K->n_pad / TC_BK;
-  P.a_bytes = TC_BM * 128;  // A in shared memory: the accumulators may take all 512 columns
+  P.a_bytes = 2 * TC_A_SUB_BYTES;  // A in shared memory: the accumulators may take all 512 columns
   P.a_tmem = 0;
   P.a_stages = 0;
+  P.n_acc = 2;
   P.acc_cols = TC_ACC_COLS;
-  P.pk_bytes = P.snps_per_tile * 16;
+  P.pk_bytes = P.snps_per_tile * (TC_BK / 4);
   P.chains_tile = std::max(1u, std::min(C, TC_ACC_COLS / KB));
   P.n_mma = P.chains_tile * KB;
-  P.b_bytes = P.n_mma * 128;
+  P.b_bytes = P.n_mma * TC_BK * 2;  // two 128-byte-swizzled boxes of 64 individuals
   P.stage_bytes = ((P.b_bytes + P.a_bytes + P.pk_bytes + 1023) / 1024) * 1024;
   P.xr_bytes = 0;
   P.b_rows_per_tile = P.chains_tile * KB;
@@ -215,7 +216,7 @@ extern "C" int bmg_schur_launch(const DevConst* K, const int* xcols, uint16_t** 
   for (uint32_t st = TC_MAX_STAGES; st >= 2 && !P.stages; --st)
     if ((size_t)st * P.stage_bytes + 1024 <= 227 * 1024 - 9 * 1024) P.stages = st;
   if (!P.stages) return 2;
-  P.a_stages = P.stages;
+  tc_set_rings(P, P.stages);
   P.m_tiles = (uint32_t)((K->p + P.snps_per_tile - 1) / P.snps_per_tile);
   P.n_tiles = (C + P.chains_tile - 1) / P.chains_tile;
   P.tiles = P.m_tiles * P.n_tiles;
@@ -236,7 +237,7 @@ extern "C" int bmg_schur_launch(const DevConst* K, const int* xcols, uint16_t** 
   {
     cuuint64_t dims[2] = {K->n_pad, (cuuint64_t)C * KB};
     cuuint64_t strides[1] = {(cuuint64_t)K->n_pad * 2};
-    cuuint32_t box[2] = {TC_BK, P.n_mma};
+    cuuint32_t box[2] = {TC_BK_SUB, P.n_mma};
     cuuint32_t es[2] = {1, 1};
     if (enc(&mb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void*)*bm, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
             CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -246,7 +247,7 @@ extern "C" int bmg_schur_launch(const DevConst* K, const int* xcols, uint16_t** 
   {
     cuuint64_t dims[2] = {K->gs, K->p};
     cuuint64_t strides[1] = {K->gs};
-    cuuint32_t box[2] = {16, P.snps_per_tile};
+    cuuint32_t box[2] = {TC_BK / 4, P.snps_per_tile};
     cuuint32_t es[2] = {1, 1};
     if (enc(&mg, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, (void*)K->geno, dims, strides, box, es,
             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,

@@ -1,29 +1,37 @@
 // The main loop shared by the tensor-core scans: D = A . B' on tcgen05 with
-// A the 0/1/2 codings of 128 (SNP, term) rows, decoded in shared memory from
-// the packed 2-bit codes, and B any bf16 matrix of n_pad columns (the
-// residual digits of the RB scan, the model columns of the Schur scan).
+// A the 0/1/2 codings of 128 (SNP, term) rows, decoded from the packed 2-bit
+// codes, and B any bf16 matrix of n_pad columns (the residual digits of the
+// RB scan, the model columns of the Schur scan).
 //
 // A persistent CTA walks the tiles (tile = blockIdx.x + i gridDim.x, m tile =
 // tile % m_tiles).  Warps 0-3 decode A, warp 4 issues the TMA loads of the
 // packed rows and of B, warp 5 owns 512 TMEM columns and issues the MMAs of
-// tile i into accumulator i & 1;
-// the kernel's own epilogue warps (from warp 6 on) drain the other one and
-// hand it back through acc_empty.  Every wait is bounded; a timeout sets
-// abort_flag and every role leaves its loop after draining its own
-// asynchronous work.
+// tile i into accumulator i % n_acc; the kernel's own epilogue warps (from
+// warp 6 on) copy a finished accumulator out of TMEM and hand it back through
+// acc_empty.  Every wait is bounded; a timeout sets abort_flag and every role
+// leaves its loop after draining its own asynchronous work.
+//
+// Rings.  Stage g (128 individuals: chunk g of the CTA's walk over its tiles'
+// K ranges) uses shared-memory slot
+// g % stages (B and the packed codes, loaded by TMA, full_bar) and A slot
+// g % a_stages (aready_bar).  The MMA of stage g commits to done_bar[g % ring],
+// ring = max(stages, a_stages): the TMA waits for the MMA of stage g - stages
+// before refilling a shared-memory slot, the decode for that of stage
+// g - a_stages before rewriting an A slot in TMEM.  Neither phase can have
+// moved on by then (a later phase of the same barrier needs the MMA of a
+// stage >= g, which needs this stage first), so parity waits are exact.
 //
 // A is staged in one of two places:
-//  - tensor memory (a_tmem): the decode warps write each stage's 128 x 64
-//    bf16 block into one of a_stages slots of 32 TMEM columns after the two
-//    accumulators, and the MMA reads A from there.  Shared memory then
-//    carries only B and the packed codes (the main loop is bound by
-//    shared-memory bandwidth and by the latency of the TMA loads), so its
-//    ring can be deeper than the TMEM ring.  Slot g % a_stages is free once
-//    the MMA of stage g - a_stages has completed: the decode waits for that
-//    stage's empty_bar phase, which cannot have moved on before stage g is
-//    decoded (a later phase needs the MMA of stage g - a_stages + stages);
-//  - shared memory, 128-byte swizzled, when the accumulators leave no room
-//    (more than 192 columns each, as in the Schur scan of large models).
+//  - tensor memory (a_tmem): each stage's 128 x 128 bf16 block goes into 64
+//    TMEM columns after the accumulators, and the MMA reads A from there.
+//    Shared memory then carries only B and the packed codes (the main loop is
+//    bound by shared-memory bandwidth and by latency).  With one accumulator
+//    (n_acc = 1) five A slots fit; the epilogue copies the accumulator to
+//    shared memory within microseconds and does its arithmetic from there
+//    while the next tile accumulates, so one accumulator costs little overlap;
+//  - shared memory, two 128-byte-swizzled sub-tiles of 64 individuals, when
+//    the accumulators leave no room (the Schur scan of large models).
+// B likewise arrives as two TMA boxes of 64 individuals per stage.
 #ifndef BMG_TC_MAINLOOP_CUH_
 #define BMG_TC_MAINLOOP_CUH_
 
@@ -32,13 +40,16 @@
 
 namespace {
 
-constexpr int TC_MAX_STAGES = 8;    // shared-memory ring (B and packed codes)
-constexpr int TC_MAX_A_STAGES = 4;  // TMEM ring of A when A is in tensor memory
-constexpr int TC_BM = 128;          // rows of D per tile
-constexpr int TC_BK = 64;           // individuals per stage (128 bytes of bf16)
-constexpr uint32_t TC_ACC_COLS = 256;  // widest accumulator
-constexpr uint32_t TC_TMEM_COLS = 512; // two accumulators (+ the A stages)
-constexpr uint32_t TC_A_COLS = TC_BK / 2;  // TMEM columns of one A stage
+constexpr int TC_MAX_STAGES = 8;     // shared-memory ring (B and packed codes)
+constexpr int TC_MAX_A_STAGES = 10;  // TMEM ring of A when A is in tensor memory
+constexpr int TC_MAX_RING = 10;      // done_bar ring: max(stages, a_stages)
+constexpr int TC_BM = 128;           // rows of D per tile
+constexpr int TC_BK = 128;           // individuals per stage
+constexpr int TC_BK_SUB = 64;        // individuals per 128-byte swizzle atom (one TMA box of B)
+constexpr uint32_t TC_ACC_COLS = 256;   // widest accumulator
+constexpr uint32_t TC_TMEM_COLS = 512;  // accumulators + the A slots
+constexpr uint32_t TC_A_COLS = TC_BK / 2;  // TMEM columns of one A slot (two bf16 per column)
+constexpr uint32_t TC_A_SUB_BYTES = TC_BM * 128;  // one swizzled A sub-tile in shared memory
 
 struct TcParams {
   uint32_t tpad;           // rows per SNP (terms rounded up to 1, 2 or 4)
@@ -48,41 +59,66 @@ struct TcParams {
   uint32_t k_chunks;       // n_pad / TC_BK
   uint32_t stages;         // shared-memory ring depth (2..TC_MAX_STAGES)
   uint32_t a_stages;       // A ring depth: TMEM slots (a_tmem), else = stages
+  uint32_t ring;           // done_bar ring depth, max(stages, a_stages)
   uint32_t m_tiles, n_tiles, tiles;
   uint32_t xr_bytes;       // epilogue shared memory after the stages
   uint32_t b_rows_per_tile;  // B rows between consecutive N tiles
   uint32_t stage_bytes;
-  uint32_t b_bytes, a_bytes, pk_bytes;  // a_bytes = 0 when A is in TMEM
-  uint32_t acc_cols;       // TMEM column stride of the two accumulators
-  uint32_t a_tmem;         // 1: A stage st at TMEM column 2 acc_cols + st TC_A_COLS
+  uint32_t b_bytes, a_bytes, pk_bytes;  // a_bytes = 0 when A is in TMEM; B and A in two sub-tiles
+  uint32_t n_acc;          // accumulators (1 or 2)
+  uint32_t acc_cols;       // TMEM column stride of the accumulators
+  uint32_t a_tmem;         // 1: A slot t at TMEM column n_acc acc_cols + t TC_A_COLS
   int32_t term_of_row[4];  // term of row u of a SNP (-1: unused)
 };
 
-// Where the accumulators and A go: A in TMEM when two accumulators of n_mma
+// Where the accumulators and A go: A in TMEM when n_acc accumulators of n_mma
 // columns (rounded up to 32) leave room for at least two A slots; else A in
-// shared memory (a_stages is then set to the ring depth by the caller).
-__host__ __device__ inline void tc_place_a(TcParams& P)
+// shared memory with two accumulators of TC_ACC_COLS.
+__host__ __device__ inline void tc_place_a(TcParams& P, uint32_t n_acc)
 {
   const uint32_t acc = ((P.n_mma + 31) / 32) * 32;
-  const uint32_t room = TC_TMEM_COLS >= 2 * acc ? (TC_TMEM_COLS - 2 * acc) / TC_A_COLS : 0;
+  const uint32_t used = n_acc * acc;
+  const uint32_t room = TC_TMEM_COLS > used ? (TC_TMEM_COLS - used) / TC_A_COLS : 0;
   const uint32_t st = room < (uint32_t)TC_MAX_A_STAGES ? room : (uint32_t)TC_MAX_A_STAGES;
   if (st >= 2) {
     P.a_tmem = 1;
     P.a_stages = st;
+    P.n_acc = n_acc;
     P.acc_cols = acc;
     P.a_bytes = 0;
   } else {
     P.a_tmem = 0;
     P.a_stages = 0;
+    P.n_acc = 2;
     P.acc_cols = TC_ACC_COLS;
-    P.a_bytes = TC_BM * 128;
+    P.a_bytes = 2 * TC_A_SUB_BYTES;
   }
 }
 
+// Once the shared-memory ring depth is known: A slots and the done ring.
+__host__ __device__ inline void tc_set_rings(TcParams& P, uint32_t stages)
+{
+  P.stages = stages;
+  if (!P.a_tmem) P.a_stages = stages;
+  P.ring = P.stages > P.a_stages ? P.stages : P.a_stages;
+}
+
+// position in a ring of n slots: slot index and phase parity, advanced
+// without divisions
+struct TcRing {
+  uint32_t i = 0, ph = 0;
+  __device__ __forceinline__ void next(uint32_t n)
+  {
+    if (++i == n) {
+      i = 0;
+      ph ^= 1;
+    }
+  }
+};
 
 // barriers and flags of one CTA
 struct TcCtl {
-  uint64_t full_bar[TC_MAX_STAGES], aready_bar[TC_MAX_STAGES], empty_bar[TC_MAX_STAGES];
+  uint64_t full_bar[TC_MAX_STAGES], aready_bar[TC_MAX_RING], done_bar[TC_MAX_RING];
   uint64_t acc_full[2], acc_empty[2], drain_bar;
   uint32_t tmem_base;
   volatile int abort_flag;
@@ -110,11 +146,9 @@ __device__ __forceinline__ uint32_t tc_setup(const TcParams& P, TcCtl& ctl, TcLu
     lut[term][x] = h[0] | (h[1] << 16);
   }
   if (tid == 0) {
-    for (uint32_t st = 0; st < P.stages; ++st) {
-      mbar_init(&ctl.full_bar[st], 1);
-      mbar_init(&ctl.empty_bar[st], 1);
-    }
+    for (uint32_t st = 0; st < P.stages; ++st) mbar_init(&ctl.full_bar[st], 1);
     for (uint32_t t = 0; t < P.a_stages; ++t) mbar_init(&ctl.aready_bar[t], 4);
+    for (uint32_t r = 0; r < P.ring; ++r) mbar_init(&ctl.done_bar[r], 1);
     for (int b = 0; b < 2; ++b) {
       mbar_init(&ctl.acc_full[b], 1);
       mbar_init(&ctl.acc_empty[b], epi_warps);
@@ -140,60 +174,79 @@ __device__ __forceinline__ void tc_main_roles(const TcParams& P, TcCtl& ctl, con
                                               const CUtensorMap& map_g)
 {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const uint32_t nk = P.k_chunks, S = P.stages, SA = P.a_stages;
+  const uint32_t nk = P.k_chunks, S = P.stages, SA = P.a_stages, R = P.ring;
   uint64_t* full_bar = ctl.full_bar;
   uint64_t* aready_bar = ctl.aready_bar;
-  uint64_t* empty_bar = ctl.empty_bar;
+  uint64_t* done_bar = ctl.done_bar;
   if (warp == 4) {
     if (lane == 0) {
       // TMA producer: packed genotype rows and the B rows of each stage
       uint32_t issued = 0;
+      TcRing slot, done;  // this stage's shared-memory slot; the done phase of stage g - S
+      const uint32_t b_half = P.b_bytes / 2;
       for (uint32_t i = 0; i < my_tiles && !ctl.abort_flag; ++i) {
         const uint32_t tile = blockIdx.x + i * gridDim.x;
         const uint32_t snp0 = (tile % P.m_tiles) * P.snps_per_tile;
         const uint32_t brow0 = (tile / P.m_tiles) * P.b_rows_per_tile;
+        bool ok = true;
         for (uint32_t k = 0; k < nk; ++k) {
-          const uint32_t g = i * nk + k, st = g % S;
-          if (g >= S && !mbar_wait(&empty_bar[st], ((g / S) - 1) & 1)) { ctl.abort_flag = 1; break; }
-          uint8_t* sp = smem + st * P.stage_bytes;
-          mbar_arrive_tx(&full_bar[st], P.b_bytes + P.pk_bytes);
-          tma_load_2d(sp, &map_b, &full_bar[st], (int)(k * TC_BK), (int)brow0);
-          tma_load_2d(sp + P.b_bytes + P.a_bytes, &map_g, &full_bar[st], (int)(k * (TC_BK / 4)), (int)snp0);
+          if (issued >= S) {  // the slot's last reader is the MMA of stage g - S
+            if (!mbar_wait(&done_bar[done.i], done.ph)) { ok = false; break; }
+            done.next(R);
+          }
+          uint8_t* sp = smem + slot.i * P.stage_bytes;
+          uint64_t* fb = &full_bar[slot.i];
+          mbar_arrive_tx(fb, P.b_bytes + P.pk_bytes);
+          tma_load_2d(sp, &map_b, fb, (int)(k * TC_BK), (int)brow0);
+          tma_load_2d(sp + b_half, &map_b, fb, (int)(k * TC_BK + TC_BK_SUB), (int)brow0);
+          tma_load_2d(sp + P.b_bytes + P.a_bytes, &map_g, fb, (int)(k * (TC_BK / 4)), (int)snp0);
+          slot.next(S);
           ++issued;
         }
+        if (!ok) { ctl.abort_flag = 1; break; }
       }
       // no load may still be landing in shared memory when the CTA exits:
-      // wait (bounded) for the last load of every stage
+      // wait (bounded) for the last load of every slot
       for (uint32_t g = issued > S ? issued - S : 0; g < issued; ++g) mbar_wait(&full_bar[g % S], (g / S) & 1);
     }
   } else if (warp == 5) {
     if (lane == 0) {
-      // MMA issuer: tile i accumulates into buffer i & 1
+      // MMA issuer: tile i accumulates into buffer i % n_acc
       const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((P.n_mma >> 3) << 17) | ((uint32_t)(TC_BM >> 4) << 24);
+      const uint32_t a_base = tmem + P.n_acc * P.acc_cols;
+      const uint32_t b_half = P.b_bytes / 2;
+      TcRing full, aslot;  // this stage's shared-memory slot and A slot
+      uint32_t dn = 0;     // done_bar slot of this stage
       for (uint32_t i = 0; i < my_tiles && !ctl.abort_flag; ++i) {
-        const uint32_t b = i & 1, u = i >> 1;
+        const uint32_t b = i % P.n_acc, u = i / P.n_acc;
         if (u >= 1 && !mbar_wait(&ctl.acc_empty[b], (u - 1) & 1)) { ctl.abort_flag = 1; break; }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t d = tmem + b * P.acc_cols;
         bool ok = true;
         for (uint32_t k = 0; k < nk; ++k) {
-          const uint32_t g = i * nk + k, st = g % S, par = (g / S) & 1, ta = g % SA;
-          if (!mbar_wait(&full_bar[st], par) || !mbar_wait(&aready_bar[ta], (g / SA) & 1)) { ok = false; break; }
+          if (!mbar_wait(&full_bar[full.i], full.ph) || !mbar_wait(&aready_bar[aslot.i], aslot.ph)) {
+            ok = false;
+            break;
+          }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-          uint8_t* sp = smem + st * P.stage_bytes;
-          const uint64_t bdesc = smem_desc(sp);
+          uint8_t* sp = smem + full.i * P.stage_bytes;
           if (P.a_tmem) {
-            const uint32_t at = tmem + 2 * P.acc_cols + ta * TC_A_COLS;
+            const uint32_t at = a_base + aslot.i * TC_A_COLS;
 #pragma unroll
             for (int kk = 0; kk < TC_BK / 16; ++kk)  // 16 bf16: 8 TMEM columns of A, 2 descriptor units of B
-              mma_bf16_tmem_a(d, at + 8 * kk, bdesc + 2 * kk, idesc, (k | kk) != 0);
+              mma_bf16_tmem_a(d, at + 8 * kk, smem_desc(sp + (kk >> 2) * b_half) + 2 * (kk & 3), idesc,
+                              (k | kk) != 0);
           } else {
-            const uint64_t adesc = smem_desc(sp + P.b_bytes);
+            uint8_t* a = sp + P.b_bytes;
 #pragma unroll
             for (int kk = 0; kk < TC_BK / 16; ++kk)  // 16 bf16 = 32 bytes = 2 descriptor units
-              mma_bf16(d, adesc + 2 * kk, bdesc + 2 * kk, idesc, (k | kk) != 0);
+              mma_bf16(d, smem_desc(a + (kk >> 2) * TC_A_SUB_BYTES) + 2 * (kk & 3),
+                       smem_desc(sp + (kk >> 2) * b_half) + 2 * (kk & 3), idesc, (k | kk) != 0);
           }
-          mma_commit(&empty_bar[st]);
+          mma_commit(&done_bar[dn]);
+          if (++dn == R) dn = 0;
+          full.next(S);
+          aslot.next(SA);
         }
         if (!ok) { ctl.abort_flag = 1; break; }
         mma_commit(&ctl.acc_full[b]);
@@ -208,42 +261,59 @@ __device__ __forceinline__ void tc_main_roles(const TcParams& P, TcCtl& ctl, con
     const uint32_t sl = row / P.tpad, u = row % P.tpad;
     const uint32_t* tl = lut[P.term_of_row[u] >= 0 ? P.term_of_row[u] : TC_LUT_ZERO];
     const uint32_t total = my_tiles * nk;
-    const uint32_t a_lane = tmem + ((uint32_t)(warp * 32) << 16) + 2 * P.acc_cols;
+    const uint32_t a_lane = tmem + ((uint32_t)(warp * 32) << 16) + P.n_acc * P.acc_cols;
+    TcRing full, aslot, done;  // this stage's slots; the done phase of stage g - SA
     for (uint32_t g = 0; g < total; ++g) {
-      const uint32_t st = g % S, par = (g / S) & 1, ta = g % SA;
-      // A in shared memory: the TMA of this stage was issued after the MMA of
-      // its previous round completed (empty_bar), so that MMA no longer reads
-      // the stage's A.  A in TMEM: slot ta is free after the MMA of stage
-      // g - SA.  The verdict is warp-uniform: the TMEM store is .sync.aligned.
-      const uint32_t gp = g - SA;
-      const bool ok = !ctl.abort_flag && mbar_wait(&full_bar[st], par) &&
-                      (!P.a_tmem || g < SA || mbar_wait(&empty_bar[gp % S], (gp / S) & 1));
-      if (!__all_sync(0xffffffffu, ok)) { ctl.abort_flag = 1; break; }
-      uint8_t* sp = smem + st * P.stage_bytes;
-      const uint8_t* pk = sp + P.b_bytes + P.a_bytes + sl * 16;
-      const uint4 bytes = *reinterpret_cast<const uint4*>(pk);
-      const uint32_t w[4] = {bytes.x, bytes.y, bytes.z, bytes.w};
+      // A in shared memory: the TMA of this stage waited for the MMA of stage
+      // g - S, the last reader of the slot.  A in TMEM: slot aslot is free
+      // after the MMA of stage g - SA.  One lane waits (mbarrier polls from
+      // the 32 lanes of a warp are served one lane at a time) and the warp
+      // barrier after the broadcast orders the other lanes' reads after its
+      // acquire.  The verdict is warp-uniform: the TMEM store is .sync.aligned.
+      const bool need_slot = P.a_tmem && g >= SA;
+      bool ok = false;
+      if (lane == 0)
+        ok = !ctl.abort_flag && mbar_wait(&full_bar[full.i], full.ph) &&
+             (!need_slot || mbar_wait(&done_bar[done.i], done.ph));
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      __syncwarp();
+      if (!ok) {
+        if (lane == 0) ctl.abort_flag = 1;
+        break;
+      }
+      if (need_slot) done.next(R);
+      uint8_t* sp = smem + full.i * P.stage_bytes;
+      const uint4* pk = reinterpret_cast<const uint4*>(sp + P.b_bytes + P.a_bytes + sl * (TC_BK / 4));
+      const uint4 c0 = pk[0], c1 = pk[1];
+      const uint32_t w[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
       if (P.a_tmem) {
-        // 64 individuals = 32 columns, column q = individuals 2q, 2q + 1
+        // 128 individuals = 64 columns, column q = individuals 2q, 2q + 1
         uint32_t v[32];
-#pragma unroll
-        for (int q = 0; q < 32; ++q) v[q] = tl[(w[q >> 3] >> (4 * (q & 7))) & 15];
+        const uint32_t col = a_lane + aslot.i * TC_A_COLS;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        tmem_st32(a_lane + ta * TC_A_COLS, v);
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+#pragma unroll
+          for (int q = 0; q < 32; ++q) v[q] = tl[(w[4 * half + (q >> 3)] >> (4 * (q & 7))) & 15];
+          tmem_st32(col + 32 * half, v);
+        }
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       } else {
         uint8_t* a = sp + P.b_bytes;
 #pragma unroll
-        for (int c = 0; c < 8; ++c) {
-          // 16-byte chunk c of the row: individuals 8c .. 8c + 7, 16 bits of codes
+        for (int c = 0; c < 16; ++c) {
+          // 16-byte chunk c of the row: individuals 8c .. 8c + 7 (16 bits of
+          // codes), in sub-tile c / 8 of 64 individuals
           const uint32_t h = w[c >> 1] >> ((c & 1) * 16);
           const uint4 v = make_uint4(tl[h & 15], tl[(h >> 4) & 15], tl[(h >> 8) & 15], tl[(h >> 12) & 15]);
-          *reinterpret_cast<uint4*>(a + row * 128 + ((c ^ (row & 7)) << 4)) = v;
+          *reinterpret_cast<uint4*>(a + (c >> 3) * TC_A_SUB_BYTES + row * 128 + (((c & 7) ^ (row & 7)) << 4)) = v;
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       }
       __syncwarp();
-      if (lane == 0) mbar_arrive(&aready_bar[ta]);
+      if (lane == 0) mbar_arrive(&aready_bar[aslot.i]);
+      full.next(S);
+      aslot.next(SA);
     }
   }
 }
