@@ -32,6 +32,8 @@ extern "C" __global__ void bmg_prep_kernel(uint8_t* geno, uint64_t n, uint64_t p
 extern "C" __global__ void bmg_trace_reset_kernel(DevChain* ch, int n_chains);
 extern "C" __global__ void bmg_mask_counts_kernel(const uint8_t* geno, uint32_t gs, uint64_t p, const uint64_t* mask2,
                                                   uint32_t n_samples, int32_t* cnt);
+extern "C" __global__ void bmg_pre_df_kernel(const double* pre, uint64_t p, uint32_t offset, uint32_t off,
+                                             float4* out);
 extern "C" __global__ void bmg_pre_kernel(const int32_t* cnt, uint64_t p, uint32_t n_samples, const double* n_of,
                                           int allow_mask, int ah, int offset, double* pre);
 extern "C" __global__ void bmg_gsum_kernel(const uint8_t* geno, uint64_t n, uint64_t p, uint32_t gs,
@@ -827,6 +829,17 @@ extern "C" bmg_status bmg_precompute(bmg_ctx* ctx)
       pheno_of[k] = k;
       chain_ee0[k] = nk;
       chain_ey0[k] = ctx->ph_ysum[k];
+    }
+  }
+  // one-type scans evaluate the posterior in double-float from FP32 copies
+  // of the two sums it reads
+  if (o.n_types == 1 && o.types[0] != 4 && !o.use_individual_tau2) {
+    const uint32_t off = (uint32_t)K.offset_type[o.types[0]];
+    for (DevPheno& r : recs) {
+      float4* pf = ctx->dalloc<float4>(p, false);
+      bmg_pre_df_kernel<<<1024, 256, 0, ctx->stream>>>(r.pre, p, (uint32_t)offset, off, pf);
+      LAUNCHED(ctx, "bmg_pre_df_kernel");
+      r.pre_f = pf;
     }
   }
   {

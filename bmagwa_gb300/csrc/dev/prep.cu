@@ -175,3 +175,16 @@ extern "C" __global__ void bmg_pre_kernel(const int32_t* cnt, uint64_t p, uint32
     }
   }
 }
+
+// Per SNP the two precomputed sums of the scan's one-type posterior as FP32:
+// out[j] = {sum x (an integer below 2^24), pre1 hi, pre1 lo, 0} with pre1 the
+// centred second moment, split into a float pair (about 48 bits).
+extern "C" __global__ void bmg_pre_df_kernel(const double* pre, uint64_t p, uint32_t offset, uint32_t off,
+                                             float4* out)
+{
+  for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < p; j += (uint64_t)gridDim.x * blockDim.x) {
+    const double* loc = pre + j * offset + off;
+    const float h = (float)loc[1];
+    out[j] = make_float4((float)loc[0], h, (float)(loc[1] - (double)h), 0.0f);
+  }
+}

@@ -8,6 +8,7 @@
 
 #include "common.cuh"
 #include "exp_table.h"
+#include "rb_df.h"
 
 static __device__ __forceinline__ bool in_model(const DevConst& K, int c, uint64_t j)
 {
@@ -50,8 +51,20 @@ static __device__ __forceinline__ double bmg_exp_tab(double a)
 static __device__ __forceinline__ double rb_fast_pr(const DevConst& K, int c, uint64_t j, long long xi, double* lo)
 {
   const RbParams& rp = K.rb[c];
+  const DevPheno& P = K.ph[K.pheno_of[c]];
   const int type = K.types[0];
-  const double* pre = K.ph[K.pheno_of[c]].pre + j * (size_t)K.offset;
+  if (!K.p_lml && P.pre_f && rp.scale_f >= 0x1p-100f) {
+    // double-float arithmetic (relative error below 1e-12); FP64 below
+    const float4 pf = __ldg(&P.pre_f[j]);
+    const double pr = rb_pr_df(xi, rp.scale_f, pf.x, dfl{pf.y, pf.z}, dfl{rp.mr_df[0], rp.mr_df[1]},
+                               dfl{rp.itv_df[type][0], rp.itv_df[type][1]}, dfl{rp.i2s_df[0], rp.i2s_df[1]},
+                               dfl{rp.cadd_df[type][0], rp.cadd_df[type][1]}, kExp2TabF);
+    if (pr >= 0) {
+      *lo = 0;
+      return pr;
+    }
+  }
+  const double* pre = P.pre + j * (size_t)K.offset;
   const int off = K.offset_type[type];
   const double xr = (double)xi * rp.scale;
   const double det = pre[off + 1] + rp.itv[type];

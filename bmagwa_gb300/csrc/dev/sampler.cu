@@ -17,6 +17,7 @@
 #include <math.h>
 
 #include "common.cuh"
+#include "df64.h"
 
 #define TAB_ADD_A 0
 #define TAB_REM_A 1
@@ -1836,6 +1837,18 @@ __device__ void prep_rb(Warp& W, bool scan_only)
       rp->itv[t] = ch->inv_t2a2[t];
       rp->nlog_itv[t] = -log(ch->inv_t2a2[t]);
     }
+    // the same constants as FP32 pairs for the double-float posterior
+    rp->scale_f = (float)rp->scale;
+    const dfl mr = df_from_double(rp->mr), i2s = df_from_double(rp->inv_2s2);
+    rp->mr_df[0] = mr.h;
+    rp->mr_df[1] = mr.l;
+    rp->i2s_df[0] = i2s.h;
+    rp->i2s_df[1] = i2s.l;
+    for (int t = 0; t < 4; ++t) {
+      const dfl v = df_from_double(rp->itv[t]);
+      rp->itv_df[t][0] = v.h;
+      rp->itv_df[t][1] = v.l;
+    }
   }
   // log prior changes of the scan (src/sampler.cpp:51-76)
   int Ns[5];
@@ -1847,7 +1860,12 @@ __device__ void prep_rb(Warp& W, bool scan_only)
     if ((uint64_t)(Ns[t] + 1) <= K.p) la = W.lchange_add(Ns, nl, t);
     if (W.lane == 0) {
       rp->lmp_add[t] = la;
-      if (t < 4) rp->cadd[t] = la - 0.5 * rp->nlog_itv[t];
+      if (t < 4) {
+        rp->cadd[t] = la - 0.5 * rp->nlog_itv[t];
+        const dfl v = df_from_double(rp->cadd[t]);
+        rp->cadd_df[t][0] = v.h;
+        rp->cadd_df[t][1] = v.l;
+      }
     }
     Ns[t]--;
     nl--;

@@ -112,6 +112,9 @@ struct RbParams {
   double itv[4];            // inv_tau2_alpha2 per term (shared tau2)
   double nlog_itv[4];       // -log(itv[t]), once per chain
   double cadd[4];           // lmp_add[t] - nlog_itv[t] / 2: the odds' constant
+  float scale_f;            // scale as FP32 (a power of two)
+  float mr_df[2], i2s_df[2];          // mr and inv_2s2 as FP32 pairs (hi, lo)
+  float itv_df[4][2], cadd_df[4][2];  // itv[t] and cadd[t] as FP32 pairs
   double lmp_add[5];
   double lmp_rem[5][5];
   double rao_iz1, rao_z2;   // running mean of p_rao: z2 old + p / z1, 1/z1 kept
@@ -159,6 +162,7 @@ struct DevPheno {
   const uint64_t* mask2; // gs / 8 words: 01 in the 2-bit slot of each individual in the sample; null: all
   const int32_t* cnt;    // p x 2: #het, #hom-alt within the sample
   const double* pre;     // p x offset: the precomputed sums within the sample
+  const float4* pre_f;   // one-type scans: {sum x, pre1 hi, pre1 lo, 0} per SNP, else null
   const int64_t* gsum;   // p x nv x 2 fixed-point sums of y and covariates, or null (X'y from the codes)
 };
 
