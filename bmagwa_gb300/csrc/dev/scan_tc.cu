@@ -42,24 +42,22 @@ __global__ void __launch_bounds__(TcShape<TC_EPI_WARPS>::threads, 1)
 bmg_scan_tc_kernel(DevConst K, TcParams P, const __grid_constant__ CUtensorMap map_b,
                    const __grid_constant__ CUtensorMap map_g)
 {
-  constexpr int TC_THREADS = TcShape<TC_EPI_WARPS>::threads;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   // 1024-byte aligned base for the swizzled tiles; the int64 sums follow the stages
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   long long* xr_s = reinterpret_cast<long long*>(smem + P.stages * P.stage_bytes);
   __shared__ TcCtl ctl;
   __shared__ int epi_ok;
-  __shared__ TcLut lut;  // per term: nibble -> 2 bf16 values
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t L = K.limbs_n;
   const uint32_t ct = P.chains_tile;
   const uint32_t xs = ct + 1;  // row stride of the sums: odd, so rows fall in distinct banks
   const uint32_t my_tiles = (P.tiles > blockIdx.x) ? (P.tiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
-  const uint32_t tmem = tc_setup(P, ctl, lut, TC_THREADS, TC_EPI_WARPS);
+  const uint32_t tmem = tc_setup(P, ctl, TC_EPI_WARPS);
 
   if (warp < 6) {
-    tc_main_roles(P, ctl, lut, smem, tmem, my_tiles, map_b, map_g);
+    tc_main_roles(P, ctl, smem, tmem, my_tiles, map_b, map_g);
   } else {
     // epilogue warps: warp w reads TMEM lanes 32 (w % 4) .. +31 (the rows of
     // the tile); the TC_EPI_WARPS / 4 warps of a quarter split the chains

@@ -104,14 +104,13 @@ bmg_schur_tc_kernel(DevConst K, TcParams P, uint32_t KB, uint32_t n_terms, doubl
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   __shared__ TcCtl ctl;
   __shared__ int epi_ok;
-  __shared__ TcLut lut;  // per term: nibble -> 2 bf16 values
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t ct = P.chains_tile;
   const uint32_t my_tiles = (P.tiles > blockIdx.x) ? (P.tiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
-  const uint32_t tmem = tc_setup(P, ctl, lut, SC_THREADS, SC_EPI);
+  const uint32_t tmem = tc_setup(P, ctl, SC_EPI);
 
   if (warp < 6) {
-    tc_main_roles(P, ctl, lut, smem, tmem, my_tiles, map_b, map_g);
+    tc_main_roles(P, ctl, smem, tmem, my_tiles, map_b, map_g);
   } else {
     // warp w reads TMEM lanes 32 (w % 4) .. +31 = rows of the tile; the two
     // warps of a quarter split the tile's chains

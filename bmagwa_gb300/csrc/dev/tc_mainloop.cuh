@@ -36,6 +36,7 @@
 #define BMG_TC_MAINLOOP_CUH_
 
 #include "common.cuh"
+#include "decode_bf16.h"
 #include "tc_common.cuh"
 
 namespace {
@@ -124,27 +125,10 @@ struct TcCtl {
   volatile int abort_flag;
 };
 
-// Decode table of one term: entry x (a nibble of packed codes, two
-// individuals) holds their bf16 values, the first in the low half.  16 entries
-// of 4 bytes sit in 16 distinct banks, so a warp's lookups never conflict.
-// Row TC_LUT_ZERO is all zeros (rows of a SNP beyond its terms).
-constexpr int TC_LUT_ZERO = 4;
-typedef uint32_t TcLut[TC_LUT_ZERO + 1][16];
-
-// All threads: decode tables, barriers, tensor memory.  Returns the TMEM base.
-__device__ __forceinline__ uint32_t tc_setup(const TcParams& P, TcCtl& ctl, TcLut& lut, int threads, int epi_warps)
+// All threads: barriers, tensor memory.  Returns the TMEM base.
+__device__ __forceinline__ uint32_t tc_setup(const TcParams& P, TcCtl& ctl, int epi_warps)
 {
   const int tid = threadIdx.x, warp = tid >> 5;
-  // bf16 bit patterns of 0, 1, 2 are 0x0000, 0x3F80, 0x4000
-  for (int e = tid; e < (TC_LUT_ZERO + 1) * 16; e += threads) {
-    const int term = e >> 4, x = e & 15;
-    uint32_t h[2];
-    for (int q = 0; q < 2; ++q) {
-      const int v = term == TC_LUT_ZERO ? 0 : term_value((x >> (2 * q)) & 3, term);
-      h[q] = v == 0 ? 0 : (v == 1 ? 0x3F80 : 0x4000);
-    }
-    lut[term][x] = h[0] | (h[1] << 16);
-  }
   if (tid == 0) {
     for (uint32_t st = 0; st < P.stages; ++st) mbar_init(&ctl.full_bar[st], 1);
     for (uint32_t t = 0; t < P.a_stages; ++t) mbar_init(&ctl.aready_bar[t], 4);
@@ -169,7 +153,7 @@ __device__ __forceinline__ uint32_t tc_setup(const TcParams& P, TcCtl& ctl, TcLu
 }
 
 // Warps 0-5: the decode, TMA and MMA roles over this CTA's tiles.
-__device__ __forceinline__ void tc_main_roles(const TcParams& P, TcCtl& ctl, const TcLut& lut, uint8_t* smem,
+__device__ __forceinline__ void tc_main_roles(const TcParams& P, TcCtl& ctl, uint8_t* smem,
                                               uint32_t tmem, uint32_t my_tiles, const CUtensorMap& map_b,
                                               const CUtensorMap& map_g)
 {
@@ -259,7 +243,9 @@ __device__ __forceinline__ void tc_main_roles(const TcParams& P, TcCtl& ctl, con
     // decode warps: packed 2-bit codes -> bf16 rows of A; thread = row = TMEM lane
     const uint32_t row = tid;  // 0..127
     const uint32_t sl = row / P.tpad, u = row % P.tpad;
-    const uint32_t* tl = lut[P.term_of_row[u] >= 0 ? P.term_of_row[u] : TC_LUT_ZERO];
+    int value[4];  // this row's coding of the four codes (-1: a padding row, zeros)
+    for (int c = 0; c < 4; ++c) value[c] = P.term_of_row[u] >= 0 ? term_value(c, P.term_of_row[u]) : -1;
+    const DecTab tab = dec_tab(value);
     const uint32_t total = my_tiles * nk;
     const uint32_t a_lane = tmem + ((uint32_t)(warp * 32) << 16) + P.n_acc * P.acc_cols;
     TcRing full, aslot, done;  // this stage's slots; the done phase of stage g - SA
@@ -288,13 +274,17 @@ __device__ __forceinline__ void tc_main_roles(const TcParams& P, TcCtl& ctl, con
       const uint32_t w[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
       if (P.a_tmem) {
         // 128 individuals = 64 columns, column q = individuals 2q, 2q + 1
+        // (code byte k gives columns 2k and 2k + 1)
         uint32_t v[32];
         const uint32_t col = a_lane + aslot.i * TC_A_COLS;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
         for (int half = 0; half < 2; ++half) {
 #pragma unroll
-          for (int q = 0; q < 32; ++q) v[q] = tl[(w[4 * half + (q >> 3)] >> (4 * (q & 7))) & 15];
+          for (int kb = 0; kb < 16; ++kb) {
+            const int k = 16 * half + kb;
+            dec_byte((w[k >> 2] >> (8 * (k & 3))) & 0xFFu, tab, v[2 * kb], v[2 * kb + 1]);
+          }
           tmem_st32(col + 32 * half, v);
         }
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -302,10 +292,12 @@ __device__ __forceinline__ void tc_main_roles(const TcParams& P, TcCtl& ctl, con
         uint8_t* a = sp + P.b_bytes;
 #pragma unroll
         for (int c = 0; c < 16; ++c) {
-          // 16-byte chunk c of the row: individuals 8c .. 8c + 7 (16 bits of
-          // codes), in sub-tile c / 8 of 64 individuals
+          // 16-byte chunk c of the row: individuals 8c .. 8c + 7 (code bytes
+          // 2c, 2c + 1), in sub-tile c / 8 of 64 individuals
           const uint32_t h = w[c >> 1] >> ((c & 1) * 16);
-          const uint4 v = make_uint4(tl[h & 15], tl[(h >> 4) & 15], tl[(h >> 8) & 15], tl[(h >> 12) & 15]);
+          uint4 v;
+          dec_byte(h & 0xFFu, tab, v.x, v.y);
+          dec_byte((h >> 8) & 0xFFu, tab, v.z, v.w);
           *reinterpret_cast<uint4*>(a + (c >> 3) * TC_A_SUB_BYTES + row * 128 + (((c & 7) ^ (row & 7)) << 4)) = v;
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
