@@ -130,8 +130,11 @@ bmg_mask_counts_kernel(const uint8_t* geno, uint32_t gs, uint64_t p, const uint6
   const int lane = threadIdx.x & 31;
   const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
   const uint64_t nw64 = gs / 8;
-  for (uint64_t t = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); t < p * n_samples; t += warps) {
-    const uint64_t j = t % p, k = t / p;
+  // SNP-major: consecutive warps take the samples of one SNP, so its row is
+  // read from memory once and from cache by the others (the masks, gs / 4
+  // bytes per sample, stay in L2)
+  for (uint64_t q = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); q < p * n_samples; q += warps) {
+    const uint64_t j = q / n_samples, k = q % n_samples, t = k * p + j;
     const uint64_t* row = reinterpret_cast<const uint64_t*>(geno + j * gs);
     const uint64_t* mk = mask2 + k * nw64;
     unsigned h = 0, r = 0;

@@ -72,15 +72,19 @@ def genotypes(n, p, ld_block, seed, device="cpu", rho=0.8, chunk=4096, block_gro
     return out, maf
 
 
-def pack(counts):
-    """Allele counts (p x n) -> PLINK SNP-major payload (p x ceil(n/4) bytes)."""
+def pack(counts, chunk=16384):
+    """Allele counts (p x n) -> PLINK SNP-major payload (p x ceil(n/4) bytes),
+    in chunks of SNPs with uint8 arithmetic (code 0 -> 00, 1 -> 10, 2 -> 11)."""
     p, n = counts.shape
     n4 = (n + 3) // 4
-    code = torch.zeros((p, n4 * 4), dtype=torch.uint8, device=counts.device)
-    c = counts.to(torch.uint8)
-    code[:, :n] = torch.where(c == 0, 0, torch.where(c == 1, 2, 3)).to(torch.uint8)
-    code = code.view(p, n4, 4)
-    return (code[..., 0] | (code[..., 1] << 2) | (code[..., 2] << 4) | (code[..., 3] << 6)).contiguous()
+    out = torch.empty((p, n4), dtype=torch.uint8, device=counts.device)
+    for j0 in range(0, p, chunk):
+        c = counts[j0:j0 + chunk].to(torch.uint8)
+        code = torch.zeros((c.shape[0], n4 * 4), dtype=torch.uint8, device=counts.device)
+        code[:, :n] = (c > 0).to(torch.uint8) * 2 + (c > 1).to(torch.uint8)
+        code = code.view(-1, n4, 4)
+        out[j0:j0 + chunk] = code[..., 0] | (code[..., 1] << 2) | (code[..., 2] << 4) | (code[..., 3] << 6)
+    return out
 
 
 def phenotype(counts, causal, beta_sd, dominance, seed, device="cpu"):
