@@ -43,6 +43,7 @@ WORKLOADS = {
 }
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM = 6800.0
+FALLBACK_BF16_SUSTAINED = 1700.0
 
 
 def env_rank():
@@ -158,6 +159,23 @@ def peak_hbm():
         return FALLBACK_HBM, "fallback"
 
 
+def peak_bf16_sustained():
+    """Dense bf16 TFLOP/s sustained over seconds (the scan runs inside a long step)."""
+    try:
+        with open(PEAKS) as f:
+            return float(json.load(f)["bf16_tflops_sustained"]), "measured (sustained)"
+    except Exception:
+        return FALLBACK_BF16_SUSTAINED, "fallback (sustained)"
+
+
+def scan_terms(types):
+    """Coding rows per SNP in the scan's GEMM (A, H, D, R; AH uses A and H)."""
+    rows = set()
+    for t in types.split(","):
+        rows |= {"A": {0}, "H": {1}, "D": {2}, "R": {3}, "AH": {0, 1}}[t]
+    return len(rows)
+
+
 def scan_traffic_per_launch(workload):
     """DRAM bytes per scan launch from the committed ncu summary, if present."""
     path = os.path.join(ROOT, "profiles", "scan_%s_ncu.md" % workload)
@@ -269,8 +287,14 @@ def run_gb300(args, wl):
     # limbs (L bf16 digits per individual and chain)
     L = int(o.scan_limbs) if o.scan_limbs else 6
     alg_bytes = p * ((n + 3) // 4) + p * C * (8 + 16) + C * n * 2 * L
-    peak, peak_kind = peak_hbm()
-    achieved = alg_bytes / (scan_ms / 1000.0) / 1e9 if scan_ms > 0 else None
+    peak_h, peak_h_kind = peak_hbm()
+    hbm_gbs = alg_bytes / (scan_ms / 1000.0) / 1e9 if scan_ms > 0 else None
+    # the scan is an exact-integer GEMM on the tensor cores: 2 n_pad (p terms)
+    # (C L) bf16 flops per launch (n_pad = individuals rounded up to 128)
+    n_pad = ((n + 127) // 128) * 128
+    flops = 2.0 * n_pad * p * scan_terms(wl["types"]) * C * L
+    peak, peak_kind = peak_bf16_sustained()
+    achieved = flops / (scan_ms / 1000.0) / 1e12 if scan_ms > 0 else None
     out = {
         "metric": "MCMC chain-iterations/s (RB scan of all SNPs every iteration)",
         "value": value,
@@ -293,11 +317,13 @@ def run_gb300(args, wl):
         "gpu_launches": launches,
         "phase_ms": {"move": ms[0], "scan": ms[1], "rebuild": ms[2], "total": ms[3],
                      "scans": n_scans, "wall_s": dt},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": (achieved / peak) if achieved else None,
                      "traffic": scan_traffic_per_launch(args.workload),
                      "kernel": "scan", "peak_kind": peak_kind, "scan_ms": scan_ms,
-                     "alg_bytes_per_launch": alg_bytes},
+                     "alg_flops_per_launch": flops, "alg_bytes_per_launch": alg_bytes,
+                     "hbm": {"achieved": hbm_gbs, "peak": peak_h, "unit": "GB/s",
+                             "frac": (hbm_gbs / peak_h) if hbm_gbs else None, "peak_kind": peak_h_kind}},
         "clocks": clocks.summary(),
     }
     if rank == 0 and args.cpu_baseline:
