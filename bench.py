@@ -258,21 +258,33 @@ def run_gb300(args, wl):
         o2.scan_impl = args.scan
         torch.cuda.synchronize()
         t0 = time.perf_counter()
+        marks = []
         ctx2 = bg.Context(o2)
+        marks.append(("create", time.perf_counter()))
         ctx2.load_bed(packed)
+        marks.append(("load_bed", time.perf_counter()))
         ctx2.set_phenotypes(y)
         ctx2.set_covariates(None)
+        marks.append(("phenotypes", time.perf_counter()))
         ctx2.precompute()
+        marks.append(("precompute", time.perf_counter()))
         col = ctx2.run(args.steps, collect=True)
+        marks.append(("run", time.perf_counter()))
         rao = [ctx2.rao(c)[0] for c in range(wl["chains"])]
         torch.cuda.synchronize()
         e2e_s = time.perf_counter() - t0
+        marks.append(("read_back", t0 + e2e_s))
+        breakdown, prev = {}, t0
+        for name, t in marks:
+            breakdown[name] = round(t - prev, 4)
+            prev = t
         d2h = sum(int(sum(a.nbytes for a in col.chain(c).values())) for c in range(wl["chains"]))
         d2h += sum(r.nbytes for r in rao)
         h2d = packed.nbytes + y.nbytes
         ctx2.close()
         e2e = {"value": args.steps * wl["chains"] * world / e2e_s, "unit": "iter/s",
-               "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps}
+               "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
+               "seconds": breakdown}
         # inclusion-indicator ESS of the same run (Geyer initial monotone
         # sequence over the thinned trace of each chain)
         from bmagwa_gb300 import ess

@@ -32,6 +32,7 @@ extern "C" __global__ void bmg_prep_kernel(uint8_t* geno, uint64_t n, uint64_t p
 extern "C" __global__ void bmg_trace_reset_kernel(DevChain* ch, int n_chains);
 extern "C" __global__ void bmg_mask_counts_kernel(const uint8_t* geno, uint32_t gs, uint64_t p, const uint64_t* mask2,
                                                   uint32_t n_samples, int32_t* cnt);
+extern "C" __global__ void bmg_tail_kernel(uint8_t* g, uint64_t p, uint64_t gs, uint64_t last, uint8_t keep);
 extern "C" __global__ void bmg_pre_df_kernel(const double* pre, uint64_t p, uint32_t offset, uint32_t off,
                                              float4* out);
 extern "C" __global__ void bmg_pre_kernel(const int32_t* cnt, uint64_t p, uint32_t n_samples, const double* n_of,
@@ -362,16 +363,18 @@ extern "C" bmg_status bmg_load_bed(bmg_ctx* ctx, const uint8_t* packed, uint64_t
   if (!packed) throw bmg_error(BMG_EINVAL, "null genotypes");
   if (n != ctx->n || p != ctx->p) throw bmg_error(BMG_EINVAL, "genotype sizes differ from the options");
   const uint64_t stride = (n + 3) / 4, gs = ctx->gs;
-  std::vector<uint8_t> rows(gs * p, 0);
   const int tail = (int)(n % 4);
-  for (uint64_t j = 0; j < p; ++j) {
-    std::memcpy(&rows[j * gs], packed + j * stride, stride);
-    if (tail) rows[j * gs + stride - 1] &= (uint8_t)((1u << (2 * tail)) - 1);
-  }
-  uint8_t* g = ctx->dalloc<uint8_t>(gs * p, false);
+  // rows of `stride` bytes into the zeroed, padded device layout in one
+  // pitched copy; the unused codes of a row's last byte are then cleared
+  uint8_t* g = ctx->dalloc<uint8_t>(gs * p);
   int32_t* cnt = ctx->dalloc<int32_t>(2 * p);
   int32_t* miss = ctx->dalloc<int32_t>(p);
-  CK(cudaMemcpyAsync(g, rows.data(), rows.size(), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpy2DAsync(g, gs, packed, stride, stride, p, cudaMemcpyHostToDevice, ctx->stream));
+  if (tail) {
+    bmg_tail_kernel<<<(unsigned)std::min<uint64_t>((p + 255) / 256, 152 * 16), 256, 0, ctx->stream>>>(
+        g, p, gs, stride - 1, (uint8_t)((1u << (2 * tail)) - 1));
+    LAUNCHED(ctx, "bmg_tail_kernel");
+  }
   unsigned blocks = (unsigned)std::min<uint64_t>((p + 7) / 8, 152 * 16);
   bmg_prep_kernel<<<blocks, 256, 0, ctx->stream>>>(g, n, p, ctx->gs, ctx->opt.recode_g_to_minor_allele_count,
                                                    cnt, miss);

@@ -191,3 +191,11 @@ extern "C" __global__ void bmg_pre_df_kernel(const double* pre, uint64_t p, uint
     out[j] = make_float4((float)loc[0], h, (float)(loc[1] - (double)h), 0.0f);
   }
 }
+
+// Clear the codes past the last individual in byte `last` of every row (the
+// .bed format pads a row to whole bytes with unspecified bits).
+extern "C" __global__ void bmg_tail_kernel(uint8_t* g, uint64_t p, uint64_t gs, uint64_t last, uint8_t keep)
+{
+  for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < p; j += (uint64_t)gridDim.x * blockDim.x)
+    g[j * gs + last] &= keep;
+}

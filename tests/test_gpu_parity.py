@@ -54,11 +54,18 @@ def synth_case(bg, tmp_path, name, **kw):
     dict(name="plain", n=700, p=3000, chains=2, iters=300, n_rao=1),
     dict(name="batched", n=900, p=4000, chains=3, iters=300, n_rao=5),
     dict(name="plain", n=1500, p=2500, chains=1, iters=500, n_rao=25),
-], ids=["rb_every_iter", "ld_types", "sparse_rb"])
+    # n not a multiple of 4 (a ragged last code byte); RB every iteration
+    # leaves the move-size tuning a tie to break in its first iterations, so
+    # the tuning is off here as in the other tests that compare states
+    dict(name="plain", n=703, p=2000, chains=2, iters=150, n_rao=1, tune=False),
+], ids=["rb_every_iter", "ld_types", "sparse_rb", "ragged_last_byte"])
 def test_gpu_matches_oracle_synthetic(bmg, oracle, tmp_path, case):
     case = dict(case)
     iters = case.pop("iters")
+    tune = case.pop("tune", True)
     opt, packed, y, e = synth_case(bmg, tmp_path, iters=iters, **case)
+    if not tune:
+        opt.adapt_p_move_size = 0
     port = oracle.Port(opt, packed, y, e)
     colp = port.run(iters)
     ctx, colg = run_gpu(bmg, opt, packed, y, e, iters)
@@ -354,3 +361,18 @@ def test_table_exp_of_the_scan_epilogue(bmg):
     ref = np.exp(a)
     ulp = np.abs(got - ref) / np.spacing(ref)
     assert ulp.max() <= 4, (ulp.max(), a[np.argmax(ulp)])
+
+
+def test_unused_bits_of_a_rows_last_byte_are_ignored(bmg, tmp_path):
+    """The .bed format pads each SNP row to whole bytes; the padding's bits are
+    unspecified.  Setting them all gives the same chains as zero padding."""
+    opt, packed, y, e = synth_case(bmg, tmp_path, "plain", n=701, p=1500, chains=2, iters=60, n_rao=1)
+    n, p = int(opt.n), int(opt.m_g)
+    stride = (n + 3) // 4
+    junk = packed.copy().reshape(p, stride)
+    junk[:, -1] |= np.uint8(0xFF & ~((1 << (2 * (n % 4))) - 1))
+    _, a = run_gpu(bmg, opt, packed, y, e, 60)
+    _, b = run_gpu(bmg, opt, junk.reshape(-1), y, e, 60)
+    for c in range(opt.n_chains):
+        for key in ("loci", "jumpdistance", "log_likelihood"):
+            np.testing.assert_array_equal(a.chain(c)[key], b.chain(c)[key])
