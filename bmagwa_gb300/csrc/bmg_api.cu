@@ -17,6 +17,7 @@
 #include <iomanip>
 #include <memory>
 #include <sstream>
+#include <thread>
 #include <string>
 #include <cstdlib>
 #include <vector>
@@ -173,8 +174,36 @@ struct bmg_ctx {
     if (zero) CK(cudaMemsetAsync(ptr, 0, bytes, stream));
     return static_cast<T*>(ptr);
   }
+  // pinned host staging for uploads and read-backs: two buffers (chunks of
+  // an upload alternate between them while the other's DMA runs)
+  uint8_t* stage[2] = {nullptr, nullptr};
+  size_t stage_cap = 0;
+  cudaEvent_t stage_ev[2] = {nullptr, nullptr};
+  void ensure_stage(size_t bytes)
+  {
+    if (stage_cap >= bytes) return;
+    for (int b = 0; b < 2; ++b) {
+      if (stage[b]) {
+        CK(cudaEventSynchronize(stage_ev[b]));
+        cudaFreeHost(stage[b]);
+        stage[b] = nullptr;
+      }
+    }
+    stage_cap = 0;
+    for (int b = 0; b < 2; ++b) {
+      CK(cudaMallocHost(reinterpret_cast<void**>(&stage[b]), bytes));
+      if (!stage_ev[b]) CK(cudaEventCreateWithFlags(&stage_ev[b], cudaEventDisableTiming));
+      CK(cudaEventRecord(stage_ev[b], stream));
+    }
+    stage_cap = bytes;
+  }
   ~bmg_ctx()
   {
+    for (int b = 0; b < 2; ++b) {
+      if (stage_ev[b]) cudaEventSynchronize(stage_ev[b]);
+      if (stage[b]) cudaFreeHost(stage[b]);
+      if (stage_ev[b]) cudaEventDestroy(stage_ev[b]);
+    }
     for (cudaEvent_t e : ev)
       if (e) cudaEventDestroy(e);
     for (cudaEvent_t e : tc_ev)
@@ -364,12 +393,32 @@ extern "C" bmg_status bmg_load_bed(bmg_ctx* ctx, const uint8_t* packed, uint64_t
   if (n != ctx->n || p != ctx->p) throw bmg_error(BMG_EINVAL, "genotype sizes differ from the options");
   const uint64_t stride = (n + 3) / 4, gs = ctx->gs;
   const int tail = (int)(n % 4);
-  // rows of `stride` bytes into the zeroed, padded device layout in one
-  // pitched copy; the unused codes of a row's last byte are then cleared
+  // rows of `stride` bytes into the zeroed, padded device layout by pitched
+  // copies from pinned staging chunks (host copies by several threads, the
+  // DMA of one chunk overlapping the host copy of the next); the unused
+  // codes of a row's last byte are then cleared
   uint8_t* g = ctx->dalloc<uint8_t>(gs * p);
   int32_t* cnt = ctx->dalloc<int32_t>(2 * p);
   int32_t* miss = ctx->dalloc<int32_t>(p);
-  CK(cudaMemcpy2DAsync(g, gs, packed, stride, stride, p, cudaMemcpyHostToDevice, ctx->stream));
+  {
+    const size_t chunk_rows = std::max<size_t>(1, (size_t(32) << 20) / stride);
+    ctx->ensure_stage(chunk_rows * stride);
+    const unsigned nth = std::max(1u, std::min(8u, std::thread::hardware_concurrency()));
+    int b = 0;
+    for (uint64_t j0 = 0; j0 < p; j0 += chunk_rows, b ^= 1) {
+      const size_t rows = std::min<uint64_t>(chunk_rows, p - j0), bytes = rows * stride;
+      CK(cudaEventSynchronize(ctx->stage_ev[b]));
+      uint8_t* dst = ctx->stage[b];
+      const uint8_t* src = packed + j0 * stride;
+      std::vector<std::thread> th;
+      const size_t part = (bytes + nth - 1) / nth;
+      for (unsigned t = 0; t < nth && t * part < bytes; ++t)
+        th.emplace_back([=] { std::memcpy(dst + t * part, src + t * part, std::min(part, bytes - t * part)); });
+      for (auto& x : th) x.join();
+      CK(cudaMemcpy2DAsync(g + j0 * gs, gs, dst, stride, stride, rows, cudaMemcpyHostToDevice, ctx->stream));
+      CK(cudaEventRecord(ctx->stage_ev[b], ctx->stream));
+    }
+  }
   if (tail) {
     bmg_tail_kernel<<<(unsigned)std::min<uint64_t>((p + 255) / 256, 152 * 16), 256, 0, ctx->stream>>>(
         g, p, gs, stride - 1, (uint8_t)((1u << (2 * tail)) - 1));
@@ -1589,12 +1638,21 @@ extern "C" bmg_status bmg_get_rao(bmg_ctx* ctx, uint32_t chain, double* p_rao, d
   API_BEGIN
   check_ready(ctx);
   if (chain >= ctx->C) throw bmg_error(BMG_EINVAL, "chain index");
-  const size_t p = ctx->p;
-  if (p_rao) CK(cudaMemcpyAsync(p_rao, ctx->K.p_rao + chain * p, 8 * p, cudaMemcpyDeviceToHost, ctx->stream));
-  if (p_rao_types && ctx->opt.n_types > 1)
-    CK(cudaMemcpyAsync(p_rao_types, ctx->K.p_rao_types + chain * p * ctx->opt.n_types, 8 * p * ctx->opt.n_types,
-                       cudaMemcpyDeviceToHost, ctx->stream));
-  CK(cudaStreamSynchronize(ctx->stream));
+  const size_t p = ctx->p, nt = ctx->opt.n_types > 1 ? ctx->opt.n_types : 0;
+  // DMA into pinned staging, then into the caller's memory
+  ctx->ensure_stage(8 * p * std::max<size_t>(1, nt));
+  CK(cudaEventSynchronize(ctx->stage_ev[0]));
+  double* st = reinterpret_cast<double*>(ctx->stage[0]);
+  if (p_rao) {
+    CK(cudaMemcpyAsync(st, ctx->K.p_rao + chain * p, 8 * p, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    std::memcpy(p_rao, st, 8 * p);
+  }
+  if (p_rao_types && nt) {
+    CK(cudaMemcpyAsync(st, ctx->K.p_rao_types + chain * p * nt, 8 * p * nt, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    std::memcpy(p_rao_types, st, 8 * p * nt);
+  }
   return BMG_OK;
   API_END
 }
