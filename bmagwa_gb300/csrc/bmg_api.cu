@@ -61,6 +61,7 @@ extern "C" cudaError_t bmg_mlp_grad(const DevConst* K, const int32_t* adam_t, co
 extern "C" int bmg_schur_launch(const DevConst* K, const int* xcols, uint16_t** bm, size_t* bm_cap, double* out,
                                 cudaStream_t stream);
 extern "C" void bmg_scan_tc_variant_name(int v, char* buf, size_t len);
+extern "C" int bmg_scan_tc_variant_redundant(const DevConst* K, int v);
 extern "C" int bmg_scan_tc_supported(const DevConst* K);
 
 using bmg_host::bmg_error;
@@ -153,6 +154,7 @@ struct bmg_ctx {
   int tc_pending = -1;     // shape whose timing events are not read yet
   cudaEvent_t tc_ev[2] = {nullptr, nullptr};
   std::vector<float> tc_ms;
+  std::vector<int> tc_cands;  // shapes the tuner times
   cudaEvent_t ev[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   uint64_t n_iter = 0;
   time_t t_start = 0;
@@ -1158,14 +1160,21 @@ static void launch_scan(bmg_ctx* ctx)
         if (ctx->tc_tuned > 1 && (slot < 0 || ms < slot)) slot = ms;
         ctx->tc_pending = -1;
       }
-      if (ctx->tc_ms.empty()) ctx->tc_ms.assign(nv, -1.0f);
-      if (ctx->tc_tuned > 2 * nv) {
-        int best = 0;
-        for (int i = 1; i < nv; ++i)
+      if (ctx->tc_ms.empty()) {
+        ctx->tc_ms.assign(nv, -1.0f);
+        // shapes whose plan repeats an earlier shape's are not timed
+        ctx->tc_cands.clear();
+        for (int i = 0; i < nv; ++i)
+          if (!bmg_scan_tc_variant_redundant(&K, i)) ctx->tc_cands.push_back(i);
+      }
+      const int nc = (int)ctx->tc_cands.size();
+      if (ctx->tc_tuned > 2 * nc) {
+        int best = ctx->tc_cands[0];
+        for (int i : ctx->tc_cands)
           if (ctx->tc_ms[i] >= 0 && (ctx->tc_ms[best] < 0 || ctx->tc_ms[i] < ctx->tc_ms[best])) best = i;
         ctx->tc_variant = v = best;
       } else {
-        v = ctx->tc_tuned == 0 ? 0 : (ctx->tc_tuned - 1) % nv;
+        v = ctx->tc_cands[ctx->tc_tuned == 0 ? 0 : (ctx->tc_tuned - 1) % nc];
         ctx->tc_pending = v;
         ++ctx->tc_tuned;
         for (int q = 0; q < 2; ++q)

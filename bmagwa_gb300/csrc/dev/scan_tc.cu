@@ -220,10 +220,12 @@ static bool tc_plan(const DevConst* K, TcParams* P, uint32_t ct_cap, uint32_t n_
 // sums and the same posterior, bit for bit.
 struct TcVariant {
   int epi;
-  int ct_div;  // chains per tile = ceil(chains / ct_div)
+  int ct_div;  // chains per tile = ceil(chains / ct_div); 0: the widest tile whose
+               // accumulators (two of 192 columns) leave A room in tensor memory
   int n_acc;   // TMEM accumulators
 };
-static const TcVariant kTcVariants[] = {{12, 1, 2}, {8, 1, 2}, {12, 2, 2}, {8, 2, 2}, {12, 1, 1}, {8, 1, 1}};
+static const TcVariant kTcVariants[] = {{12, 1, 2}, {8, 1, 2}, {12, 2, 2}, {8, 2, 2},
+                                        {12, 1, 1}, {8, 1, 1}, {12, 0, 2}, {8, 0, 2}};
 constexpr int kTcVariantCount = sizeof(kTcVariants) / sizeof(kTcVariants[0]);
 
 extern "C" int bmg_scan_tc_variants() { return kTcVariantCount; }
@@ -231,14 +233,36 @@ extern "C" int bmg_scan_tc_variants() { return kTcVariantCount; }
 extern "C" void bmg_scan_tc_variant_name(int v, char* buf, size_t len)
 {
   if (v < 0 || v >= kTcVariantCount) v = 0;
-  snprintf(buf, len, "epilogue_warps=%d chains_per_tile=1/%d accumulators=%d", kTcVariants[v].epi,
-           kTcVariants[v].ct_div, kTcVariants[v].n_acc);
+  if (kTcVariants[v].ct_div == 0)
+    snprintf(buf, len, "epilogue_warps=%d chains_per_tile=A-in-TMEM accumulators=%d", kTcVariants[v].epi,
+             kTcVariants[v].n_acc);
+  else
+    snprintf(buf, len, "epilogue_warps=%d chains_per_tile=1/%d accumulators=%d", kTcVariants[v].epi,
+             kTcVariants[v].ct_div, kTcVariants[v].n_acc);
 }
 
 static uint32_t tc_cap(const DevConst* K, int v)
 {
   const int d = kTcVariants[v].ct_div;
+  // two accumulators and two A slots: each accumulator at most (512 - 2 x 64) / 2 columns
+  if (d == 0) return std::max(1u, (TC_TMEM_COLS - 2 * TC_A_COLS) / 2 / K->limbs_n);
   return (K->n_chains + d - 1) / d;
+}
+
+// 1 when shape v would run the same plan as an earlier shape (the tuner
+// skips it): the same epilogue warps, chains per tile and accumulators
+extern "C" int bmg_scan_tc_variant_redundant(const DevConst* K, int v)
+{
+  if (v <= 0 || v >= kTcVariantCount) return 0;
+  TcParams P;
+  if (!tc_plan(K, &P, tc_cap(K, v), (uint32_t)kTcVariants[v].n_acc)) return 1;
+  for (int u = 0; u < v; ++u) {
+    TcParams Q;
+    if (kTcVariants[u].epi != kTcVariants[v].epi || !tc_plan(K, &Q, tc_cap(K, u), (uint32_t)kTcVariants[u].n_acc))
+      continue;
+    if (Q.chains_tile == P.chains_tile && Q.n_acc == P.n_acc && Q.a_tmem == P.a_tmem) return 1;
+  }
+  return 0;
 }
 
 extern "C" int bmg_scan_tc_supported(const DevConst* K)
