@@ -403,7 +403,7 @@ extern "C" bmg_status bmg_load_bed(bmg_ctx* ctx, const uint8_t* packed, uint64_t
   int32_t* cnt = ctx->dalloc<int32_t>(2 * p);
   int32_t* miss = ctx->dalloc<int32_t>(p);
   {
-    const size_t chunk_rows = std::max<size_t>(1, (size_t(32) << 20) / stride);
+    const size_t chunk_rows = std::min<size_t>(p, std::max<size_t>(1, (size_t(32) << 20) / stride));
     ctx->ensure_stage(chunk_rows * stride);
     const unsigned nth = std::max(1u, std::min(8u, std::thread::hardware_concurrency()));
     int b = 0;
