@@ -75,6 +75,23 @@ static int sample_discrete_naive(const double* cumsum, int m, Rand& rng)
   throw std::logic_error("sample_discrete_naive reached end");
 }
 
+/* src/utils.cpp:73-101: `level` bisection steps, then a linear search */
+static size_t sample_discrete(const double* cumsum, size_t m, int level, Rand& rng)
+{
+  size_t a = 0, b = m - 1, c;
+  double z = cumsum[b];
+  double r = rng.rand_01() * z;
+  while (level > 0) {
+    c = (a + b) / 2;
+    if (r < cumsum[c]) b = c;
+    else a = c + 1;
+    --level;
+  }
+  for (size_t i = a; i <= b; ++i)
+    if (r < cumsum[i]) return i;
+  throw std::logic_error("sample_discrete reached end");
+}
+
 /* src/utils.cpp:144-152 */
 static void geometric_dist_cdf(int maxsize, double p, double* values)
 {
@@ -404,6 +421,13 @@ struct Prior {
     }
     if (g_a <= 0 || g_b <= 0 || std::isnan(g_a) || std::isnan(g_b))
       throw std::runtime_error("Invalid a or b.");
+  }
+  /* src/prior.hpp:212-219 */
+  double log_det_invQ_e() const
+  {
+    double log_sum_2 = 0.0;
+    for (size_t i = 1; i < m_e; ++i) log_sum_2 += log(inv_tau2_e[i]);
+    return log_sum_2;
   }
   /* src/prior.hpp:144-167 */
   double compute_log_change_on_add(const int* Ns, int nl, int type) const
@@ -790,7 +814,322 @@ struct Model {
       vlen = xcols;
     }
   }
+
+  /* src/symmmatrix.cpp:220-264: swap columns col and col + 1 of the upper
+     Cholesky factor (length llen, leading dimension cap) and restore it with
+     one Givens rotation; rotate v alongside */
+  void cholesky_swapadj(size_t col, std::vector<double>* vv)
+  {
+    double* col1 = l.data() + col * cap;
+    double* col2 = col1 + cap;
+    for (size_t i = 0; i < col + 2; ++i) std::swap(*col1++, *col2++);
+    *(--col2) = 0.0;
+    col1 = l.data() + col * cap + col;
+    col2 = col1 + 1;
+    double c, sn;
+    cblas_drotg(col1, col2, &c, &sn);
+    if (*col1 < 0) {
+      *col1 *= -1.0;
+      sn *= -1.0;
+      c *= -1.0;
+    }
+    double tmp;
+    for (size_t i = col + 1; i < llen; ++i) {
+      col1 += cap;
+      col2 = col1 + 1;
+      tmp = *col1 * sn - *col2 * c;
+      *col1 = *col2 * sn + *col1 * c;
+      *col2 = tmp;
+    }
+    if (vv) {
+      col1 = &(*vv)[col];
+      col2 = &(*vv)[col + 1];
+      tmp = *col1 * sn - *col2 * c;
+      *col1 = *col2 * sn + *col1 * c;
+      *col2 = tmp;
+    }
+  }
 };
+
+/* src/model.hpp:585-844: the last n terms of a model, whose 2^n sub-models
+   are visited by adding terms and moving them left (delayed rejection) */
+struct ExhModel : Model {
+  size_t model_size_ = 0, const_loci_ = 0, v_size_ = 0;
+  double log_model_prior_ = 0.0;
+
+  ExhModel(const Data* d, const DataModel* m, const Prior* p, Stats* s, size_t cap_) : Model(d, m, p, s, cap_) {}
+
+  double log_prob() const { return log_likelihood_ + log_model_prior_; }
+
+  double update_to_model(const Model& src, size_t const_loci)
+  {
+    llen = src.llen;
+    for (size_t c = 0; c < src.llen; ++c)
+      for (size_t r = 0; r <= c; ++r) l[c * cap + r] = src.l[c * cap + r];
+    std::memcpy(xy.data(), src.xy.data(), sizeof(double) * src.xcols);
+    vlen = src.vlen;
+    std::memcpy(v.data(), src.v.data(), sizeof(double) * src.vlen);
+    std::memcpy(inv.data(), src.inv.data(), sizeof(double) * src.xcols);
+    type_inds = src.type_inds;
+    x_types = src.x_types;
+    x_ind1 = src.x_ind1;
+    x_ind2 = src.x_ind2;
+    const_loci_ = const_loci;
+    model_size_ = const_loci_;
+    if (model_size_ > 0) {
+      if (AH == dm->types[type_inds[model_size_ - 1]]) v_size_ = x_ind2[model_size_ - 1] + 1;
+      else v_size_ = x_ind1[model_size_ - 1] + 1;
+    } else {
+      v_size_ = dm->m_e;
+    }
+    syx_plus_vs2 = prior->nus2_plus_yy - ddot(v_size_, v.data(), v.data());
+    log_det_invQ_plus_xx = 0;
+    for (size_t i = 0; i < v_size_; i++) log_det_invQ_plus_xx += log(L(i, i));
+    log_det_invQ = prior->log_det_invQ_e();
+    for (size_t i = dm->m_e; i < v_size_; ++i) log_det_invQ += log(inv[i]);
+    log_det_invQ *= 0.5;
+    log_likelihood_ = log_det_invQ - log_det_invQ_plus_xx + prior->minus_n_plus_nu_2 * log(syx_plus_vs2);
+    log_model_prior_ = 0.0;
+    for (int i = 0; i < 5; ++i) Ns[i] = 0;
+    for (size_t i = 0; i < model_size_; ++i) ++Ns[dm->types[type_inds[i]]];
+    return log_likelihood_ + log_model_prior_;
+  }
+
+  double update_on_add()
+  {
+    int type = dm->types[type_inds[model_size_]];
+    syx_plus_vs2 -= v[v_size_] * v[v_size_];
+    log_det_invQ += 0.5 * log(inv[v_size_]);
+    log_det_invQ_plus_xx += log(L(v_size_, v_size_));
+    ++v_size_;
+    if (AH == type) {
+      syx_plus_vs2 -= v[v_size_] * v[v_size_];
+      log_det_invQ += 0.5 * log(inv[v_size_]);
+      log_det_invQ_plus_xx += log(L(v_size_, v_size_));
+      ++v_size_;
+    }
+    log_likelihood_ = log_det_invQ - log_det_invQ_plus_xx + prior->minus_n_plus_nu_2 * log(syx_plus_vs2);
+    log_model_prior_ += prior->compute_log_change_on_add(Ns, (int)model_size_, type);
+    ++Ns[type];
+    ++model_size_;
+    return log_likelihood_ + log_model_prior_;
+  }
+
+  double update_on_moveleft()
+  {
+    --model_size_;
+    size_t ind_keep = model_size_;
+    size_t ind_rem = model_size_ - 1;
+    int type_keep = dm->types[type_inds[ind_keep]];
+    int type_rem = dm->types[type_inds[ind_rem]];
+    --v_size_;
+    syx_plus_vs2 += v[v_size_] * v[v_size_];
+    log_det_invQ_plus_xx -= log(L(v_size_, v_size_));
+    if (AH == type_keep) {
+      --v_size_;
+      syx_plus_vs2 += v[v_size_] * v[v_size_];
+      log_det_invQ_plus_xx -= log(L(v_size_, v_size_));
+    }
+    --v_size_;
+    syx_plus_vs2 += v[v_size_] * v[v_size_];
+    log_det_invQ -= 0.5 * log(inv[v_size_]);
+    log_det_invQ_plus_xx -= log(L(v_size_, v_size_));
+    if (AH == type_rem) {
+      --v_size_;
+      syx_plus_vs2 += v[v_size_] * v[v_size_];
+      log_det_invQ -= 0.5 * log(inv[v_size_]);
+      log_det_invQ_plus_xx -= log(L(v_size_, v_size_));
+    }
+    std::swap(type_inds[ind_keep], type_inds[ind_rem]);
+    if (AH == type_rem) {
+      if (AH == type_keep) {
+        size_t swap_ind = x_ind2[ind_rem];
+        cholesky_swapadj(swap_ind, &v);
+        ++swap_ind;
+        cholesky_swapadj(swap_ind, &v);
+        swap_ind -= 2;
+        cholesky_swapadj(swap_ind, &v);
+        ++swap_ind;
+        cholesky_swapadj(swap_ind, &v);
+        std::swap(xy[x_ind1[ind_keep]], xy[x_ind2[ind_rem]]);
+        std::swap(xy[x_ind1[ind_keep]], xy[x_ind2[ind_keep]]);
+        std::swap(xy[x_ind1[ind_rem]], xy[x_ind2[ind_rem]]);
+        std::swap(xy[x_ind1[ind_keep]], xy[x_ind2[ind_rem]]);
+        std::swap(inv[x_ind1[ind_keep]], inv[x_ind2[ind_rem]]);
+        std::swap(inv[x_ind1[ind_keep]], inv[x_ind2[ind_keep]]);
+        std::swap(inv[x_ind1[ind_rem]], inv[x_ind2[ind_rem]]);
+        std::swap(inv[x_ind1[ind_keep]], inv[x_ind2[ind_rem]]);
+      } else {
+        size_t swap_ind = x_ind2[ind_rem];
+        cholesky_swapadj(swap_ind, &v);
+        --swap_ind;
+        cholesky_swapadj(swap_ind, &v);
+        std::swap(xy[x_ind2[ind_rem]], xy[x_ind1[ind_keep]]);
+        std::swap(xy[x_ind1[ind_rem]], xy[x_ind2[ind_rem]]);
+        std::swap(inv[x_ind2[ind_rem]], inv[x_ind1[ind_keep]]);
+        std::swap(inv[x_ind1[ind_rem]], inv[x_ind2[ind_rem]]);
+        std::swap(x_types[x_ind2[ind_rem]], x_types[x_ind1[ind_keep]]);
+        std::swap(x_types[x_ind1[ind_rem]], x_types[x_ind2[ind_rem]]);
+        x_ind2[ind_keep] = x_ind1[ind_keep];
+        --x_ind1[ind_keep];
+      }
+    } else {
+      if (AH == type_keep) {
+        size_t swap_ind = x_ind1[ind_rem];
+        cholesky_swapadj(swap_ind, &v);
+        ++swap_ind;
+        cholesky_swapadj(swap_ind, &v);
+        std::swap(xy[x_ind1[ind_rem]], xy[x_ind1[ind_keep]]);
+        std::swap(xy[x_ind1[ind_keep]], xy[x_ind2[ind_keep]]);
+        std::swap(inv[x_ind1[ind_rem]], inv[x_ind1[ind_keep]]);
+        std::swap(inv[x_ind1[ind_keep]], inv[x_ind2[ind_keep]]);
+        std::swap(x_types[x_ind1[ind_rem]], x_types[x_ind1[ind_keep]]);
+        std::swap(x_types[x_ind1[ind_keep]], x_types[x_ind2[ind_keep]]);
+        x_ind2[ind_rem] = x_ind1[ind_keep];
+        x_ind1[ind_keep] = x_ind2[ind_keep];
+      } else {
+        size_t swap_ind = x_ind1[ind_rem];
+        cholesky_swapadj(swap_ind, &v);
+        std::swap(xy[x_ind1[ind_keep]], xy[x_ind1[ind_rem]]);
+        std::swap(inv[x_ind1[ind_keep]], inv[x_ind1[ind_rem]]);
+        std::swap(x_types[x_ind1[ind_keep]], x_types[x_ind1[ind_rem]]);
+      }
+    }
+    syx_plus_vs2 -= v[v_size_] * v[v_size_];
+    log_det_invQ_plus_xx += log(L(v_size_, v_size_));
+    ++v_size_;
+    if (AH == type_keep) {
+      syx_plus_vs2 -= v[v_size_] * v[v_size_];
+      log_det_invQ_plus_xx += log(L(v_size_, v_size_));
+      ++v_size_;
+    }
+    log_likelihood_ = log_det_invQ - log_det_invQ_plus_xx + prior->minus_n_plus_nu_2 * log(syx_plus_vs2);
+    log_model_prior_ += prior->compute_log_change_on_rem(Ns, (int)model_size_ + 1, type_rem);
+    --Ns[type_rem];
+    return log_likelihood_ + log_model_prior_;
+  }
+
+  double update_on_twonewswap()
+  {
+    update_on_add();
+    update_on_add();
+    return update_on_moveleft();
+  }
+};
+
+/* src/sampler.cpp:882-978: the log probabilities of all 2^n_inds sub-models
+   of the exhaustive model's last n_inds terms, by adds and left moves */
+static void compute_exhaustive_modelset(size_t n_inds, ExhModel* exhmodel, double* log_model_probabilities,
+                                        double& max_log_model)
+{
+  size_t nmodels = 0, tmp;
+  size_t cmodel_binary = 0;
+  int model_size = 0;
+  std::vector<size_t> cmodel_inds(n_inds);
+  for (size_t i = 0; i < n_inds; ++i) cmodel_inds[i] = i;
+  log_model_probabilities[cmodel_binary] = exhmodel->log_prob();
+  max_log_model = log_model_probabilities[cmodel_binary];
+  for (size_t i = 0; i < n_inds; ++i) {
+    ++model_size;
+    if (i > 1) {
+      ++model_size;
+      exhmodel->update_on_add();
+    }
+    cmodel_binary = (size_t)std::pow(2, model_size) - 1;
+    log_model_probabilities[cmodel_binary] = exhmodel->update_on_add();
+    if (log_model_probabilities[cmodel_binary] > max_log_model) max_log_model = log_model_probabilities[cmodel_binary];
+    for (size_t j = 0; j < i; ++j) {
+      --model_size;
+      tmp = cmodel_inds[model_size - 1];
+      cmodel_inds[model_size - 1] = cmodel_inds[model_size];
+      cmodel_inds[model_size] = tmp;
+      cmodel_binary &= ~(1 << tmp);
+      log_model_probabilities[cmodel_binary] = exhmodel->update_on_moveleft();
+      if (log_model_probabilities[cmodel_binary] > max_log_model) max_log_model = log_model_probabilities[cmodel_binary];
+    }
+    nmodels = (size_t)std::pow(2, i) - i - 1;
+    size_t j = 0;
+    size_t K, nK = 0;
+    char do_lefts = 0;
+    while (j < nmodels) {
+      if (do_lefts < 2) {
+        ++model_size;
+        tmp = cmodel_inds[model_size];
+        cmodel_inds[model_size] = cmodel_inds[model_size - 1];
+        cmodel_inds[model_size - 1] = tmp;
+        cmodel_binary |= (1 << tmp);
+        log_model_probabilities[cmodel_binary] = exhmodel->update_on_twonewswap();
+        if (log_model_probabilities[cmodel_binary] > max_log_model)
+          max_log_model = log_model_probabilities[cmodel_binary];
+        ++j;
+        ++do_lefts;
+      } else {
+        ++nK;
+        K = 0;
+        while (((nK >> K) & 1) == 0) K++;
+        for (size_t k = 0; k <= K; ++k) {
+          --model_size;
+          tmp = cmodel_inds[model_size - 1];
+          cmodel_inds[model_size - 1] = cmodel_inds[model_size];
+          cmodel_inds[model_size] = tmp;
+          cmodel_binary &= ~(1 << tmp);
+          log_model_probabilities[cmodel_binary] = exhmodel->update_on_moveleft();
+          if (log_model_probabilities[cmodel_binary] > max_log_model)
+            max_log_model = log_model_probabilities[cmodel_binary];
+          ++j;
+        }
+        do_lefts = 0;
+      }
+    }
+  }
+}
+
+/* src/sampler.cpp:980-1049: adds the log proposal probability of reaching
+   each sub-model from the "empty" one (adds in order, removals in reverse) */
+static void compute_proposal_probs_for_exh_modelset(bool use_types, int n_inds,
+                                                    const unsigned char* bit_to_normalized_order,
+                                                    const double* q_add, const double* q_rem, double z_add,
+                                                    double z_rem, size_t const_loci, size_t m_g,
+                                                    const double* log_q_add_types, double* log_prop_probs)
+{
+  std::vector<char> isadd(n_inds);
+  unsigned long nmodels = (unsigned long)std::pow(2, n_inds);
+  for (unsigned long i = 0; i < nmodels; ++i) {
+    size_t max_adds = m_g - const_loci;
+    size_t max_rems = const_loci;
+    double z_a = z_add;
+    double z_r = z_rem;
+    for (int j = 0; j < n_inds; ++j) {
+      unsigned char bit = (i >> j) & 1;
+      unsigned char nind = bit_to_normalized_order[j];
+      if (bit) {
+        isadd[nind] = false;
+        z_a -= q_add[nind];
+        z_r += q_rem[nind];
+        ++max_rems;
+        --max_adds;
+      } else {
+        isadd[nind] = true;
+      }
+    }
+    int last_rem_pos = n_inds - 1;
+    for (int j = 0; j < n_inds; ++j) {
+      if (max_adds > 0 && max_rems > 0) log_prop_probs[i] += kLogHalf;
+      if (isadd[j]) {
+        --max_adds;
+        log_prop_probs[i] += log(q_add[j]) - log(z_a);
+        z_a -= q_add[j];
+        if (use_types) log_prop_probs[i] += log_q_add_types[j];
+      } else {
+        --max_rems;
+        while (isadd[last_rem_pos]) --last_rem_pos;
+        log_prop_probs[i] += log(q_rem[last_rem_pos]) - log(z_r);
+        z_r -= q_rem[last_rem_pos];
+        --last_rem_pos;
+      }
+    }
+  }
+}
 
 /* src/prior.cpp:30-69 */
 double Prior::sample_alpha(Model* model, Rand& rng)
@@ -1055,6 +1394,11 @@ struct Sampler {
   double pves[3];
   std::vector<double> r_cm, r_om, xs;  /* RB scratch */
   Trace tr;
+  /* delayed rejection (src/sampler.hpp:163-169, 272-281) */
+  unsigned char delay_rejection = 0;
+  ExhModel* exh = nullptr;
+  std::vector<double> dr_model_probabilities, dr_q_add, dr_q_rem, dr_log_q_add_types;
+  std::vector<unsigned char> dr_bit_to_normalized_order;
 
   Sampler(const bmg_options& opt, const Data* d, const PreXX* p, uint32_t seed_)
   : o(opt), data(d), pre(p), n_iter(0), do_n_iter(opt.do_n_iter), n_accepted(0),
@@ -1085,7 +1429,7 @@ struct Sampler {
     size_t cap = opt.max_model_size ? opt.max_model_size : 1024;
     cur = new Model(d, dm, prior, &stats, cap);
     nm = new Model(d, dm, prior, &stats, cap);
-    stats.n_full += 1;  /* the reference also builds an ExhModel (src/sampler.hpp:203) */
+    exh = new ExhModel(d, dm, prior, &stats, cap);  /* src/sampler.hpp:203 */
     p_proposal.assign(m_g, 0.0);
     if (n_types > 1) p_proposal_types.assign(m_g * n_types, 0.0);
     p_rao.assign(m_g, 0.0);
@@ -1101,6 +1445,14 @@ struct Sampler {
     q_add_min = 1.0 / (m_g - opt.e_qg);
     q_rem_min = 1.0 / opt.e_qg;
     max_move_size = (unsigned char)std::min(std::min(m_g, (size_t)255), (size_t)opt.max_move_size);
+    delay_rejection = (unsigned char)std::min((size_t)max_move_size, (size_t)opt.delay_rejection);
+    if (delay_rejection > 0) {
+      dr_model_probabilities.assign((size_t)std::pow(2, delay_rejection), 0.0);
+      dr_q_add.assign(delay_rejection, 0.0);
+      dr_q_rem.assign(delay_rejection, 0.0);
+      dr_log_q_add_types.assign(delay_rejection, 0.0);
+      dr_bit_to_normalized_order.assign(delay_rejection, 0);
+    }
     max_nbh = opt.max_SNP_neighborhood_size;
     p_move_size = opt.p_move_size;
     p_move_size_nbs = opt.p_move_size_nbs;
@@ -1132,7 +1484,7 @@ struct Sampler {
   }
   ~Sampler()
   {
-    delete dd_add; delete dd_rem; delete cur; delete nm; delete prior; delete dm;
+    delete dd_add; delete dd_rem; delete cur; delete nm; delete exh; delete prior; delete dm;
   }
 
   /* src/sampler.hpp:351-362 */
@@ -1464,7 +1816,7 @@ struct Sampler {
     prepare_add_new_term_nm(type, itv);
   }
 
-  /* src/sampler.hpp:899-1123 (delayed rejection off) */
+  /* src/sampler.hpp:899-1123 */
   unsigned char do_multistep_additions_and_removals()
   {
     movesize = (unsigned char)(sample_discrete_naive(q_p_move_size.data(), max_move_size, rng) + 1);
@@ -1475,12 +1827,16 @@ struct Sampler {
     backward_prepare_addrem(lqb, movesize);
     double log_r = lqb - lqf;
     log_r += lmpc + nm->log_likelihood_ - cur->log_likelihood_;
-    r_ms_sum[movesize - 1] += (log_r >= 0 ? 1.0 : exp(log_r));
+    if (delay_rejection == 0) r_ms_sum[movesize - 1] += (log_r >= 0 ? 1.0 : exp(log_r));
     r_ms_n[movesize - 1] += 1.0;
     if (log_r >= 0 || log(rng.rand_01()) <= log_r) {
       cur->copy_from(*nm);
+      if (delay_rejection != 0) r_ms_sum[movesize - 1] += 1.0;
       return movesize;
     }
+    /* the delayed rejection can propose the current model only for moves of
+       more than one SNP */
+    if (movesize <= delay_rejection && movesize > 1) return delayed_rejection(ms_rem);
     nm->copy_from(*cur);
     for (unsigned char i = 0; i < movesize; ++i) {
       size_t ind = move_inds[i];
@@ -1489,6 +1845,188 @@ struct Sampler {
     }
     return 0;
   }
+  /* src/sampler.hpp:1009-1028 (also :1571-1595): each sub-model i below
+     2^(movesize-1) is paired with its complement; the pair's weight is the
+     difference of their probabilities, carried by the likelier one (the
+     other's entry records which: -1 when the complement, 1 when i).  Samples
+     a pair by its cumulative weight and returns the sub-model that carries
+     it. */
+  unsigned long dr_sample_pair(double max_log_model)
+  {
+    unsigned long nmodels = (unsigned long)std::pow(2, movesize);
+    unsigned long mask = nmodels - 1;
+    double* pm = dr_model_probabilities.data();
+    double sum = 0.0;
+    for (unsigned long i = 0; i < nmodels / 2; ++i) {
+      unsigned int j = (~i) & mask;
+      double a = pm[j] - pm[i];
+      if (a > 0) {
+        pm[i] = exp(pm[j] - max_log_model) * (1 - exp(-a));
+        pm[j] = -1.0;
+      } else {
+        pm[i] = exp(pm[i] - max_log_model) * (1 - exp(a));
+        pm[j] = 1.0;
+      }
+      pm[i] += sum;
+      sum = pm[i];
+    }
+    unsigned long sampled_model = sample_discrete(pm, nmodels / 2, (int)movesize / 2 - 3, rng);
+    if (pm[(~sampled_model) & mask] < 0) sampled_model = (~sampled_model) & mask;
+    return sampled_model;
+  }
+
+  /* src/sampler.hpp:1547-1618: the same second stage after a rejected
+     state change of movesize > 1 SNPs near a central in-model SNP; sub-model
+     bits are the added SNPs then the removed ones, and each sub-model's
+     probability includes choosing the central SNP among its in-model SNPs */
+  unsigned char delayed_rejection_statechange(unsigned char ms_add, unsigned char ms_rem)
+  {
+    size_t const_loci = cur->size() - ms_rem;
+    unsigned long newmodel_binary = ((1 << ms_add) - 1);
+    for (unsigned char i_move = 0; i_move < ms_rem; ++i_move) {
+      size_t ind = move_inds_rem[i_move];
+      int cmi = cur->model_inds[ind];
+      int t_ind = cur->type_inds[cmi];
+      if (dm->types[t_ind] == AH) {
+        double itv2[2] = {cur->inv[cur->x_ind1[cmi]], cur->inv[cur->x_ind2[cmi]]};
+        nm->add_term((uint32_t)ind, t_ind, itv2);
+      } else {
+        double itv1 = cur->inv[cur->x_ind1[cmi]];
+        nm->add_term((uint32_t)ind, t_ind, &itv1);
+      }
+    }
+    exh->update_to_model(*nm, const_loci);
+    double max_log_model;
+    compute_exhaustive_modelset(movesize, exh, dr_model_probabilities.data(), max_log_model);
+    unsigned long nmodels = (unsigned long)std::pow(2, movesize);
+    unsigned long mask = nmodels - 1;
+    for (unsigned int i = 0; i < nmodels; ++i)
+      dr_model_probabilities[i] -= log(const_loci + __builtin_popcount(i));
+    unsigned long sampled_model = dr_sample_pair(max_log_model);
+    unsigned char moved = 0;
+    if (sampled_model == ((~newmodel_binary) & mask)) {
+      nm->copy_from(*cur);
+    } else {
+      for (unsigned char i_move = 0; i_move < movesize; ++i_move) {
+        if (1 == ((sampled_model >> i_move) & 1)) {
+          if (1 == ((newmodel_binary >> i_move) & 1)) {
+            ++moved;
+            size_t ind = move_inds_add[i_move];
+            dd_add->adddate(ind);
+            dd_rem->remdate(ind);
+          }
+        } else {
+          if (0 == ((newmodel_binary >> i_move) & 1)) {
+            ++moved;
+            size_t ind = move_inds_rem[i_move - ms_add];
+            dd_add->remdate(ind);
+            dd_rem->adddate(ind);
+          }
+        }
+      }
+      unsigned long removals = mask & sampled_model;
+      for (unsigned char i = 0; i < movesize; ++i) {
+        if ((removals & 1) == 0) {
+          nm->remove_term((int)(const_loci + i));
+          --const_loci;
+        }
+        removals >>= 1;
+      }
+      cur->copy_from(*nm);
+    }
+    return moved;
+  }
+
+  /* src/sampler.hpp:929-1098: after a rejected move of movesize > 1 SNPs,
+     sample among all 2^movesize sub-models of the involved SNPs (the current
+     and the proposed model excepted), pairing each sub-model with its
+     complement so the second stage keeps detailed balance */
+  unsigned char delayed_rejection(unsigned char ms_rem)
+  {
+    size_t const_loci = cur->size() - ms_rem;
+    unsigned char ms_add = movesize - ms_rem;
+    double z_add = dd_add->total_w;
+    double z_rem = dd_rem->total_w;
+    unsigned long newmodel_binary = ((1 << ms_add) - 1);
+    for (unsigned char i_move = 0; i_move < movesize; ++i_move) {
+      size_t ind = move_inds[i_move];
+      if (move_isadd[i_move]) {
+        z_add += q_add[ind];
+        z_rem -= q_rem[ind];
+      } else {
+        int cmi = cur->model_inds[ind];
+        int t_ind = cur->type_inds[cmi];
+        if (dm->types[t_ind] == AH) {
+          double itv2[2] = {cur->inv[cur->x_ind1[cmi]], cur->inv[cur->x_ind2[cmi]]};
+          nm->add_term((uint32_t)ind, t_ind, itv2);
+        } else {
+          double itv1 = cur->inv[cur->x_ind1[cmi]];
+          nm->add_term((uint32_t)ind, t_ind, &itv1);
+        }
+      }
+    }
+    for (unsigned char i_move = 0; i_move < movesize; ++i_move) {
+      size_t ind = (size_t)move_inds_map[i_move];
+      size_t model_ind = (size_t)nm->model_inds[ind];
+      dr_bit_to_normalized_order[model_ind - const_loci] = i_move;
+      dr_q_add[i_move] = q_add[ind];
+      dr_q_rem[i_move] = q_rem[ind];
+      if (n_types > 1) {
+        unsigned char t_ind = nm->type_inds[nm->model_inds[ind]];
+        dr_log_q_add_types[i_move] = log(q_add_types[ind * n_types + t_ind] / q_p_add_types[ind * n_types + n_types - 1]);
+      }
+    }
+    exh->update_to_model(*nm, const_loci);
+    double max_log_model;
+    compute_exhaustive_modelset(movesize, exh, dr_model_probabilities.data(), max_log_model);
+    compute_proposal_probs_for_exh_modelset(use_types, movesize, dr_bit_to_normalized_order.data(), dr_q_add.data(),
+                                            dr_q_rem.data(), z_add, z_rem, const_loci, m_g,
+                                            dr_log_q_add_types.data(), dr_model_probabilities.data());
+    unsigned long nmodels = (unsigned long)std::pow(2, movesize);
+    unsigned long mask = nmodels - 1;
+    unsigned long sampled_model = dr_sample_pair(max_log_model);
+    unsigned char moved = 0;
+    if (sampled_model == ((~newmodel_binary) & mask)) {
+      nm->copy_from(*cur);
+      for (unsigned char i_move = 0; i_move < movesize; ++i_move) {
+        size_t ind = move_inds[i_move];
+        if (move_isadd[i_move]) { dd_add->remdate(ind); dd_rem->adddate(ind); }
+        else { dd_add->adddate(ind); dd_rem->remdate(ind); }
+      }
+    } else {
+      for (unsigned char i_move = 0; i_move < movesize; ++i_move) {
+        if (1 == ((sampled_model >> i_move) & 1)) {
+          if (0 == ((newmodel_binary >> i_move) & 1)) {
+            size_t ind = (size_t)move_inds_map[dr_bit_to_normalized_order[i_move]];
+            dd_add->adddate(ind);
+            dd_rem->remdate(ind);
+          } else {
+            ++moved;
+          }
+        } else {
+          if (1 == ((newmodel_binary >> i_move) & 1)) {
+            size_t ind = (size_t)move_inds_map[dr_bit_to_normalized_order[i_move]];
+            dd_add->remdate(ind);
+            dd_rem->adddate(ind);
+          } else {
+            ++moved;
+          }
+        }
+      }
+      unsigned long removals = mask & sampled_model;
+      for (unsigned char i = 0; i < movesize; ++i) {
+        if ((removals & 1) == 0) {
+          nm->remove_term((int)(const_loci + i));
+          --const_loci;
+        }
+        removals >>= 1;
+      }
+      r_ms_sum[movesize - 1] += (double)moved / (double)movesize;
+      cur->copy_from(*nm);
+    }
+    return moved;
+  }
+
   /* src/sampler.hpp:1126-1165 */
   void prepare_addrem(double& lqf, unsigned char& n_rem, unsigned char ms)
   {
@@ -1725,6 +2263,7 @@ struct Sampler {
       }
       return movesize;
     }
+    if (movesize <= delay_rejection && movesize > 1) return delayed_rejection_statechange(ms_add, ms_rem);
     nm->copy_from(*cur);
     return 0;
   }
@@ -1941,7 +2480,6 @@ extern "C" int bmgport_create(const bmg_options* opt, const uint8_t* packed, con
 {
   try {
     if (opt->sampler_type != 0) throw std::runtime_error("only the PMV sampler is restated");
-    if (opt->delay_rejection != 0) throw std::runtime_error("delayed rejection is not restated");
     bmgport* P = new bmgport();
     P->p.opt = *opt;
     P->p.seeds.assign(opt->seeds, opt->seeds + opt->n_chains);

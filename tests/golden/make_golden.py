@@ -10,7 +10,8 @@ Runs only where the reference tree and its oracle build (oracle/_ref) exist:
      reference's test configurations and its example dataset, with every
      input file stored in the fixture.
 
-Usage:  python tests/golden/make_golden.py [REFERENCE_DIR]
+Usage:  python tests/golden/make_golden.py [REFERENCE_DIR [CASE ...]]
+(all cases when none is named)
 """
 import os
 import re
@@ -74,7 +75,7 @@ adaptation = {adaptation}
 verbosity = {verbosity}
 thin = {thin}
 n_sample_tau2_and_missing = {nst}
-delay_rejection = 0
+delay_rejection = {dr}
 p_move_size = 0.2
 p_move_size_nbc = 0.25
 p_move_size_nbs = 0.7
@@ -125,6 +126,7 @@ def run_case(name, files, **kw):
     kw.setdefault("nbh", 20)
     kw.setdefault("maxms", 20)
     kw.setdefault("indiv", 0)
+    kw.setdefault("dr", 0)
     ini = INI.format(**kw)
     with tempfile.TemporaryDirectory() as d:
         for fn, data in files.items():
@@ -146,22 +148,14 @@ def run_case(name, files, **kw):
     np.savez_compressed(os.path.join(HERE, "ref_%s.npz" % name), **out)
 
 
-def main():
-    if not os.path.exists(REF_BIN):
-        raise SystemExit("build oracle/_ref first (make -C oracle)")
-    known_answers()
+def cases():
+    """name -> (files, run_case keywords)"""
     tdir = os.path.join(REF, "src/tests/testdata")
     rd = lambda path: np.frombuffer(open(path, "rb").read(), dtype=np.uint8)
     small = {"data.bed": rd(os.path.join(tdir, "small_modelspace.bed")),
              "data.fam": rd(os.path.join(tdir, "small_modelspace.fam"))}
-    # the exhaustive-posterior test setting (src/tests/testdata/small_modelspace_tau2.ini),
-    # shortened and with delayed rejection off
-    run_case("small", small, n=30, p=7, iters=3000, n_rao=10, burnin=50, thin=5, nst=10,
-             chains=2, seeds="1245,77", types="A", e_qg=2, var_qg=2)
-    run_case("small_types", small, n=30, p=7, iters=2000, n_rao=10, burnin=20, thin=2, nst=6,
-             chains=1, seeds="99", types="A,AH", e_qg=2, var_qg=2, indiv=1, maxms=5, nbh=3)
     # the example dataset (testdata/testdata.ini): first 1500 SNPs, its covariate
-    # and alternate phenotype files, individual tau2, n_rao 10
+    # and alternate phenotype files
     ex = os.path.join(REF, "testdata")
     bed = rd(os.path.join(ex, "testdata.bed"))
     n = 1000
@@ -170,13 +164,45 @@ def main():
     sub = np.concatenate([bed[:3], bed[3:3 + p * stride]])
     files = {"data.bed": sub, "data.fam": rd(os.path.join(ex, "testdata.fam")),
              "data.e": rd(os.path.join(ex, "testdata.e")), "data.y": rd(os.path.join(ex, "testdata.y"))}
-    run_case("example", files, n=n, p=p, iters=600, n_rao=10, burnin=20, thin=10, nst=10,
-             chains=2, seeds="1234,2345", types="A", e_qg=20, var_qg=300, m_e=2,
-             efile="file_e = {DIR}/data.e\n", yfile="file_y = {DIR}/data.y\n", indiv=1,
-             verbosity=100)
-    run_case("example_types", files, n=n, p=p, iters=400, n_rao=20, burnin=5, thin=4, nst=8,
-             chains=1, seeds="4321", types="A,H,D,R,AH", e_qg=20, var_qg=300, m_e=2,
-             efile="file_e = {DIR}/data.e\n", yfile="file_y = {DIR}/data.y\n", adaptation=1, acpt=0.3)
+    efiles = dict(efile="file_e = {DIR}/data.e\n", yfile="file_y = {DIR}/data.y\n")
+    return {
+        # the exhaustive-posterior test setting (src/tests/testdata/small_modelspace_tau2.ini),
+        # shortened and with delayed rejection off
+        "small": (small, dict(n=30, p=7, iters=3000, n_rao=10, burnin=50, thin=5, nst=10,
+                              chains=2, seeds="1245,77", types="A", e_qg=2, var_qg=2)),
+        "small_types": (small, dict(n=30, p=7, iters=2000, n_rao=10, burnin=20, thin=2, nst=6,
+                                    chains=1, seeds="99", types="A,AH", e_qg=2, var_qg=2, indiv=1, maxms=5, nbh=3)),
+        # individual tau2, n_rao 10
+        "example": (files, dict(n=n, p=p, iters=600, n_rao=10, burnin=20, thin=10, nst=10,
+                                chains=2, seeds="1234,2345", types="A", e_qg=20, var_qg=300, m_e=2,
+                                indiv=1, verbosity=100, **efiles)),
+        "example_types": (files, dict(n=n, p=p, iters=400, n_rao=20, burnin=5, thin=4, nst=8,
+                                      chains=1, seeds="4321", types="A,H,D,R,AH", e_qg=20, var_qg=300, m_e=2,
+                                      adaptation=1, acpt=0.3, **efiles)),
+        # delayed rejection: the small setting with it on (moves of up to 5 SNPs),
+        # the example dataset with the example configuration's delay_rejection = 10,
+        # and an A,AH case for the left moves of two-column terms
+        "small_dr": (small, dict(n=30, p=7, iters=3000, n_rao=10, burnin=50, thin=5, nst=10,
+                                 chains=2, seeds="1245,77", types="A", e_qg=2, var_qg=2, maxms=5, dr=5)),
+        "example_dr": (files, dict(n=n, p=p, iters=500, n_rao=10, burnin=20, thin=10, nst=10,
+                                   chains=2, seeds="1234,2345", types="A", e_qg=20, var_qg=300, m_e=2,
+                                   dr=10, **efiles)),
+        "small_types_dr": (small, dict(n=30, p=7, iters=2000, n_rao=10, burnin=20, thin=2, nst=6,
+                                       chains=1, seeds="99", types="A,AH", e_qg=2, var_qg=2, maxms=5, nbh=3,
+                                       dr=5)),
+    }
+
+
+def main():
+    if not os.path.exists(REF_BIN):
+        raise SystemExit("build oracle/_ref first (make -C oracle)")
+    names = sys.argv[2:]
+    if not names:
+        known_answers()
+    for name, (files, kw) in cases().items():
+        if names and name not in names:
+            continue
+        run_case(name, files, **kw)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

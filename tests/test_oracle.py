@@ -165,9 +165,11 @@ def test_rb_closed_form(bmg, oracle):
         assert pr[j] == pytest.approx(e / (1 + e), abs=1e-10)
 
 
-@pytest.mark.parametrize("name", ["small", "small_types", "example", "example_types"])
+@pytest.mark.parametrize("name", ["small", "small_types", "example", "example_types", "small_dr", "example_dr",
+                                  "small_types_dr"])
 def test_oracle_matches_reference_traces(bmg, oracle, tmp_path, name):
-    """The oracle reproduces the compiled reference's traces bit for bit."""
+    """The oracle reproduces the compiled reference's traces bit for bit (the
+    *_dr cases with delayed rejection on)."""
     z = H.golden("ref_" + name)
     ini = H.materialize(z, tmp_path)
     opt = bmg.options_from_ini(ini)
