@@ -66,6 +66,8 @@ def lib():
         L.bmgport_get_genotypes.argtypes = [C.c_void_p, C.c_uint32, C.c_uint64, C.c_void_p]
         L.bmgport_model_lml.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p,
                                         C.c_void_p, C.c_void_p]
+        L.bmgport_exh_modelset.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p,
+                                           C.c_uint32, C.c_void_p, C.c_void_p]
         L.bmgport_destroy.argtypes = [C.c_void_p]
         _lib = L
     return _lib
@@ -196,6 +198,20 @@ class Port:
                                    _ptr(out)) != 0:
             raise RuntimeError("oracle model failed")
         return out
+
+    def exh_modelset(self, snps, t_inds, inv_pairs, const_loci):
+        """(exhaustive, direct): log probabilities of the 2^m sub-models of the
+        last m = len(snps) - const_loci terms, by the delayed-rejection
+        enumeration and by building each model from scratch."""
+        snps = np.ascontiguousarray(snps, dtype=np.uint32)
+        t_inds = np.ascontiguousarray(t_inds, dtype=np.uint8)
+        inv = np.ascontiguousarray(inv_pairs, dtype=np.float64).reshape(-1)
+        nm = len(snps) - const_loci
+        exh, direct = np.zeros(1 << nm), np.zeros(1 << nm)
+        if lib().bmgport_exh_modelset(self.h, len(snps), _ptr(snps), _ptr(t_inds), _ptr(inv),
+                                      const_loci, _ptr(exh), _ptr(direct)) != 0:
+            raise RuntimeError("oracle exhaustive model set failed")
+        return exh, direct
 
 
 def read_ref_outputs(basename, chain, m_g, n_types=1):

@@ -2692,4 +2692,52 @@ extern "C" int bmgport_model_lml(bmgport* P, uint32_t n_add, const uint32_t* snp
   }
 }
 
+/* The known-answer check of src/tests/model_tests.hpp:92-235: the model holds
+   n_terms terms, of which the first const_loci stay; the exhaustive model
+   set over the other m = n_terms - const_loci gives, per subset bit mask,
+   the log likelihood plus the log prior change of adding that subset
+   (exh_out), which must equal the same model built directly term by term
+   (direct_out). */
+extern "C" int bmgport_exh_modelset(bmgport* P, uint32_t n_terms, const uint32_t* snps,
+                                    const uint8_t* t_inds, const double* itv, uint32_t const_loci,
+                                    double* exh_out, double* direct_out)
+{
+  try {
+    if (const_loci > n_terms || n_terms - const_loci > 16) return 1;
+    Sampler* s = P->p.chains.at(0);
+    Stats st;
+    size_t cap = s->cur->cap;
+    Model m(P->p.data, s->dm, s->prior, &st, cap);
+    for (uint32_t i = 0; i < n_terms; ++i) m.add_term(snps[i], t_inds[i], &itv[2 * i]);
+    ExhModel exh(P->p.data, s->dm, s->prior, &st, cap);
+    exh.update_to_model(m, const_loci);
+    size_t nm = n_terms - const_loci;
+    double max_log_model;
+    compute_exhaustive_modelset(nm, &exh, exh_out, max_log_model);
+    for (size_t mask = 0; mask < ((size_t)1 << nm); ++mask) {
+      Model d(P->p.data, s->dm, s->prior, &st, cap);
+      int Ns[5] = {0, 0, 0, 0, 0};
+      for (uint32_t i = 0; i < const_loci; ++i) {
+        d.add_term(snps[i], t_inds[i], &itv[2 * i]);
+        ++Ns[s->dm->types[t_inds[i]]];
+      }
+      int nl = (int)const_loci;
+      double lp = 0;
+      for (size_t j = 0; j < nm; ++j) {
+        if (!((mask >> j) & 1)) continue;
+        size_t k = const_loci + j;
+        int type = s->dm->types[t_inds[k]];
+        d.add_term(snps[k], t_inds[k], &itv[2 * k]);
+        lp += s->prior->compute_log_change_on_add(Ns, nl, type);
+        ++Ns[type];
+        ++nl;
+      }
+      direct_out[mask] = lp + d.log_likelihood_;
+    }
+    return 0;
+  } catch (...) {
+    return 1;
+  }
+}
+
 extern "C" void bmgport_destroy(bmgport* P) { delete P; }

@@ -54,6 +54,12 @@ int bmgport_get_genotypes(bmgport* P, uint32_t type, uint64_t snp, double* out);
 int bmgport_model_lml(bmgport* P, uint32_t n_add, const uint32_t* snps,
                       const uint8_t* t_inds, const double* inv_tau2_alpha2,
                       double* lml_after_each);
+/* exhaustive model set of the last n_terms - const_loci terms (2^m log
+   probabilities) and the same probabilities from models built directly
+   (src/sampler.cpp:882-978, src/tests/model_tests.hpp:92-235) */
+int bmgport_exh_modelset(bmgport* P, uint32_t n_terms, const uint32_t* snps,
+                         const uint8_t* t_inds, const double* inv_tau2_alpha2,
+                         uint32_t const_loci, double* exh_out, double* direct_out);
 void bmgport_destroy(bmgport* P);
 
 #ifdef __cplusplus

@@ -133,6 +133,77 @@ def test_lml_matches_numpy(bmg, oracle):
         assert lml[step] == pytest.approx(exp, rel=1e-11)
 
 
+@pytest.mark.parametrize("terms,const_loci", [
+    ([(0, 0), (1, 1), (2, 0), (3, 0), (4, 1)], 0),
+    ([(0, 1), (1, 0), (2, 0), (3, 1), (4, 0), (5, 0), (6, 0), (7, 0)], 2),
+])
+def test_exhaustive_modelset_known_answer(bmg, oracle, terms, const_loci):
+    """ModelTests.ExhaustiveComputation{,WithConstLoci} (src/tests/model_tests.hpp:92-235):
+    every sub-model the delayed-rejection enumeration visits by adds and left
+    moves has the log probability of the same model built from scratch."""
+    z = H.golden("data_tests")
+    packed, n = z["plink_bed"][3:], 5
+    fam = z["plink_fam"].tobytes().decode().split()
+    y = np.array([float(fam[6 * i + 5]) for i in range(n)])
+    o = small_opts(bmg, n, 10, [0, 4], e_qg=2, var_qg=4, nu_sigma2=4, s2_sigma2=1, mu_alpha=2,
+                   inv_tau2_e_const_val=0)
+    port = oracle.Port(o, packed, y)
+    inv = 1.0 / (2.0 * 2.0 * (4.0 * 1.0 / (4.0 - 2.0)))
+    snps, tinds = zip(*terms)
+    exh, direct = port.exh_modelset(snps, tinds, [[inv, inv]] * len(terms), const_loci)
+    assert len(exh) == 1 << (len(terms) - const_loci)
+    assert np.all(np.isfinite(exh))
+    np.testing.assert_allclose(exh, direct, rtol=0, atol=1e-10)
+
+
+def test_exhaustive_modelset_matches_numpy(bmg, oracle):
+    """The enumeration over 8 terms with 3 kept, on sampled genotypes, against
+    a dense numpy LML plus the beta-binomial/Dirichlet prior change of each
+    added term (src/prior.hpp:144-150, :273-290)."""
+    rng = np.random.default_rng(5)
+    n, p = 90, 30
+    g = rng.integers(0, 3, size=(p, n))
+    code = np.where(g == 0, 0, np.where(g == 1, 2, 3)).astype(np.uint8)
+    pad = np.zeros((p, (n + 3) // 4 * 4), dtype=np.uint8)
+    pad[:, :n] = code
+    pad = pad.reshape(p, -1, 4)
+    packed = (pad[..., 0] | pad[..., 1] << 2 | pad[..., 2] << 4 | pad[..., 3] << 6).astype(np.uint8)
+    y = rng.normal(size=n)
+    o = small_opts(bmg, n, p, [0, 4], e_qg=3, var_qg=4, nu_sigma2=2, s2_sigma2=0.7,
+                   inv_tau2_e_const_val=0.01)
+    tp = [o.types_prior[0], o.types_prior[4]]
+    port = oracle.Port(o, packed.reshape(-1), y)
+    snps = [3, 17, 5, 29, 22, 8, 11, 0, 14, 26, 19]
+    tinds = [0, 1, 0, 1, 0, 0, 1, 0, 1, 0, 0]
+    invs = [[0.3 + 0.1 * i, 0.9 - 0.05 * i] for i in range(len(snps))]
+    const = 3
+    exh, direct = port.exh_modelset(snps, tinds, invs, const)
+    np.testing.assert_allclose(exh, direct, rtol=0, atol=1e-9)
+    zq = (4 - 3 * (1 - 3)) / ((p - 1) * 3)
+    ga = (zq - 1) / (1 - p * zq / 3)
+    gb = (p / 3 - 1) * ga
+    nm = len(snps) - const
+    for mask in range(1 << nm):
+        keep = list(range(const)) + [const + j for j in range(nm) if (mask >> j) & 1]
+        cols, precs = [np.ones(n)], [0.01]
+        for k in keep:
+            cols.append(H.coding(g[snps[k]], 0))
+            precs.append(invs[k][0])
+            if tinds[k] == 1:
+                cols.append(H.coding(g[snps[k]], 1))
+                precs.append(invs[k][1])
+        lml = H.lml_numpy(np.stack(cols, 1), y, np.array(precs), 2 * 0.7 + y @ y, n + 2)
+        ns = [sum(1 for k in range(const) if tinds[k] == t) for t in (0, 1)]
+        nl, lp = const, 0.0
+        for k in keep[const:]:
+            t = tinds[k]
+            lp += (math.log(ga + nl) - math.log(gb + p - nl - 1)) + \
+                  (math.log(tp[t] + ns[t]) - math.log(tp[0] + tp[1] + nl))
+            ns[t] += 1
+            nl += 1
+        assert exh[mask] == pytest.approx(lml + lp, rel=1e-10, abs=1e-9), mask
+
+
 def test_rb_closed_form(bmg, oracle):
     """RaoBlackwellizerTests.EmptyCurrentModel (src/tests/raoblackwellizer_tests.hpp:31-93)."""
     z = H.golden("data_tests")
