@@ -68,6 +68,7 @@ def lib():
                                         C.c_void_p, C.c_void_p]
         L.bmgport_exh_modelset.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p,
                                            C.c_uint32, C.c_void_p, C.c_void_p]
+        L.bmgport_get_inv_tau2_alpha2.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p]
         L.bmgport_destroy.argtypes = [C.c_void_p]
         _lib = L
     return _lib
@@ -152,6 +153,12 @@ class Port:
         lib().bmgport_get_state(self.h, chain, C.byref(st), _ptr(loci), _ptr(types), cap)
         k = st.model_size
         return st, loci[:k].copy(), types[:k].copy()
+
+    def inv_tau2_alpha2(self, chain=0):
+        out = np.zeros(4)
+        if lib().bmgport_get_inv_tau2_alpha2(self.h, chain, _ptr(out)) != 0:
+            raise IndexError(chain)
+        return out
 
     def rao(self, chain=0):
         p = np.zeros(self.m_g)

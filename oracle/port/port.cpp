@@ -2623,6 +2623,16 @@ extern "C" int bmgport_get_state(bmgport* P, uint32_t chain, bmg_chain_state* st
   return 0;
 }
 
+/* The prior's shared 1/(tau2 alpha^2) per term type of a chain
+   (Prior::get_inv_tau2_alpha2_value, src/prior.hpp:126-132): the precision every new
+   term of that type gets while tau2 is shared. */
+extern "C" int bmgport_get_inv_tau2_alpha2(bmgport* P, uint32_t chain, double* out4)
+{
+  if (chain >= P->p.chains.size()) return 1;
+  for (int t = 0; t < 4; ++t) out4[t] = P->p.chains[chain]->prior->inv_tau2_alpha2[t];
+  return 0;
+}
+
 extern "C" int bmgport_get_rao(bmgport* P, uint32_t chain, double* p_rao, double* p_rao_types)
 {
   if (chain >= P->p.chains.size()) return 1;

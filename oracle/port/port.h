@@ -40,6 +40,8 @@ int bmgport_scan_yhat(bmgport* P, uint32_t chain, const double* y_hat, double si
                       double* p_r, double* p_r_types);
 int bmgport_get_state(bmgport* P, uint32_t chain, bmg_chain_state* st,
                       uint32_t* loci, uint8_t* type_inds, uint32_t cap);
+/* the prior's shared 1/(tau2 alpha^2) per term type (A, H, D, R) */
+int bmgport_get_inv_tau2_alpha2(bmgport* P, uint32_t chain, double* out4);
 int bmgport_get_rao(bmgport* P, uint32_t chain, double* p_rao, double* p_rao_types);
 /* the adaptive proposal p_proposal (src/sampler.hpp:363-383) */
 int bmgport_get_proposal(bmgport* P, uint32_t chain, double* p_prop, double* p_prop_types);

@@ -91,3 +91,49 @@ def lml_numpy(X, y, inv, nu_s2_plus_yy, n_plus_nu):
     v = np.linalg.solve(Lc, X.T @ y)
     s = nu_s2_plus_yy - v @ v
     return 0.5 * np.sum(np.log(inv[1:])) - np.sum(np.log(np.diag(Lc))) - 0.5 * n_plus_nu * np.log(s)
+
+
+def small_opts(bg, n, p, types, **kw):
+    """Options of a small test case: n individuals, p SNPs, the given effect
+    types, no covariates, seed 1245; keyword arguments override fields."""
+    o = bg.default_options()
+    o.n, o.m_g, o.m_e = n, p, 0
+    o.n_types = len(types)
+    for i, t in enumerate(sorted(types)):
+        o.types[i] = t
+    o.do_n_iter, o.n_rao, o.n_rao_burnin, o.thin, o.n_sample_tau2_and_missing = 100, 10, 1, 10, 10
+    o.e_qg, o.var_qg, o.nu_sigma2, o.s2_sigma2 = 2, 2, 1, 1
+    for t in range(4):
+        o.nu_tau2[t], o.s2_tau2[t] = 4, 1
+    o.mu_alpha = 1
+    for k, v in kw.items():
+        setattr(o, k, v)
+    bg.set_seeds(o, [1245])
+    return o
+
+
+def small_modelspace_opts(bg, n_iter, dr, seed):
+    """The 7-SNP configuration of src/tests/testdata/small_modelspace_tau2.ini
+    with tau2 and alpha drawn once at the start and then held (the
+    n_sample_tau2_and_missing = 10^9 of onesnp_notau2.ini), so that the
+    exact posterior is a sum over the 2^7 models at that fixed precision."""
+    o = small_opts(bg, 30, 7, [0], e_qg=2, var_qg=2, nu_sigma2=1, s2_sigma2=0, R2mode_sigma2=0.2,
+                   recode_g_to_minor_allele_count=1, inv_tau2_e_const_val=0, do_n_iter=n_iter,
+                   n_rao=10, n_rao_burnin=100, thin=1, n_sample_tau2_and_missing=10 ** 9, adaptation=0,
+                   delay_rejection=dr)
+    o.nu_tau2[0], o.s2_tau2[0] = 3, 0.02
+    bg.set_seeds(o, [seed])
+    return o
+
+
+def exact_pips(port):
+    """Posterior inclusion probabilities of the 7 SNPs by enumerating all 2^7
+    models (SamplerTestsF.SmallModelSpaceWithSharedTau2,
+    src/tests/sampler_tests.hpp:348-446, with the tau2/alpha integral replaced
+    by the chain's fixed precision)."""
+    inv = port.inv_tau2_alpha2()[0]
+    logp, _ = port.exh_modelset(list(range(7)), [0] * 7, [[inv, inv]] * 7, 0)
+    w = np.exp(logp - logp.max())
+    w /= w.sum()
+    masks = np.arange(128)
+    return np.array([w[(masks >> j) & 1 == 1].sum() for j in range(7)])
