@@ -69,6 +69,11 @@ def lib():
         L.bmgport_exh_modelset.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p,
                                            C.c_uint32, C.c_void_p, C.c_void_p]
         L.bmgport_get_inv_tau2_alpha2.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p]
+        L.bmgport_exh_proposal_probs.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                 C.c_double, C.c_double, C.c_uint64, C.c_uint64,
+                                                 C.c_void_p, C.c_void_p]
+        L.bmgport_model_lml_remove.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p,
+                                               C.c_uint32, C.POINTER(C.c_double)]
         L.bmgport_destroy.argtypes = [C.c_void_p]
         _lib = L
     return _lib
@@ -206,6 +211,17 @@ class Port:
             raise RuntimeError("oracle model failed")
         return out
 
+    def model_lml_remove(self, snps, t_inds, inv_pairs, rem):
+        """LML after adding the terms in order and removing model index rem."""
+        snps = np.ascontiguousarray(snps, dtype=np.uint32)
+        t_inds = np.ascontiguousarray(t_inds, dtype=np.uint8)
+        inv = np.ascontiguousarray(inv_pairs, dtype=np.float64).reshape(-1)
+        out = C.c_double()
+        if lib().bmgport_model_lml_remove(self.h, len(snps), _ptr(snps), _ptr(t_inds), _ptr(inv), rem,
+                                          C.byref(out)) != 0:
+            raise RuntimeError("oracle model failed")
+        return out.value
+
     def exh_modelset(self, snps, t_inds, inv_pairs, const_loci):
         """(exhaustive, direct): log probabilities of the 2^m sub-models of the
         last m = len(snps) - const_loci terms, by the delayed-rejection
@@ -219,6 +235,21 @@ class Port:
                                       const_loci, _ptr(exh), _ptr(direct)) != 0:
             raise RuntimeError("oracle exhaustive model set failed")
         return exh, direct
+
+
+def exh_proposal_probs(bit_to_order, q_add, q_rem, z_add, z_rem, const_loci, m_g, log_q_add_types=None):
+    """Log proposal probabilities of the 2^m sub-models of a delayed-rejection
+    move (src/sampler.cpp:980-1049), m = len(q_add), in bit order."""
+    m = len(q_add)
+    order = np.ascontiguousarray(bit_to_order, dtype=np.uint8)
+    qa = np.ascontiguousarray(q_add, dtype=np.float64)
+    qr = np.ascontiguousarray(q_rem, dtype=np.float64)
+    lt = None if log_q_add_types is None else np.ascontiguousarray(log_q_add_types, dtype=np.float64)
+    out = np.zeros(1 << m)
+    if lib().bmgport_exh_proposal_probs(int(lt is not None), m, _ptr(order), _ptr(qa), _ptr(qr), z_add, z_rem,
+                                        const_loci, m_g, None if lt is None else _ptr(lt), _ptr(out)) != 0:
+        raise ValueError("move size out of range")
+    return out
 
 
 def read_ref_outputs(basename, chain, m_g, n_types=1):

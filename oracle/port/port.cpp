@@ -2750,4 +2750,39 @@ extern "C" int bmgport_exh_modelset(bmgport* P, uint32_t n_terms, const uint32_t
   }
 }
 
+/* Log proposal probability of every sub-model of a delayed-rejection move
+   (compute_proposal_probs_for_exh_modelset, src/sampler.cpp:980-1049), for
+   the closed forms of src/tests/sampler_tests.hpp:611-700.  out (2^n_inds
+   entries) is added to, as in the reference. */
+extern "C" int bmgport_exh_proposal_probs(int use_types, int n_inds, const uint8_t* bit_to_normalized_order,
+                                          const double* q_add, const double* q_rem, double z_add,
+                                          double z_rem, uint64_t const_loci, uint64_t m_g,
+                                          const double* log_q_add_types, double* out)
+{
+  if (n_inds < 1 || n_inds > 20) return 1;
+  compute_proposal_probs_for_exh_modelset(use_types != 0, n_inds, bit_to_normalized_order, q_add, q_rem,
+                                          z_add, z_rem, (size_t)const_loci, (size_t)m_g, log_q_add_types, out);
+  return 0;
+}
+
+/* LML after adding n_add terms and then removing the term at model index
+   rem (Model::remove_term, src/model.hpp:270-312: column shift, dchex job 2
+   downdate of the Cholesky factor, sign fix and re-solve, src/model.hpp:508-556) */
+extern "C" int bmgport_model_lml_remove(bmgport* P, uint32_t n_add, const uint32_t* snps,
+                                        const uint8_t* t_inds, const double* itv, uint32_t rem, double* lml)
+{
+  try {
+    if (rem >= n_add) return 1;
+    Sampler* s = P->p.chains.at(0);
+    Stats st;
+    Model m(P->p.data, s->dm, s->prior, &st, s->cur->cap);
+    for (uint32_t i = 0; i < n_add; ++i) m.add_term(snps[i], t_inds[i], &itv[2 * i]);
+    m.remove_term((int)rem);
+    *lml = m.log_likelihood_;
+    return 0;
+  } catch (...) {
+    return 1;
+  }
+}
+
 extern "C" void bmgport_destroy(bmgport* P) { delete P; }

@@ -62,6 +62,15 @@ int bmgport_model_lml(bmgport* P, uint32_t n_add, const uint32_t* snps,
 int bmgport_exh_modelset(bmgport* P, uint32_t n_terms, const uint32_t* snps,
                          const uint8_t* t_inds, const double* inv_tau2_alpha2,
                          uint32_t const_loci, double* exh_out, double* direct_out);
+/* log proposal probabilities of the 2^n_inds sub-models of a
+   delayed-rejection move (src/sampler.cpp:980-1049); out is added to */
+int bmgport_exh_proposal_probs(int use_types, int n_inds, const uint8_t* bit_to_normalized_order,
+                               const double* q_add, const double* q_rem, double z_add, double z_rem,
+                               uint64_t const_loci, uint64_t m_g, const double* log_q_add_types,
+                               double* out);
+/* LML after n_add add_term calls and one remove_term (src/model.hpp:270-312) */
+int bmgport_model_lml_remove(bmgport* P, uint32_t n_add, const uint32_t* snps, const uint8_t* t_inds,
+                             const double* inv_tau2_alpha2, uint32_t rem, double* lml);
 void bmgport_destroy(bmgport* P);
 
 #ifdef __cplusplus

@@ -119,6 +119,40 @@ def test_lml_matches_numpy(bmg, oracle):
         assert lml[step] == pytest.approx(exp, rel=1e-11)
 
 
+def test_lml_after_removal_matches_numpy(bmg, oracle):
+    """Removing each term of a 7-term model (A and AH columns) by the Givens
+    downdate (src/model.hpp:270-312,508-556; the reference's CholeskyDowndate
+    test, src/tests/symmmatrix_tests.hpp:106-142, at the model level) gives the
+    dense numpy LML of the model without it."""
+    rng = np.random.default_rng(17)
+    n, p = 70, 25
+    g = rng.integers(0, 3, size=(p, n))
+    code = np.where(g == 0, 0, np.where(g == 1, 2, 3)).astype(np.uint8)
+    pad = np.zeros((p, (n + 3) // 4 * 4), dtype=np.uint8)
+    pad[:, :n] = code
+    pad = pad.reshape(p, -1, 4)
+    packed = (pad[..., 0] | pad[..., 1] << 2 | pad[..., 2] << 4 | pad[..., 3] << 6).astype(np.uint8)
+    y = rng.normal(size=n)
+    o = small_opts(bmg, n, p, [0, 4], nu_sigma2=2, s2_sigma2=0.7, inv_tau2_e_const_val=0.01)
+    port = oracle.Port(o, packed.reshape(-1), y)
+    snps = [4, 19, 7, 12, 0, 23, 9]
+    tinds = [1, 0, 1, 0, 0, 1, 0]
+    invs = [[0.4 + 0.1 * i, 0.8 - 0.07 * i] for i in range(len(snps))]
+    for rem in range(len(snps)):
+        got = port.model_lml_remove(snps, tinds, invs, rem)
+        cols, precs = [np.ones(n)], [0.01]
+        for k in range(len(snps)):
+            if k == rem:
+                continue
+            cols.append(H.coding(g[snps[k]], 0))
+            precs.append(invs[k][0])
+            if tinds[k] == 1:
+                cols.append(H.coding(g[snps[k]], 1))
+                precs.append(invs[k][1])
+        exp = H.lml_numpy(np.stack(cols, 1), y, np.array(precs), 2 * 0.7 + y @ y, n + 2)
+        assert got == pytest.approx(exp, rel=1e-11), rem
+
+
 @pytest.mark.parametrize("terms,const_loci", [
     ([(0, 0), (1, 1), (2, 0), (3, 0), (4, 1)], 0),
     ([(0, 1), (1, 0), (2, 0), (3, 1), (4, 0), (5, 0), (6, 0), (7, 0)], 2),
@@ -140,6 +174,32 @@ def test_exhaustive_modelset_known_answer(bmg, oracle, terms, const_loci):
     assert len(exh) == 1 << (len(terms) - const_loci)
     assert np.all(np.isfinite(exh))
     np.testing.assert_allclose(exh, direct, rtol=0, atol=1e-10)
+
+
+def test_exhaustive_proposal_probabilities_known_answer(oracle):
+    """SamplerTests.ExhProposals (src/tests/sampler_tests.hpp:611-700): SNPs 1
+    and 2 are in the model, the move {+0, -2, +3} was proposed and SNP 1 stays;
+    each of the 8 sub-models gets the probability of proposing it from the
+    model with only SNP 1 (adds in order, removals in reverse, a factor 1/2
+    while both adds and removes are possible)."""
+    qa = [0.3, 0.4, 0.5, 0.6]
+    qr = [0.7, 0.6, 0.5, 0.4]
+    out = oracle.exh_proposal_probs([0, 2, 1], [0.3, 0.5, 0.6], [0.7, 0.5, 0.4], z_add=0.3 + 0.5 + 0.6,
+                                    z_rem=0.6, const_loci=1, m_g=4)
+    lh = math.log(0.5)
+    lg = math.log
+    expect = [
+        lg(qa[0] / (qa[0] + qa[2] + qa[3])) + lh + lg(qa[2] / (qa[2] + qa[3])) + lh + lh,
+        lg(qr[0] / (qr[0] + qr[1])) + lh + lg(qa[2] / (qa[2] + qa[3])) + lh + lh,
+        lg(qa[0] / (qa[0] + qa[2])) + lh + lh + lg(qr[3] / (qr[1] + qr[3])),
+        lg(qr[3] / (qr[0] + qr[1] + qr[3])) + lh + lh + lg(qr[0] / (qr[1] + qr[0])),
+        lg(qa[0] / (qa[0] + qa[3])) + lh + lg(qr[2] / (qr[1] + qr[2])) + lh + lh,
+        lg(qr[2] / (qr[0] + qr[1] + qr[2])) + lh + lg(qr[0] / (qr[1] + qr[0])) + lh + lh,
+        lh + lg(qr[3] / (qr[3] + qr[1] + qr[2])) + lg(qr[2] / (qr[1] + qr[2])),
+        lg(qr[3] / (qr[0] + qr[3] + qr[1] + qr[2])) + lg(qr[2] / (qr[0] + qr[1] + qr[2]))
+        + lg(qr[0] / (qr[0] + qr[1])),
+    ]
+    np.testing.assert_allclose(out, expect, rtol=0, atol=1e-10)
 
 
 def test_exhaustive_modelset_matches_numpy(bmg, oracle):
