@@ -74,6 +74,8 @@ def lib():
                                                  C.c_void_p, C.c_void_p]
         L.bmgport_model_lml_remove.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p,
                                                C.c_uint32, C.POINTER(C.c_double)]
+        L.bmgport_dd_exercise.argtypes = [C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64, C.c_uint32,
+                                          C.c_uint64, C.c_void_p, C.POINTER(C.c_double), C.c_void_p]
         L.bmgport_destroy.argtypes = [C.c_void_p]
         _lib = L
     return _lib
@@ -250,6 +252,22 @@ def exh_proposal_probs(bit_to_order, q_add, q_rem, z_add, z_rem, const_loci, m_g
                                         const_loci, m_g, None if lt is None else _ptr(lt), _ptr(out)) != 0:
         raise ValueError("move size out of range")
     return out
+
+
+def dd_exercise(w, ops=(), seed=1234, n_samples=0):
+    """The proposal tree alone (src/discrete_distribution.hpp:64-330): apply
+    ops (k >= 0 zeroes SNP k, k < 0 restores SNP -k - 1); returns (node values,
+    total weight, draw counts per SNP)."""
+    w = np.ascontiguousarray(w, dtype=np.float64)
+    o = np.ascontiguousarray(ops, dtype=np.int64)
+    vals = np.zeros(len(w))
+    counts = np.zeros(len(w), dtype=np.uint64)
+    tot = C.c_double()
+    rc = lib().bmgport_dd_exercise(_ptr(w), len(w), _ptr(o) if len(o) else None, len(o), seed, n_samples,
+                                   _ptr(vals), C.byref(tot), _ptr(counts))
+    if rc != 0:
+        raise ValueError("dd_exercise failed (%d)" % rc)
+    return vals, tot.value, counts
 
 
 def read_ref_outputs(basename, chain, m_g, n_types=1):

@@ -2785,4 +2785,39 @@ extern "C" int bmgport_model_lml_remove(bmgport* P, uint32_t n_add, const uint32
   }
 }
 
+/* The proposal tree on its own (DiscreteDistribution, src/discrete_distribution.hpp:64-330),
+   for the known answers of src/tests/discrete_distribution_tests.hpp.  ops
+   are applied in order: op >= 0 zeroes SNP op (adddate), op < 0 restores SNP
+   -op - 1 (remdate).  Then node values and the total are written, and
+   n_samples draws (seed) are counted per SNP. */
+extern "C" int bmgport_dd_exercise(const double* w, uint64_t n, const int64_t* ops, uint64_t n_ops,
+                                   uint32_t seed, uint64_t n_samples, double* values_out, double* total_out,
+                                   uint64_t* counts_out)
+{
+  try {
+    if (n == 0) return 1;
+    Rand rng(seed, 1.0);
+    DD dd(w, (size_t)n, &rng);
+    for (uint64_t i = 0; i < n_ops; ++i) {
+      int64_t op = ops[i];
+      if (op >= (int64_t)n || -op - 1 >= (int64_t)n) return 1;
+      if (op >= 0) dd.adddate((size_t)op);
+      else dd.remdate((size_t)(-op - 1));
+    }
+    if (values_out) for (uint64_t i = 0; i < n; ++i) values_out[i] = dd.value[i];
+    *total_out = dd.total_w;
+    if (counts_out) {
+      for (uint64_t i = 0; i < n; ++i) counts_out[i] = 0;
+      for (uint64_t i = 0; i < n_samples; ++i) {
+        size_t k = dd.sample();
+        if (k >= n) return 2;
+        ++counts_out[k];
+      }
+    }
+    return 0;
+  } catch (...) {
+    return 1;
+  }
+}
+
 extern "C" void bmgport_destroy(bmgport* P) { delete P; }

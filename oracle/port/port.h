@@ -71,6 +71,10 @@ int bmgport_exh_proposal_probs(int use_types, int n_inds, const uint8_t* bit_to_
 /* LML after n_add add_term calls and one remove_term (src/model.hpp:270-312) */
 int bmgport_model_lml_remove(bmgport* P, uint32_t n_add, const uint32_t* snps, const uint8_t* t_inds,
                              const double* inv_tau2_alpha2, uint32_t rem, double* lml);
+/* the proposal tree alone: zero/restore ops, node values, total, draw counts
+   (src/discrete_distribution.hpp:64-330) */
+int bmgport_dd_exercise(const double* w, uint64_t n, const int64_t* ops, uint64_t n_ops, uint32_t seed,
+                        uint64_t n_samples, double* values_out, double* total_out, uint64_t* counts_out);
 void bmgport_destroy(bmgport* P);
 
 #ifdef __cplusplus

@@ -363,3 +363,54 @@ def test_schur_scan_matches_dense_lml(bmg, oracle):
         assert dl[j, 0] == pytest.approx(exp, rel=1e-9, abs=1e-9)
         checked += 1
     assert checked == p - len(loci)
+
+
+def test_proposal_tree_known_answers(oracle):
+    """DiscreteDistributionTests.{Construction,Updates} (src/tests/discrete_distribution_tests.hpp:31-200):
+    node values (own weight plus the left subtree) and the total after zeroing
+    and restoring SNPs; switchdate(a, b) is written as zeroing a and restoring b."""
+    w = [0.1, 0.2, 0.3, 0.4, 0.5]
+    full = [0.1 + 0.2 + 0.4 + 0.5, 0.2 + 0.4, 0.3, 0.4, 0.5]
+    steps = [
+        ([], full, 1.5),
+        ([0], [0.2 + 0.4 + 0.5, 0.6, 0.3, 0.4, 0.5], 1.4),
+        ([0, 4], [0.6, 0.6, 0.3, 0.4, 0.0], 0.9),
+        ([0, 4, 2], [0.6, 0.6, 0.0, 0.4, 0.0], 0.6),
+        ([0, 4, 2, -1], [0.7, 0.6, 0.0, 0.4, 0.0], 0.7),
+        ([0, 4, 2, -1, 3, -3, 2, -4, 3, -3], [0.1 + 0.2, 0.2, 0.3, 0.0, 0.0], 0.6),
+        ([0, 4, 2, -1, 3, -3, 2, -4, 3, -3, -5, -4], full, 1.5),
+        ([0, 1, 2, 3, 4], [0.0] * 5, 0.0),
+        ([0, 1, 2, 3, 4, -1, -2, -3, -4, -5], full, 1.5),
+    ]
+    for ops, values, total in steps:
+        v, t, _ = oracle.dd_exercise(w, ops)
+        np.testing.assert_allclose(v, values, rtol=0, atol=1e-15, err_msg=str(ops))
+        assert t == pytest.approx(total, abs=1e-15), ops
+    # many zero/restore rounds leave the tree where it started
+    rng = np.random.default_rng(1234)
+    ops = []
+    for ind in rng.integers(0, 5, size=200000):
+        ind = int(ind)
+        ops += [ind, (ind + 2) % 5, (ind + 1) % 5, -ind - 1, -((ind + 2) % 5) - 1, -((ind + 1) % 5) - 1]
+    v, t, _ = oracle.dd_exercise(w, ops)
+    np.testing.assert_allclose(v, full, rtol=0, atol=1e-15)
+    assert t == pytest.approx(1.5, abs=1e-15)
+
+
+def test_proposal_tree_sampling(oracle):
+    """DiscreteDistributionTests.{Sample,SampleManySizes,SampleSomeZeroed}
+    (src/tests/discrete_distribution_tests.hpp:202-385): draw frequencies
+    match the normalised weights of the SNPs that are not zeroed (1M draws per
+    case, 0.002 absolute)."""
+    _, _, c = oracle.dd_exercise([0.1, 0.001, 0.3, 0.099, 0.5], n_samples=1000000)
+    np.testing.assert_allclose(c / 1e6, [0.1, 0.001, 0.3, 0.099, 0.5], rtol=0, atol=0.002)
+    rng = np.random.default_rng(1234)
+    for size in range(1, 32):
+        p = rng.random(size)
+        p /= p.sum()
+        zero = rng.choice(size, size // 2, replace=False) if size < 16 else np.array([], dtype=int)
+        _, t, c = oracle.dd_exercise(p, list(zero), seed=size, n_samples=1000000)
+        q = p.copy()
+        q[zero] = 0
+        assert t == pytest.approx(q.sum(), rel=1e-12)
+        np.testing.assert_allclose(c / 1e6, q / q.sum(), rtol=0, atol=0.002, err_msg="size %d" % size)
