@@ -148,6 +148,19 @@ def run_case(name, files, **kw):
     np.savez_compressed(os.path.join(HERE, "ref_%s.npz" % name), **out)
 
 
+def with_missing(bed, n, p, frac, seed):
+    """A copy of a SNP-major .bed (3-byte magic first) with a seeded fraction
+    of the n calls of each of the p SNPs set to the missing code 01."""
+    out = np.array(bed, dtype=np.uint8, copy=True)
+    stride = (n + 3) // 4
+    rng = np.random.default_rng(seed)
+    snp, ind = np.nonzero(rng.random((p, n)) < frac)
+    pos = 3 + snp * stride + ind // 4
+    shift = (2 * (ind % 4)).astype(np.uint8)
+    out[pos] = (out[pos] & ~(np.uint8(3) << shift)) | (np.uint8(1) << shift)
+    return out
+
+
 def cases():
     """name -> (files, run_case keywords)"""
     tdir = os.path.join(REF, "src/tests/testdata")
@@ -165,6 +178,8 @@ def cases():
     files = {"data.bed": sub, "data.fam": rd(os.path.join(ex, "testdata.fam")),
              "data.e": rd(os.path.join(ex, "testdata.e")), "data.y": rd(os.path.join(ex, "testdata.y"))}
     efiles = dict(efile="file_e = {DIR}/data.e\n", yfile="file_y = {DIR}/data.y\n")
+    small_miss = dict(small, **{"data.bed": with_missing(small["data.bed"], 30, 7, 0.05, 11)})
+    files_miss = dict(files, **{"data.bed": with_missing(sub, n, p, 0.02, 12)})
     return {
         # the exhaustive-posterior test setting (src/tests/testdata/small_modelspace_tau2.ini),
         # shortened and with delayed rejection off
@@ -190,6 +205,15 @@ def cases():
         "small_types_dr": (small, dict(n=30, p=7, iters=2000, n_rao=10, burnin=20, thin=2, nst=6,
                                        chains=1, seeds="99", types="A,AH", e_qg=2, var_qg=2, maxms=5, nbh=3,
                                        dr=5)),
+        # missing calls (5 % and 2 % of the calls, seeded): imputation from each
+        # SNP's genotype frequencies at every RB step and the Gibbs update of the
+        # in-model SNPs' missing calls every nst iterations
+        "small_types_missing": (small_miss, dict(n=30, p=7, iters=2000, n_rao=10, burnin=20, thin=2, nst=6,
+                                                 chains=1, seeds="99", types="A,AH", e_qg=2, var_qg=2, indiv=1,
+                                                 maxms=5, nbh=3)),
+        "example_missing": (files_miss, dict(n=n, p=p, iters=600, n_rao=10, burnin=20, thin=10, nst=10,
+                                             chains=2, seeds="1234,2345", types="A", e_qg=20, var_qg=300, m_e=2,
+                                             indiv=1, **efiles)),
     }
 
 

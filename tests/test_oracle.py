@@ -308,10 +308,11 @@ def test_rb_closed_form(bmg, oracle):
 
 
 @pytest.mark.parametrize("name", ["small", "small_types", "example", "example_types", "small_dr", "example_dr",
-                                  "small_types_dr"])
+                                  "small_types_dr", "small_types_missing", "example_missing"])
 def test_oracle_matches_reference_traces(bmg, oracle, tmp_path, name):
     """The oracle reproduces the compiled reference's traces bit for bit (the
-    *_dr cases with delayed rejection on)."""
+    *_dr cases with delayed rejection on, the *_missing cases with missing
+    genotype calls imputed and Gibbs-updated)."""
     z = H.golden("ref_" + name)
     ini = H.materialize(z, tmp_path)
     opt = bmg.options_from_ini(ini)
