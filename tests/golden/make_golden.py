@@ -30,7 +30,7 @@ TRACE_FILES = {
     "jumpdistance": np.uint8, "move_type": np.uint8, "move_size": np.uint8,
     "modelsize": np.uint32, "loci": np.uint32, "log_likelihood": np.float64,
     "log_prior": np.float64, "sigma2": np.float64, "alpha": np.float64, "pve": np.float64,
-    "rao": np.float64, "types": np.uint8, "rao_types": np.float64,
+    "rao": np.float64, "types": np.uint8, "rao_types": np.float64, "beta": np.float64,
 }
 
 
@@ -80,10 +80,11 @@ p_move_size = 0.2
 p_move_size_nbc = 0.25
 p_move_size_nbs = 0.7
 max_SNP_neighborhood_size = {nbh}
-adapt_p_move_size = 1
+adapt_p_move_size = {adapt_ms}
 p_move_size_acpt_goal = {acpt}
 max_move_size = {maxms}
-flat_proposal_dist = 0
+flat_proposal_dist = {flat}
+save_beta = {save_beta}
 [thread]
 n_threads = {chains}
 basename = {{DIR}}/out/chain
@@ -127,6 +128,9 @@ def run_case(name, files, **kw):
     kw.setdefault("maxms", 20)
     kw.setdefault("indiv", 0)
     kw.setdefault("dr", 0)
+    kw.setdefault("adapt_ms", 1)
+    kw.setdefault("flat", 0)
+    kw.setdefault("save_beta", 0)
     ini = INI.format(**kw)
     with tempfile.TemporaryDirectory() as d:
         for fn, data in files.items():
@@ -211,6 +215,14 @@ def cases():
         "small_types_missing": (small_miss, dict(n=30, p=7, iters=2000, n_rao=10, burnin=20, thin=2, nst=6,
                                                  chains=1, seeds="99", types="A,AH", e_qg=2, var_qg=2, indiv=1,
                                                  maxms=5, nbh=3)),
+        # a flat proposal (no RB-adapted add weights), the beta trace, raw
+        # (not minor-allele recoded) genotypes and a fixed move-size distribution
+        "small_flat": (small, dict(n=30, p=7, iters=2000, n_rao=10, burnin=20, thin=2, nst=6, chains=2,
+                                   seeds="5,6", types="A", e_qg=2, var_qg=2, flat=1, save_beta=1, recode=0,
+                                   adapt_ms=0)),
+        "example_flat": (files, dict(n=n, p=p, iters=400, n_rao=10, burnin=20, thin=10, nst=10, chains=1,
+                                     seeds="31", types="A,AH", e_qg=20, var_qg=300, m_e=2, flat=1, save_beta=1,
+                                     **efiles)),
         "example_missing": (files_miss, dict(n=n, p=p, iters=600, n_rao=10, burnin=20, thin=10, nst=10,
                                              chains=2, seeds="1234,2345", types="A", e_qg=20, var_qg=300, m_e=2,
                                              indiv=1, **efiles)),

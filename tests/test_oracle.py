@@ -308,11 +308,13 @@ def test_rb_closed_form(bmg, oracle):
 
 
 @pytest.mark.parametrize("name", ["small", "small_types", "example", "example_types", "small_dr", "example_dr",
-                                  "small_types_dr", "small_types_missing", "example_missing"])
+                                  "small_types_dr", "small_types_missing", "example_missing", "small_flat",
+                                  "example_flat"])
 def test_oracle_matches_reference_traces(bmg, oracle, tmp_path, name):
     """The oracle reproduces the compiled reference's traces bit for bit (the
     *_dr cases with delayed rejection on, the *_missing cases with missing
-    genotype calls imputed and Gibbs-updated)."""
+    genotype calls imputed and Gibbs-updated, the *_flat cases with a flat
+    proposal, raw genotypes and the beta trace)."""
     z = H.golden("ref_" + name)
     ini = H.materialize(z, tmp_path)
     opt = bmg.options_from_ini(ini)
@@ -322,6 +324,8 @@ def test_oracle_matches_reference_traces(bmg, oracle, tmp_path, name):
     for c in range(opt.n_chains):
         ref = H.ref_chain(z, c)
         H.compare(ref, col.chain(c), rtol=0.0, label="%s chain %d" % (name, c))
+        if "c%d_beta" % c in z.files:
+            assert np.array_equal(col.chain(c)["beta"], z["c%d_beta" % c]), "%s chain %d beta" % (name, c)
         rao, raot = port.rao(c)
         assert np.array_equal(rao, ref["rao"])
         if raot is not None:
