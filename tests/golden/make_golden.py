@@ -13,6 +13,7 @@ Runs only where the reference tree and its oracle build (oracle/_ref) exist:
 Usage:  python tests/golden/make_golden.py [REFERENCE_DIR [CASE ...]]
 (all cases when none is named)
 """
+import json
 import os
 import re
 import subprocess
@@ -25,6 +26,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
 REF_BIN = os.path.join(ROOT, "oracle", "_ref", "bmagwa_ref")
+REF_PROBE = os.path.join(ROOT, "oracle", "_ref", "ref_probe")
 
 TRACE_FILES = {
     "jumpdistance": np.uint8, "move_type": np.uint8, "move_size": np.uint8,
@@ -229,12 +231,109 @@ def cases():
     }
 
 
+def edit_ini(text, section, key, value):
+    """Set (or with value None delete) one key of an INI text; a key that is
+    absent is added at the top of its section."""
+    pat = re.compile(r"(?m)^%s\s*[=:].*$" % re.escape(key))
+    if pat.search(text):
+        return pat.sub("" if value is None else "%s = %s" % (key, value), text)
+    if value is None:
+        return text
+    return text.replace("[%s]\n" % section, "[%s]\n%s = %s\n" % (section, key, value), 1)
+
+
+# edits of the example configuration (testdata/testdata.ini): one rule of the
+# reference's parser (src/options.hpp:138-321) each
+OPTION_EDITS = {
+    "example": [],
+    "types_unsorted": [("model", "types", "H, A, AH")],
+    "types_all": [("model", "types", "AH,R,D,H,A"), ("prior", "nu_tau2_D", "4"), ("prior", "eh_tau2_D", "0.2"),
+                  ("prior", "nu_tau2_R", "3"), ("prior", "s2_tau2_R", "0.01")],
+    "types_unknown": [("model", "types", "A, Q")],
+    "types_empty": [("model", "types", "")],
+    "types_missing_prior": [("model", "types", "A, R")],
+    "thin_not_divisor": [("sampler", "thin", "3")],
+    "defaults": [("sampler", k, None) for k in ("max_move_size", "p_move_size", "p_move_size_nbc", "p_move_size_nbs",
+                                               "max_SNP_neighborhood_size", "adapt_p_move_size",
+                                               "p_move_size_acpt_goal", "flat_proposal_dist", "delay_rejection",
+                                               "adaptation", "type")] +
+                [("thread", "basename", None), ("prior", "use_individual_tau2", None), ("prior", "type_AH", None),
+                 ("prior", "mu_alpha", None)],
+    "p_move_size_above_1": [("sampler", "p_move_size", "1.5")],
+    "p_move_size_nbs_zero": [("sampler", "p_move_size_nbs", "0")],
+    "acpt_goal": [("sampler", "p_move_size_acpt_goal", "0.3")],
+    "acpt_goal_above_1": [("sampler", "p_move_size_acpt_goal", "1.2")],
+    "seeds_short": [("thread", "n_threads", "3")],
+    "seeds_repeated": [("thread", "seeds", "7, 7")],
+    "sampler_unknown": [("sampler", "type", "XYZ")],
+    "sampler_nk_ah": [("sampler", "type", "NK"), ("model", "types", "A, AH")],
+    "bool_bad": [("sampler", "adaptation", "2")],
+    "bool_words": [("sampler", "adaptation", "true"), ("sampler", "flat_proposal_dist", "no")],
+    "r2mode_bad": [("prior", "R2mode_sigma2", "1.5")],
+    "s2_sigma2_given": [("prior", "R2mode_sigma2", None), ("prior", "s2_sigma2", "0.5")],
+    "nu_sigma2_negative": [("prior", "nu_sigma2", "-1")],
+    "n_missing": [("sizes", "n", None)],
+    "n_not_integer": [("sizes", "n", "12x")],
+    "n_zero": [("sizes", "n", "0")],
+    "no_covariates": [("sizes", "m_e", "0"), ("datafiles", "file_e", None)],
+    "covariates_without_file": [("datafiles", "file_e", None)],
+    "eh_tau2": [("prior", "s2_tau2_A", None), ("prior", "eh_tau2_A", "0.1")],
+    "shared_tau2": [("prior", "use_individual_tau2", "0"), ("prior", "inv_tau2_e_const_val", "0.5")],
+    "no_y_file": [("datafiles", "file_y", None)],
+    "recode_off": [("datafiles", "recode_g_to_minor_allele_count", "0")],
+    "verbosity_missing": [("sampler", "verbosity", None)],
+    "burnin_zero": [("sampler", "n_rao_burnin", "0")],
+}
+
+
+def option_cases():
+    """INI texts for the parser parity fixture: the reference's own INI files
+    and the edits of OPTION_EDITS."""
+    out = {}
+    example = open(os.path.join(REF, "testdata", "testdata.ini")).read()
+    for name, edits in OPTION_EDITS.items():
+        text = example
+        for section, key, value in edits:
+            text = edit_ini(text, section, key, value)
+        out[name] = text
+    tdir = os.path.join(REF, "src", "tests", "testdata")
+    for f in sorted(os.listdir(tdir)):
+        if f.endswith(".ini"):
+            out["tests_" + f[:-4]] = open(os.path.join(tdir, f)).read()
+    return out
+
+
+def options_fixture():
+    """Run the reference's option parser (oracle/_ref/ref_probe) over every
+    case; store each INI text with the parsed fields (or the error) and the
+    warnings it printed, in order."""
+    cases = []
+    with tempfile.TemporaryDirectory() as d:
+        for name, text in option_cases().items():
+            path = os.path.join(d, "opt.ini")
+            with open(path, "w") as f:
+                f.write(text)
+            r = subprocess.run([REF_PROBE, path], check=True, capture_output=True, text=True)
+            fields, warnings = {}, []
+            for line in r.stdout.splitlines():
+                if line.startswith("opt."):
+                    k, v = line[4:].split("=", 1)
+                    fields[k] = v
+                elif line.startswith("Warning"):
+                    warnings.append(line)
+            cases.append({"name": name, "ini": text, "fields": fields, "warnings": warnings})
+    with open(os.path.join(HERE, "options_ref.json"), "w") as f:
+        json.dump(cases, f, indent=0, sort_keys=True)
+
+
 def main():
     if not os.path.exists(REF_BIN):
         raise SystemExit("build oracle/_ref first (make -C oracle)")
     names = sys.argv[2:]
     if not names:
         known_answers()
+    if not names or "options" in names:
+        options_fixture()
     for name, (files, kw) in cases().items():
         if names and name not in names:
             continue

@@ -2,6 +2,7 @@
 option rules (src/options.hpp:138-321, src/inih/ini.c:57-130) and the PLINK
 readers (src/data.cpp:141-273).  Nothing here launches a kernel."""
 import ctypes as C
+import json
 import os
 import re
 
@@ -221,3 +222,50 @@ def test_options_struct_matches_the_library():
     assert L.bmg_options_size() == C.sizeof(abi.Options)
     o = bg.default_options()
     assert o.learned_topk == 1024 and o.learned_mix == pytest.approx(0.3)
+
+
+def _option_cases():
+    with open(os.path.join(os.path.dirname(__file__), "golden", "options_ref.json")) as f:
+        return json.load(f)
+
+
+@pytest.mark.parametrize("case", _option_cases(), ids=lambda c: c["name"])
+def test_options_match_the_reference_parser(tmp_path, capfd, case):
+    """bmg_options_from_ini against the reference's own parser
+    (src/options.hpp:138-321, run over the same INI text by
+    tests/golden/make_golden.py): every field, the error message, and the
+    default-value warnings in the order printed."""
+    path = tmp_path / "opt.ini"
+    path.write_text(case["ini"])
+    ref = case["fields"]
+    capfd.readouterr()
+    if "error" in ref:
+        with pytest.raises(bg.BmgError) as ei:
+            bg.options_from_ini(str(path), quiet=False)
+        assert str(ei.value).split(": ", 1)[1] == ref["error"]
+        return
+    o = bg.options_from_ini(str(path), quiet=False)
+    out = capfd.readouterr().out
+    warnings = [ln for ln in out.splitlines() if ln.startswith("Warning")]
+    assert warnings == case["warnings"]
+    for k in ("file_fam", "file_g", "file_e", "file_y", "basename"):
+        assert getattr(o, k).decode() == ref[k], k
+    ints = ("n", "m_g", "m_e", "recode_g_to_minor_allele_count", "sampler_type", "do_n_iter", "n_rao",
+            "n_rao_burnin", "thin", "n_sample_tau2_and_missing", "max_move_size", "max_SNP_neighborhood_size",
+            "adapt_p_move_size", "adaptation", "flat_proposal_dist", "save_beta", "verbosity", "delay_rejection",
+            "n_chains", "use_individual_tau2")
+    for k in ints:
+        assert int(getattr(o, k)) == int(ref[k]), k
+    reals = ("p_move_size", "p_move_size_nbs", "p_move_size_nbc", "p_move_size_acpt_goal", "e_qg", "var_qg",
+             "nu_sigma2", "s2_sigma2", "R2mode_sigma2", "mu_alpha", "inv_tau2_e_const_val", "inv_tau2_e_val")
+    for k in reals:
+        assert getattr(o, k) == float(ref[k]), k
+    types = [int(t) for t in ref["types"].split(",")]
+    assert [o.types[i] for i in range(o.n_types)] == types
+    assert list(o.seeds[:o.n_chains]) == [int(s) for s in ref["seeds"].split(",")]
+    for t in range(5):
+        assert o.types_prior[t] == float(ref["types_prior.%d" % t]), t
+    terms = {t for ty in types for t in ((0, 1) if ty == 4 else (ty,))}
+    for t in terms:
+        for k in ("nu_tau2", "s2_tau2", "eh_tau2"):
+            assert getattr(o, k)[t] == float(ref["%s.%d" % (k, t)]), (k, t)
