@@ -4,12 +4,18 @@
 // (bmagwa::Options, src/options.hpp:138-321, built from the unmodified
 // reference sources by oracle/Makefile) and prints every parsed field as
 // "opt.<name>=<value>" lines, or "opt.error=<message>" when the parser
-// throws.  tests/golden/make_golden.py runs it over the reference's INI files
-// and over edited copies to pin the product's parser (bmg_options_from_ini).
+// throws.  With --data it also loads the data the INI names with the
+// reference's Data class (src/data.hpp:45-72, src/data.cpp:141-434) and
+// prints the phenotypes, the covariates and the summary statistics as
+// "data.<name>=<value>" lines, or "data.error=<message>".
+// tests/golden/make_golden.py runs it over the reference's INI files, over
+// edited copies and over edited input files, to pin the product's parser
+// (bmg_options_from_ini) and readers (bmg_read_plink).
 #include <cstdio>
 #include <exception>
 #include <string>
 
+#include "data.hpp"
 #include "options.hpp"
 
 static void put(const char* k, const std::string& v) { std::printf("opt.%s=%s\n", k, v.c_str()); }
@@ -18,12 +24,27 @@ static void put(const char* k, unsigned long long v) { std::printf("opt.%s=%llu\
 
 int main(int argc, char** argv)
 {
-  if (argc != 2) {
-    std::fprintf(stderr, "usage: ref_probe INIFILE\n");
+  bool data = argc == 3 && std::string(argv[1]) == "--data";
+  if (argc != 2 && !data) {
+    std::fprintf(stderr, "usage: ref_probe [--data] INIFILE\n");
     return 2;
   }
   try {
-    bmagwa::Options o(argv[1]);
+    bmagwa::Options o(argv[argc - 1]);
+    if (data) {
+      try {
+        bmagwa::Data d(o.n, o.m_g, o.m_e, o.file_fam, o.file_g, o.recode_g_to_minor_allele_count, o.file_e,
+                       o.file_y);
+        for (size_t i = 0; i < o.n; ++i) std::printf("data.y.%zu=%.17g\n", i, d.y()(i));
+        for (size_t j = 1; j < d.m_e; ++j)
+          for (size_t i = 0; i < o.n; ++i) std::printf("data.e.%zu.%zu=%.17g\n", j - 1, i, d.e()(i, j));
+        std::printf("data.yy=%.17g\ndata.var_y=%.17g\ndata.mean_x=%.17g\ndata.var_x=%.17g\n", d.yy(),
+                    d.var_y(), d.mean_x(), d.var_x());
+      } catch (const std::exception& ex) {
+        std::printf("data.error=%s\n", ex.what());
+      }
+      return 0;
+    }
     put("file_fam", o.file_fam);
     put("file_g", o.file_g);
     put("file_e", o.file_e);

@@ -13,6 +13,7 @@ Runs only where the reference tree and its oracle build (oracle/_ref) exist:
 Usage:  python tests/golden/make_golden.py [REFERENCE_DIR [CASE ...]]
 (all cases when none is named)
 """
+import base64
 import json
 import os
 import re
@@ -326,6 +327,117 @@ def options_fixture():
         json.dump(cases, f, indent=0, sort_keys=True)
 
 
+READER_INI = """[datafiles]
+file_fam = {DIR}/d.fam
+file_g = {DIR}/d.bed
+recode_g_to_minor_allele_count = 1
+%s
+[sizes]
+n = 11
+m_g = 4
+m_e = %d
+[sampler]
+do_n_iter = 10
+n_rao = 10
+n_rao_burnin = 1
+thin = 1
+n_sample_tau2_and_missing = 10
+verbosity = 0
+[thread]
+n_threads = 1
+seeds = 5
+[model]
+types = A
+[prior]
+e_qg = 1
+var_qg = 1
+nu_sigma2 = 1
+R2mode_sigma2 = 0.2
+nu_tau2_A = 5
+s2_tau2_A = 0.05
+mu_alpha = 1
+inv_tau2_e_const_val = 0
+inv_tau2_e_val = 0.001
+"""
+
+
+def reader_cases():
+    """Input files of the reader parity fixture: n = 11 individuals, 4 SNPs,
+    two covariates, and one edit per reader rule of src/data.cpp:141-273.
+    A .fam with more than n rows is left out: the reference writes past the
+    end of its phenotype vector before it checks the count (src/data.cpp:158)."""
+    rng = np.random.default_rng(21)
+    n, p = 11, 4
+    ids = [("F%d" % (i // 3), "I%d" % i) for i in range(n)]
+    g = rng.integers(0, 3, size=(p, n))
+    code = np.where(g == 0, 0, np.where(g == 1, 2, 3)).astype(np.uint8)
+    pad = np.zeros((p, 12), dtype=np.uint8)
+    pad[:, :n] = code
+    pad = pad.reshape(p, 3, 4)
+    body = (pad[..., 0] | pad[..., 1] << 2 | pad[..., 2] << 4 | pad[..., 3] << 6).astype(np.uint8).reshape(-1)
+    bed = bytes([0x6C, 0x1B, 0x01]) + body.tobytes()
+    y = np.round(rng.normal(size=n), 6)
+    yalt = np.round(rng.normal(size=n), 6)
+    ecov = np.round(rng.normal(size=(n, 2)), 6)
+    order = rng.permutation(n)
+    fam_rows = ["%s %s 0 0 %d %.17g" % (f, i, 1 + k % 2, y[k]) for k, (f, i) in enumerate(ids)]
+    y_rows = ["%s %s %.17g" % (ids[k][0], ids[k][1], yalt[k]) for k in order]
+    e_rows = ["%s %s %.17g %.17g" % (ids[k][0], ids[k][1], ecov[k, 0], ecov[k, 1]) for k in order]
+    join = lambda rows: "\n".join(rows) + "\n"
+    base = {"d.fam": join(fam_rows), "d.y": join(y_rows + ["nobody nobody 1.5"]), "d.e": join(e_rows),
+            "d.bed": bed}
+    edit = lambda **kw: dict(base, **kw)
+    fam_tab = [r.replace(" ", "\t", 2) for r in fam_rows]
+    cases = {
+        "base": (base, True, True),
+        "no_alternate_files": (base, False, False),
+        "fam_no_trailing_newline": (edit(**{"d.fam": "\n".join(fam_rows)}), True, True),
+        "fam_tabs": (edit(**{"d.fam": join(fam_tab)}), True, True),
+        "fam_minus_9": (edit(**{"d.fam": join(fam_rows[:3] + ["F1 I3 0 0 1 -9"] + fam_rows[4:])}), False, False),
+        "fam_na": (edit(**{"d.fam": join(fam_rows[:5] + ["F1 I5 0 0 1 NA"] + fam_rows[6:])}), False, False),
+        "fam_duplicate": (edit(**{"d.fam": join(fam_rows[:10] + [fam_rows[9]])}), False, False),
+        "fam_short": (edit(**{"d.fam": join(fam_rows[:-1])}), False, False),
+        "y_missing_row": (edit(**{"d.y": join(y_rows[1:])}), True, False),
+        "y_no_trailing_newline": (edit(**{"d.y": "\n".join(y_rows)}), True, False),
+        "y_extra_column": (edit(**{"d.y": join([y_rows[0] + " 7"] + y_rows[1:])}), True, False),
+        "y_duplicate_row": (edit(**{"d.y": join(y_rows + [y_rows[0]])}), True, False),
+        "e_nan_first": (edit(**{"d.e": join(["%s %s nan 1.0" % ids[0]] + e_rows)}), False, True),
+        "e_nan_last": (edit(**{"d.e": join(e_rows + ["%s %s nan 1.0" % ids[0]])}), False, True),
+        "e_short_row": (edit(**{"d.e": join([" ".join(e_rows[0].split()[:3])] + e_rows[1:])}), False, True),
+        "e_unknown_row": (edit(**{"d.e": join(["X Y 1 2"] + e_rows)}), False, True),
+        "bed_bad_magic": (edit(**{"d.bed": bytes([0x6C, 0x1C, 0x01]) + body.tobytes()}), False, False),
+        "bed_individual_major": (edit(**{"d.bed": bytes([0x6C, 0x1B, 0x00]) + body.tobytes()}), False, False),
+        "bed_short": (edit(**{"d.bed": bed[:-1]}), False, False),
+        "bed_longer": (edit(**{"d.bed": bed + bytes([0xFF, 0x00])}), False, False),
+    }
+    return cases
+
+
+def readers_fixture():
+    """Run the reference's Data class (oracle/_ref/ref_probe --data) on each
+    reader case; store the files (the .bed base64-encoded), the INI and what
+    it read (phenotypes, covariates, summary statistics) or its error."""
+    out = []
+    with tempfile.TemporaryDirectory() as d:
+        for name, (files, with_y, with_e) in reader_cases().items():
+            extra = ("file_y = {DIR}/d.y\n" if with_y else "") + ("file_e = {DIR}/d.e\n" if with_e else "")
+            ini = READER_INI % (extra, 2 if with_e else 0)
+            for fn, data in files.items():
+                with open(os.path.join(d, fn), "wb") as f:
+                    f.write(data if isinstance(data, bytes) else data.encode())
+            with open(os.path.join(d, "r.ini"), "w") as f:
+                f.write(ini.replace("{DIR}", d))
+            r = subprocess.run([REF_PROBE, "--data", os.path.join(d, "r.ini")], check=True, capture_output=True,
+                               text=True)
+            if "opt.error=" in r.stdout:
+                raise SystemExit("reader case %s: %s" % (name, r.stdout.split("opt.error=")[1].strip()))
+            res = dict(line[5:].split("=", 1) for line in r.stdout.splitlines() if line.startswith("data."))
+            enc = {fn: (base64.b64encode(v).decode() if isinstance(v, bytes) else v) for fn, v in files.items()}
+            out.append({"name": name, "ini": ini, "files": enc, "result": res})
+    with open(os.path.join(HERE, "readers_ref.json"), "w") as f:
+        json.dump(out, f, indent=0, sort_keys=True)
+
+
 def main():
     if not os.path.exists(REF_BIN):
         raise SystemExit("build oracle/_ref first (make -C oracle)")
@@ -334,6 +446,8 @@ def main():
         known_answers()
     if not names or "options" in names:
         options_fixture()
+    if not names or "readers" in names:
+        readers_fixture()
     for name, (files, kw) in cases().items():
         if names and name not in names:
             continue

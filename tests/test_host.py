@@ -269,3 +269,56 @@ def test_options_match_the_reference_parser(tmp_path, capfd, case):
     for t in terms:
         for k in ("nu_tau2", "s2_tau2", "eh_tau2"):
             assert getattr(o, k)[t] == float(ref["%s.%d" % (k, t)]), (k, t)
+
+
+def _reader_cases():
+    with open(os.path.join(os.path.dirname(__file__), "golden", "readers_ref.json")) as f:
+        return json.load(f)
+
+
+def _materialize_reader_case(tmp_path, case):
+    import base64
+    for fn, v in case["files"].items():
+        data = base64.b64decode(v) if fn.endswith(".bed") else v.encode()
+        (tmp_path / fn).write_bytes(data)
+    ini = tmp_path / "r.ini"
+    ini.write_text(case["ini"].replace("{DIR}", str(tmp_path)))
+    return str(ini)
+
+
+@pytest.mark.parametrize("case", _reader_cases(), ids=lambda c: c["name"])
+def test_readers_match_the_reference_data_class(tmp_path, oracle, case):
+    """bmg_read_plink against the reference's Data class (src/data.cpp:141-273,
+    run on the same files by tests/golden/make_golden.py): the phenotypes of
+    the .fam or the alternate .y file, the covariates of the .e file, and the
+    error message of each malformed input; the oracle's summary statistics
+    (src/data.hpp:45-72) on the data read."""
+    o = bg.options_from_ini(_materialize_reader_case(tmp_path, case))
+    ref = case["result"]
+    if "error" in ref:
+        with pytest.raises(bg.BmgError) as ei:
+            bg.read_plink(o)
+        assert str(ei.value).split(": ", 1)[1] == ref["error"]
+        return
+    packed, y, e = bg.read_plink(o)
+    n = int(o.n)
+    assert [float(ref["y.%d" % i]) for i in range(n)] == list(y)
+    if o.m_e:
+        e = np.asarray(e).reshape(o.m_e, n)
+        for j in range(o.m_e):
+            assert [float(ref["e.%d.%d" % (j, i)]) for i in range(n)] == list(e[j]), j
+    port = oracle.Port(o, packed, y, e if o.m_e else None)
+    var_x, mean_x, var_y, yy = port.data_stats()
+    assert (var_x, mean_x, var_y, yy) == tuple(float(ref[k]) for k in ("var_x", "mean_x", "var_y", "yy"))
+
+
+def test_fam_with_more_rows_than_n_is_an_error(tmp_path):
+    """A .fam with n + 1 rows: the reference writes past its phenotype vector
+    before checking the count (src/data.cpp:158-166); the product reports the
+    count error the reference's check names."""
+    case = _reader_cases()[0]
+    fam = case["files"]["d.fam"]
+    case = dict(case, files=dict(case["files"], **{"d.fam": fam + "F9 I99 0 0 1 0.5\n"}))
+    o = bg.options_from_ini(_materialize_reader_case(tmp_path, case))
+    with pytest.raises(bg.BmgError, match="FAM file size does not match given n"):
+        bg.read_plink(o)
