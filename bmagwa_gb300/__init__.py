@@ -154,7 +154,7 @@ class Context:
         h = C.c_void_p()
         rc = lib().bmg_create(C.byref(opt), C.byref(h))
         if rc != 0:
-            raise BmgError(rc, "bmg_create failed")
+            raise BmgError(rc, lib().bmg_last_error(None).decode())
         self.h = h
 
     def _check(self, rc):

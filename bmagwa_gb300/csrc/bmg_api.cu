@@ -302,6 +302,9 @@ static void device_error_check(bmg_ctx* ctx)
 
 // ---------------------------------------------------------------- create
 
+// message of the last failed bmg_create on this thread (no context holds it)
+static thread_local std::string g_create_error;
+
 extern "C" bmg_status bmg_create(const bmg_options* opt, bmg_ctx** out)
 {
   bmg_ctx* ctx = nullptr;
@@ -358,16 +361,21 @@ extern "C" bmg_status bmg_create(const bmg_options* opt, bmg_ctx** out)
     return BMG_OK;
   } catch (const bmg_error& e) {
     if (out) *out = nullptr;
+    g_create_error = e.what();
     return e.status;
   } catch (const std::exception& e) {
     if (out) *out = nullptr;
+    g_create_error = e.what();
     return BMG_EINVAL;
   }
 }
 
 extern "C" void bmg_destroy(bmg_ctx* ctx) { delete ctx; }
 
-extern "C" const char* bmg_last_error(const bmg_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+extern "C" const char* bmg_last_error(const bmg_ctx* ctx)
+{
+  return ctx ? ctx->err.c_str() : g_create_error.c_str();
+}
 
 extern "C" const char* bmg_status_string(bmg_status s)
 {

@@ -341,6 +341,8 @@ bmg_status bmg_precompute_noalloc(const uint8_t* d_packed, uint64_t n, uint64_t 
                                   const int32_t* types, uint32_t n_types, double* d_out,
                                   uint32_t* offset_out, int32_t* d_flag, void* stream);
 
+/* Message of the last failed call on ctx; with ctx NULL, the message of the
+ * last failed bmg_create on the calling thread (which returns no context). */
 const char* bmg_last_error(const bmg_ctx* ctx);
 const char* bmg_status_string(bmg_status s);
 void bmg_destroy(bmg_ctx* ctx);

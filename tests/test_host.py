@@ -212,6 +212,11 @@ def test_create_rejects_unsupported_options_before_touching_the_device(tmp_path)
         rc = L.bmg_create(C.byref(o), C.byref(h))
         L.bmg_status_string.restype = C.c_char_p
         assert L.bmg_status_string(rc).decode() == status, field
+        assert h.value is None
+        # the message of a failed create stays readable without a context
+        assert len(L.bmg_last_error(None)) > 10, field
+        with pytest.raises(bg.BmgError, match=status):
+            bg.Context(o)
         setattr(o, field, old)
 
 
