@@ -73,7 +73,7 @@ bmg_scan_tc_kernel(DevConst K, TcParams P, const __grid_constant__ CUtensorMap m
       const uint32_t chain0 = (tile / P.m_tiles) * ct;
       const uint32_t chains_here = min(ct, K.n_chains - chain0);
       const uint32_t b = i % P.n_acc, u = i / P.n_acc;
-      // one warp waits; the verdict is shared so that all epilogue warps take
+      // one warp waits; the outcome is shared so that all epilogue warps take
       // the same number of named-barrier steps
       if (e == 0) {
         bool ok = false;

@@ -255,7 +255,7 @@ __device__ __forceinline__ void tc_main_roles(const TcParams& P, TcCtl& ctl, uin
       // after the MMA of stage g - SA.  One lane waits (mbarrier polls from
       // the 32 lanes of a warp are served one lane at a time) and the warp
       // barrier after the broadcast orders the other lanes' reads after its
-      // acquire.  The verdict is warp-uniform: the TMEM store is .sync.aligned.
+      // acquire.  The outcome is warp-uniform: the TMEM store is .sync.aligned.
       const bool need_slot = P.a_tmem && g >= SA;
       bool ok = false;
       if (lane == 0)

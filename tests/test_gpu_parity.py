@@ -3,7 +3,7 @@ and against the CPU oracle on synthetic data, same seeds, same random stream.
 
 Integer traces (moves, sizes, model sizes, loci, types) must be identical;
 floating-point traces and the Rao-Blackwellised posteriors agree to 1e-9
-relative (the spec LML tolerance)."""
+relative (the tolerance on every log marginal likelihood)."""
 import numpy as np
 import pytest
 
