@@ -1,7 +1,7 @@
 """Python handle on the CPU oracle (oracle/port) and on the reference build.
 
 ORACLE / TEST INFRASTRUCTURE: imported only by tests/, __graft_entry__.smoke()
-and bench.py's CPU-baseline leg, as the checker.  The product never imports it.
+and bench.py's CPU-baseline leg, as the oracle.  The product never imports it.
 """
 import ctypes as C
 import os

@@ -1,7 +1,7 @@
 /*
  * oracle/port/port.h -- C API of the CPU restatement of bmagwa's sampler.
  *
- * ORACLE / TEST INFRASTRUCTURE.  This is the checker the GPU path is compared
+ * ORACLE / TEST INFRASTRUCTURE.  This is the oracle the GPU path is compared
  * against and the CPU baseline bench.py times; it is never linked into, or
  * called by, the product.  It restates the reference algorithm
  * (src/sampler.hpp, src/sampler.cpp, src/model.hpp, src/prior.*, src/data*.cpp,

@@ -1,6 +1,6 @@
 """The CPU oracle against the reference's known answers and traces.
 
-The oracle (oracle/port) is the checker of every GPU parity test, so it is
+The oracle (oracle/port) is what every GPU parity test compares with, so it is
 pinned first: against the golden vectors of the reference's own tests
 (src/tests/*_tests.hpp) and against traces of the reference itself (the
 fixtures of tests/golden, made by tests/golden/make_golden.py)."""
