@@ -73,11 +73,17 @@ def build(force=False, verbose=False):
     if force or todo or _stale(LIB, objs):
         cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
         subprocess.run(cmd, check=True, capture_output=not verbose)
+    # the command-line entry; libbmg's own dependencies (the CUDA runtime) are
+    # resolved when it runs, not when it links.  A failed link leaves the
+    # library usable and is reported, not raised.
     cli_src = os.path.join(CSRC, "cli.cpp")
     if os.path.exists(cli_src) and (force or _stale(CLI, [cli_src, LIB])):
         cmd = ["g++", "-std=c++17", "-O2"] + INC + [cli_src, "-o", CLI, "-L" + OUT, "-lbmg",
-                                                    "-Wl,-rpath,$ORIGIN"]
-        subprocess.run(cmd, check=True, capture_output=not verbose)
+                                                    "-Wl,-rpath,$ORIGIN", "-Wl,--allow-shlib-undefined"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            print("warning: the bmagwa-gb300 command was not built:\n%s%s" % (r.stdout, r.stderr),
+                  file=sys.stderr)
     return LIB
 
 
