@@ -226,6 +226,11 @@ def cases():
         "example_flat": (files, dict(n=n, p=p, iters=400, n_rao=10, burnin=20, thin=10, nst=10, chains=1,
                                      seeds="31", types="A,AH", e_qg=20, var_qg=300, m_e=2, flat=1, save_beta=1,
                                      **efiles)),
+        # the features together: missing calls, two effect types, delayed
+        # rejection and continued adaptation with an acceptance-rate goal
+        "small_types_dr_missing": (small_miss, dict(n=30, p=7, iters=2000, n_rao=10, burnin=20, thin=2, nst=6,
+                                                    chains=2, seeds="3,4", types="A,AH", e_qg=2, var_qg=2,
+                                                    indiv=1, maxms=5, nbh=3, dr=5, adaptation=1, acpt=0.3)),
         "example_missing": (files_miss, dict(n=n, p=p, iters=600, n_rao=10, burnin=20, thin=10, nst=10,
                                              chains=2, seeds="1234,2345", types="A", e_qg=20, var_qg=300, m_e=2,
                                              indiv=1, **efiles)),
