@@ -76,6 +76,8 @@ def lib():
                                                C.c_uint32, C.POINTER(C.c_double)]
         L.bmgport_dd_exercise.argtypes = [C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64, C.c_uint32,
                                           C.c_uint64, C.c_void_p, C.POINTER(C.c_double), C.c_void_p]
+        L.bmgport_missing_step.argtypes = [C.c_void_p, C.c_uint32, C.c_uint64, C.c_uint64, C.c_void_p,
+                                           C.c_void_p, C.c_void_p]
         L.bmgport_destroy.argtypes = [C.c_void_p]
         _lib = L
     return _lib
@@ -160,6 +162,19 @@ class Port:
         lib().bmgport_get_state(self.h, chain, C.byref(st), _ptr(loci), _ptr(types), cap)
         k = st.model_size
         return st, loci[:k].copy(), types[:k].copy()
+
+    def missing_step(self, snp, n_reps=1, chain=0):
+        """n_reps imputations of a SNP's missing calls: (counts of the value
+        imputed for its first missing call, corrected precomputed row, the
+        four codings A, H, D, R after the last draw)."""
+        off = self.precomputed().shape[1]
+        xx = np.zeros(off)
+        g = np.zeros((4, int(self.opt.n)))
+        counts = np.zeros(3, dtype=np.uint64)
+        rc = lib().bmgport_missing_step(self.h, chain, snp, n_reps, _ptr(xx), _ptr(g), _ptr(counts))
+        if rc != 0:
+            raise ValueError("bad argument")
+        return counts, xx, g
 
     def inv_tau2_alpha2(self, chain=0):
         out = np.zeros(4)

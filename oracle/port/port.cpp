@@ -2820,4 +2820,28 @@ extern "C" int bmgport_dd_exercise(const double* w, uint64_t n, const int64_t* o
   }
 }
 
+/* Missing-call imputation of one SNP (DataModel::sample_missing_single and
+   update_prexx_cov, src/data_model.cpp:90-167), for the known answers of
+   src/tests/data_model_tests.hpp:129-322: n_reps draws from the chain's
+   stream, counting the value imputed for the SNP's first missing call; then
+   the SNP's precomputed row corrected for the last draw (xx_out, offset
+   values) and its four codings with the imputed values (geno_out, 4 x n). */
+extern "C" int bmgport_missing_step(bmgport* P, uint32_t chain, uint64_t snp, uint64_t n_reps, double* xx_out,
+                                    double* geno_out, uint64_t* counts)
+{
+  if (chain >= P->p.chains.size() || snp >= P->p.data->m_g) return 1;
+  Sampler* s = P->p.chains[chain];
+  for (int k = 0; k < 3; ++k) counts[k] = 0;
+  for (uint64_t r = 0; r < n_reps && !s->dm->miss_val[snp].empty(); ++r) {
+    s->dm->sample_missing_single((uint32_t)snp, s->rng);
+    ++counts[(int)s->dm->miss_val[snp][0]];
+  }
+  const PreXX* pre = P->p.pre;
+  for (int i = 0; i < pre->offset; ++i) xx_out[i] = pre->xx[snp * pre->offset + i];
+  s->dm->update_prexx_cov(snp, xx_out);
+  size_t n = P->p.data->n;
+  for (int t = 0; t < 4; ++t) s->dm->get_genotypes(t, snp, geno_out + t * n);
+  return 0;
+}
+
 extern "C" void bmgport_destroy(bmgport* P) { delete P; }

@@ -75,6 +75,11 @@ int bmgport_model_lml_remove(bmgport* P, uint32_t n_add, const uint32_t* snps, c
    (src/discrete_distribution.hpp:64-330) */
 int bmgport_dd_exercise(const double* w, uint64_t n, const int64_t* ops, uint64_t n_ops, uint32_t seed,
                         uint64_t n_samples, double* values_out, double* total_out, uint64_t* counts_out);
+/* n_reps imputations of one SNP's missing calls; the count of each value
+   imputed for its first missing call, the corrected precomputed row and the
+   four codings after the last draw (src/data_model.cpp:90-167) */
+int bmgport_missing_step(bmgport* P, uint32_t chain, uint64_t snp, uint64_t n_reps, double* xx_out,
+                         double* geno_out, uint64_t* counts);
 void bmgport_destroy(bmgport* P);
 
 #ifdef __cplusplus

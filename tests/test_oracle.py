@@ -419,3 +419,33 @@ def test_proposal_tree_sampling(oracle):
         q[zero] = 0
         assert t == pytest.approx(q.sum(), rel=1e-12)
         np.testing.assert_allclose(c / 1e6, q / q.sum(), rtol=0, atol=0.002, err_msg="size %d" % size)
+
+
+@pytest.mark.parametrize("types", [[0], [0, 4], [0, 1, 2, 3, 4]], ids=["A", "A_AH", "all"])
+def test_missing_call_imputation_known_answers(bmg, oracle, types):
+    """DataModelTests.{MissingSampling,XXUpdatesA,XXUpdatesAAH,XXUpdatesAll}
+    (src/tests/data_model_tests.hpp:129-322) on plinktest (n = 5, SNP 0 has a
+    missing call): the imputed value follows SNP 0's observed genotype
+    frequencies (0.25, 0.25, 0.5), and after every draw the corrected
+    precomputed sums equal the sums of the imputed codings."""
+    z = H.golden("data_tests")
+    packed, n = z["plink_bed"][3:], 5
+    fam = z["plink_fam"].tobytes().decode().split()
+    y = np.array([float(fam[6 * i + 5]) for i in range(n)])
+    o = small_opts(bmg, n, 10, types, recode_g_to_minor_allele_count=0)
+    port = oracle.Port(o, packed, y)
+    counts, _, g = port.missing_step(0, n_reps=100000)
+    assert g[0][3] >= 0
+    np.testing.assert_allclose(counts / counts.sum(), [0.25, 0.25, 0.5], atol=0.01)
+    terms = sorted({t for ty in types for t in ((0, 1) if ty == 4 else (ty,))})
+    for _ in range(100):
+        for snp in (0, 3):
+            _, xx, g = port.missing_step(snp, n_reps=1 if snp == 0 else 0)
+            assert np.all(g >= 0)
+            for k, t in enumerate(terms):
+                x = g[t]
+                assert xx[2 * k] == pytest.approx(x.sum(), abs=1e-12)
+                assert xx[2 * k + 1] == pytest.approx(x @ x - x.sum() ** 2 / n, abs=1e-12)
+            if 4 in types:
+                a, h = g[0], g[1]
+                assert xx[-1] == pytest.approx(a @ h - a.sum() * h.sum() / n, abs=1e-10)
