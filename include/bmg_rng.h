@@ -60,12 +60,13 @@ BMG_RNG_FN void bmg_mulhilo32(uint32_t a, uint32_t b, uint32_t* hi, uint32_t* lo
   *lo = (uint32_t)p;
 }
 
-/* One Philox4x32-10 block for counter (slot, sub). */
-BMG_RNG_FN void bmg_rng_block(uint32_t key0, uint32_t key1, uint64_t slot,
-                              uint32_t sub, uint32_t out[4])
+/* Philox4x32-10 of a 128-bit counter under a 64-bit key: ten rounds of two
+   32x32->64 multiplications, the key bumped by the Weyl constants between
+   rounds (the published algorithm; its known-answer vectors are checked on
+   the CPU). */
+BMG_RNG_FN void bmg_philox4x32_10(const uint32_t ctr[4], uint32_t key0, uint32_t key1, uint32_t out[4])
 {
-  uint32_t c0 = (uint32_t)slot, c1 = (uint32_t)(slot >> 32), c2 = sub,
-           c3 = BMG_RNG_TAG;
+  uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
   uint32_t k0 = key0, k1 = key1;
   for (int round = 0; round < 10; ++round) {
     uint32_t hi0, lo0, hi1, lo1;
@@ -78,6 +79,14 @@ BMG_RNG_FN void bmg_rng_block(uint32_t key0, uint32_t key1, uint64_t slot,
     k1 += 0xBB67AE85u;
   }
   out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+/* One block of a chain's stream: counter (slot, sub, tag). */
+BMG_RNG_FN void bmg_rng_block(uint32_t key0, uint32_t key1, uint64_t slot,
+                              uint32_t sub, uint32_t out[4])
+{
+  const uint32_t ctr[4] = {(uint32_t)slot, (uint32_t)(slot >> 32), sub, BMG_RNG_TAG};
+  bmg_philox4x32_10(ctr, key0, key1, out);
 }
 
 /* 53 random bits from two words, scaled into [0, 1). */

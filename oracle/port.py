@@ -78,6 +78,9 @@ def lib():
                                           C.c_uint64, C.c_void_p, C.POINTER(C.c_double), C.c_void_p]
         L.bmgport_missing_step.argtypes = [C.c_void_p, C.c_uint32, C.c_uint64, C.c_uint64, C.c_void_p,
                                            C.c_void_p, C.c_void_p]
+        L.bmgport_sample_beta_sigma2.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                 C.c_uint32, C.c_uint64, C.c_void_p, C.c_void_p, C.c_uint32,
+                                                 C.POINTER(C.c_uint32)]
         L.bmgport_destroy.argtypes = [C.c_void_p]
         _lib = L
     return _lib
@@ -175,6 +178,22 @@ class Port:
         if rc != 0:
             raise ValueError("bad argument")
         return counts, xx, g
+
+    def sample_beta_sigma2(self, snps, t_inds, inv_pairs, n_samples, seed=1234):
+        """(sigma2 draws, beta draws n_samples x blen) given the model of the
+        listed terms, from a stream seeded with seed."""
+        snps = np.ascontiguousarray(snps, dtype=np.uint32)
+        t_inds = np.ascontiguousarray(t_inds, dtype=np.uint8)
+        inv = np.ascontiguousarray(inv_pairs, dtype=np.float64).reshape(-1)
+        cap = 1 + 2 * len(snps) + int(self.opt.m_e)
+        s2 = np.zeros(n_samples)
+        beta = np.zeros((n_samples, cap))
+        blen = C.c_uint32()
+        if lib().bmgport_sample_beta_sigma2(self.h, len(snps), _ptr(snps) if len(snps) else None,
+                                            _ptr(t_inds) if len(snps) else None, _ptr(inv) if len(snps) else None,
+                                            seed, n_samples, _ptr(s2), _ptr(beta), cap, C.byref(blen)) != 0:
+            raise RuntimeError("oracle sampling failed")
+        return s2, beta[:, :blen.value]
 
     def inv_tau2_alpha2(self, chain=0):
         out = np.zeros(4)

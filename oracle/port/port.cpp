@@ -2844,4 +2844,34 @@ extern "C" int bmgport_missing_step(bmgport* P, uint32_t chain, uint64_t snp, ui
   return 0;
 }
 
+/* Draws of (sigma2, beta) from their joint conditional posterior given a
+   model of n_add terms (Model::sample_beta_sigma2, src/model.hpp:326-342,
+   Rand::rand_mvnormal_invchol, src/rand.hpp:144-168), from a stream of its
+   own (seed), for the distribution checks of
+   src/tests/model_tests.hpp:314-410.  beta_out holds n_samples rows of
+   *blen coefficients (constant first, then the model's columns). */
+extern "C" int bmgport_sample_beta_sigma2(bmgport* P, uint32_t n_add, const uint32_t* snps, const uint8_t* t_inds,
+                                          const double* itv, uint32_t seed, uint64_t n_samples, double* s2_out,
+                                          double* beta_out, uint32_t blen_cap, uint32_t* blen)
+{
+  try {
+    Sampler* s = P->p.chains.at(0);
+    Stats st;
+    Model m(P->p.data, s->dm, s->prior, &st, s->cur->cap);
+    m.compute_log_likelihood();
+    for (uint32_t i = 0; i < n_add; ++i) m.add_term(snps[i], t_inds[i], &itv[2 * i]);
+    Rand rng(seed, s->prior->n_plus_nu);
+    for (uint64_t r = 0; r < n_samples; ++r) {
+      m.sample_beta_sigma2(rng);
+      if (m.blen > blen_cap) return 1;
+      s2_out[r] = m.sigma2;
+      for (size_t j = 0; j < m.blen; ++j) beta_out[r * blen_cap + j] = m.beta[j];
+    }
+    *blen = (uint32_t)m.blen;
+    return 0;
+  } catch (...) {
+    return 1;
+  }
+}
+
 extern "C" void bmgport_destroy(bmgport* P) { delete P; }

@@ -80,6 +80,11 @@ int bmgport_dd_exercise(const double* w, uint64_t n, const int64_t* ops, uint64_
    four codings after the last draw (src/data_model.cpp:90-167) */
 int bmgport_missing_step(bmgport* P, uint32_t chain, uint64_t snp, uint64_t n_reps, double* xx_out,
                          double* geno_out, uint64_t* counts);
+/* n_samples draws of (sigma2, beta) given a model of n_add terms
+   (src/model.hpp:326-342); beta_out rows of blen_cap values */
+int bmgport_sample_beta_sigma2(bmgport* P, uint32_t n_add, const uint32_t* snps, const uint8_t* t_inds,
+                               const double* inv_tau2_alpha2, uint32_t seed, uint64_t n_samples, double* s2_out,
+                               double* beta_out, uint32_t blen_cap, uint32_t* blen);
 void bmgport_destroy(bmgport* P);
 
 #ifdef __cplusplus

@@ -38,3 +38,38 @@ def test_register_decode_of_packed_codes(tmp_path):
     out = subprocess.run([exe], capture_output=True, text=True)
     assert out.returncode == 0, out.stdout
     assert "mismatches 0" in out.stdout
+
+
+def test_random_stream(tmp_path):
+    """The stream every chain draws from (include/bmg_rng.h), compiled as C
+    for the host: Philox4x32-10 reproduces the published known-answer
+    vectors of Salmon et al. (SC'11), and the uniform, normal and gamma
+    variates have their moments over 4M / 1M draws (six standard errors)."""
+    cc = shutil.which("gcc")
+    if not cc:
+        pytest.skip("no C compiler")
+    exe = str(tmp_path / "rng_check")
+    subprocess.run([cc, "-O2", "-std=c11", "-ffp-contract=off", "-I" + os.path.join(os.path.dirname(HERE), "include"),
+                    os.path.join(HERE, "rng_check.c"), "-o", exe, "-lm"], check=True)
+    out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout
+    v = dict(line.split() for line in out.splitlines() if line.strip())
+    assert v["kat_zero"] == "6627e8d5e169c58dbc57ac4c9b00dbd8"
+    assert v["kat_ones"] == "408f276d41c83b0ea20bc7c66d5451fd"
+    assert v["kat_pi"] == "d16cfe0994fdcceb5001e42024126ea1"
+    f = {k: float(x) for k, x in v.items() if not k.startswith("kat")}
+    n = 4e6
+    assert abs(f["uniform_mean"] - 0.5) < 6 * (1 / 12) ** 0.5 / n ** 0.5
+    assert abs(f["uniform_var"] - 1 / 12) < 6 * (1 / 180) ** 0.5 / n ** 0.5
+    assert 0 <= f["uniform_min"] < 1e-5 and 1 - 1e-5 < f["uniform_max"] < 1
+    assert abs(f["normal_m1"]) < 6 / n ** 0.5
+    assert abs(f["normal_m2"] - 1) < 6 * 2 ** 0.5 / n ** 0.5
+    assert abs(f["normal_m3"]) < 6 * 15 ** 0.5 / n ** 0.5
+    assert abs(f["normal_m4"] - 3) < 6 * 96 ** 0.5 / n ** 0.5
+    m = n / 4
+    for a in (0.3, 0.5, 1.0, 2.5, 10.0, 100.0):
+        mean, var = f["gamma_mean_%g" % a], f["gamma_var_%g" % a]
+        assert abs(mean - a) < 6 * a ** 0.5 / m ** 0.5, a
+        # variance of the sample variance of a gamma: (mu4 - var^2) / m, mu4 = 3a^2 + 6a
+        assert abs(var - a) < 6 * ((3 * a * a + 6 * a - a * a) / m) ** 0.5, a
+    assert f["gamma_nan"] == 0
+    assert f["slot_addressable"] == 1

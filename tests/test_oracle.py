@@ -449,3 +449,47 @@ def test_missing_call_imputation_known_answers(bmg, oracle, types):
             if 4 in types:
                 a, h = g[0], g[1]
                 assert xx[-1] == pytest.approx(a @ h - a.sum() * h.sum() / n, abs=1e-10)
+
+
+def test_sigma2_beta_draws_follow_their_posterior(bmg, oracle):
+    """ModelTests.Sigma2BetaSampling (src/tests/model_tests.hpp:314-410):
+    draws of (sigma2, beta) given the constant-only model and given the model
+    with SNP 5 in A,H coding, on plinktest with nu_sigma2 = 0.  The reference's
+    constants (the residual sums of squares and the posterior means) are
+    checked against the closed form, and 1M draws through the oracle's random
+    stream against the closed-form moments: S / sigma2 ~ chi2(n) (its mean and
+    variance), and the mean and variance of each coefficient (a Student t with
+    n degrees of freedom around the posterior mean, scale sigma2 A^-1)."""
+    z = H.golden("data_tests")
+    packed, n = z["plink_bed"][3:], 5
+    fam = z["plink_fam"].tobytes().decode().split()
+    y = np.array([float(fam[6 * i + 5]) for i in range(n)])
+    o = small_opts(bmg, n, 10, [0, 4], e_qg=2, var_qg=4, nu_sigma2=0, s2_sigma2=1, mu_alpha=1,
+                   inv_tau2_e_const_val=0, recode_g_to_minor_allele_count=0)
+    port = oracle.Port(o, packed, y)
+    inv = 1.0 / (1.0 * 1.0 * (4.0 * 1.0 / (4.0 - 2.0)))
+    g = H.decode(packed, n, 10)
+    cases = [
+        ([], np.ones((n, 1)), np.array([0.0]), 0.0680, [0.32]),
+        ([5], np.column_stack([np.ones(n), H.coding(g[5], 0), H.coding(g[5], 1)]), np.array([0.0, inv, inv]),
+         0.02988235294117647101, [None, -0.11999999999999999556, -0.03529411764705892018]),
+    ]
+    N = 1000000
+    for snps, X, prec, syy_ref, means_ref in cases:
+        A = X.T @ X + np.diag(prec)
+        Ainv = np.linalg.inv(A)
+        mu = Ainv @ X.T @ y
+        S = y @ y - (X.T @ y) @ mu
+        assert S == pytest.approx(syy_ref, rel=1e-9)
+        for m_ref, m in zip(means_ref, mu):
+            if m_ref is not None:
+                assert m == pytest.approx(m_ref, rel=1e-9, abs=1e-12)
+        s2, beta = port.sample_beta_sigma2(snps, [1] * len(snps), [[inv, inv]] * len(snps), N, seed=1234)
+        q = S / s2
+        assert q.mean() == pytest.approx(n, abs=0.02)
+        assert q.var() == pytest.approx(2 * n, abs=0.15)
+        es2 = S / (n - 2)
+        for j in range(len(mu)):
+            sd = np.sqrt(es2 * Ainv[j, j])
+            assert beta[:, j].mean() == pytest.approx(mu[j], abs=6 * sd / np.sqrt(N))
+            assert beta[:, j].var() == pytest.approx(es2 * Ainv[j, j], rel=0.02)
