@@ -81,6 +81,7 @@ def lib():
         L.bmgport_sample_beta_sigma2.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p,
                                                  C.c_uint32, C.c_uint64, C.c_void_p, C.c_void_p, C.c_uint32,
                                                  C.POINTER(C.c_uint32)]
+        L.bmgport_prior_terms.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p]
         L.bmgport_destroy.argtypes = [C.c_void_p]
         _lib = L
     return _lib
@@ -194,6 +195,15 @@ class Port:
                                             seed, n_samples, _ptr(s2), _ptr(beta), cap, C.byref(blen)) != 0:
             raise RuntimeError("oracle sampling failed")
         return s2, beta[:, :blen.value]
+
+    def prior_terms(self, Ns, nl, ta, tr=0):
+        """(log model prior of Ns, change on add of type ta with nl loci,
+        change on removal of type ta with nl loci, change on switch ta -> tr)."""
+        ns = np.ascontiguousarray(Ns, dtype=np.int32)
+        out = np.zeros(4)
+        if lib().bmgport_prior_terms(self.h, _ptr(ns), nl, ta, tr, _ptr(out)) != 0:
+            raise ValueError("bad type")
+        return out
 
     def inv_tau2_alpha2(self, chain=0):
         out = np.zeros(4)

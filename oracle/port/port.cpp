@@ -2874,4 +2874,21 @@ extern "C" int bmgport_sample_beta_sigma2(bmgport* P, uint32_t n_add, const uint
   }
 }
 
+/* The model prior of chain 0 (Prior::compute_log_model and the changes on
+   add, remove and type switch, src/prior.hpp:144-183): out = {log model
+   prior of Ns, change on adding a term of type ta with nl loci, change on
+   removing one of type ta with nl loci, change on switching ta -> tr}. */
+extern "C" int bmgport_prior_terms(bmgport* P, const int32_t* Ns, int32_t nl, int32_t ta, int32_t tr, double* out)
+{
+  if (P->p.chains.empty() || ta < 0 || ta > 4 || tr < 0 || tr > 4) return 1;
+  const Prior* pr = P->p.chains[0]->prior;
+  int ns[5];
+  for (int t = 0; t < 5; ++t) ns[t] = Ns[t];
+  out[0] = pr->compute_log_model(ns);
+  out[1] = pr->compute_log_change_on_add(ns, nl, ta);
+  out[2] = pr->compute_log_change_on_rem(ns, nl, ta);
+  out[3] = pr->compute_log_change_on_swi(ns, ta, tr);
+  return 0;
+}
+
 extern "C" void bmgport_destroy(bmgport* P) { delete P; }

@@ -85,6 +85,9 @@ int bmgport_missing_step(bmgport* P, uint32_t chain, uint64_t snp, uint64_t n_re
 int bmgport_sample_beta_sigma2(bmgport* P, uint32_t n_add, const uint32_t* snps, const uint8_t* t_inds,
                                const double* inv_tau2_alpha2, uint32_t seed, uint64_t n_samples, double* s2_out,
                                double* beta_out, uint32_t blen_cap, uint32_t* blen);
+/* log model prior of Ns and its changes on add / remove (type ta, nl loci)
+   and on a type switch ta -> tr (src/prior.hpp:144-183) */
+int bmgport_prior_terms(bmgport* P, const int32_t* Ns, int32_t nl, int32_t ta, int32_t tr, double* out);
 void bmgport_destroy(bmgport* P);
 
 #ifdef __cplusplus

@@ -493,3 +493,30 @@ def test_sigma2_beta_draws_follow_their_posterior(bmg, oracle):
             sd = np.sqrt(es2 * Ainv[j, j])
             assert beta[:, j].mean() == pytest.approx(mu[j], abs=6 * sd / np.sqrt(N))
             assert beta[:, j].var() == pytest.approx(es2 * Ainv[j, j], rel=0.02)
+
+
+def test_model_prior_changes_known_answer(bmg, oracle):
+    """PriorTests.SimpleAddRemove (src/tests/prior_tests.hpp:31-125): with
+    e_qg = 3, var_qg = 9 and types A, AH, each change on add, remove and type
+    switch equals the difference of the log model priors (1e-6 there; 1e-12
+    here)."""
+    z = H.golden("data_tests")
+    packed, n = z["plink_bed"][3:], 5
+    fam = z["plink_fam"].tobytes().decode().split()
+    y = np.array([float(fam[6 * i + 5]) for i in range(n)])
+    o = small_opts(bmg, n, 10, [0, 4], e_qg=3, var_qg=9, nu_sigma2=1, s2_sigma2=1, mu_alpha=1,
+                   inv_tau2_e_const_val=0)
+    for t in range(4):
+        o.nu_tau2[t], o.s2_tau2[t] = 3, 1
+    port = oracle.Port(o, packed, y)
+    A, AH = 0, 4
+    lm = lambda ns: port.prior_terms(ns, 0, A)[0]
+    for ns, ns_new, nl, t in [([0, 0, 0, 0, 0], [1, 0, 0, 0, 0], 0, A), ([2, 0, 0, 0, 3], [3, 0, 0, 0, 3], 5, A),
+                              ([0, 0, 0, 0, 0], [0, 0, 0, 0, 1], 0, AH), ([3, 0, 0, 0, 2], [3, 0, 0, 0, 3], 5, AH)]:
+        assert port.prior_terms(ns, nl, t)[1] == pytest.approx(lm(ns_new) - lm(ns), abs=1e-12)
+        assert port.prior_terms(ns_new, nl + 1, t)[2] == pytest.approx(lm(ns) - lm(ns_new), abs=1e-12)
+    same = [3, 0, 0, 0, 3]
+    assert port.prior_terms(same, 6, AH, AH)[3] == pytest.approx(0.0, abs=1e-12)
+    ns, ns_new = [3, 0, 0, 0, 2], [2, 0, 0, 0, 3]
+    assert port.prior_terms(ns, 5, AH, A)[3] == pytest.approx(lm(ns_new) - lm(ns), abs=1e-12)
+    assert port.prior_terms(ns_new, 5, A, AH)[3] == pytest.approx(lm(ns) - lm(ns_new), abs=1e-12)
