@@ -231,6 +231,11 @@ def cases():
         "small_types_dr_missing": (small_miss, dict(n=30, p=7, iters=2000, n_rao=10, burnin=20, thin=2, nst=6,
                                                     chains=2, seeds="3,4", types="A,AH", e_qg=2, var_qg=2,
                                                     indiv=1, maxms=5, nbh=3, dr=5, adaptation=1, acpt=0.3)),
+        # a prior that puts most mass on ~600 of the 1500 SNPs: the model grows
+        # past 128 columns (A,AH terms), where the GPU keeps its Cholesky
+        # factors in global memory instead of shared memory
+        "example_large": (files, dict(n=n, p=p, iters=300, n_rao=10, burnin=10, thin=5, nst=10, chains=1,
+                                      seeds="17", types="A,AH", e_qg=600, var_qg=2000, m_e=2, **efiles)),
         "example_missing": (files_miss, dict(n=n, p=p, iters=600, n_rao=10, burnin=20, thin=10, nst=10,
                                              chains=2, seeds="1234,2345", types="A", e_qg=20, var_qg=300, m_e=2,
                                              indiv=1, **efiles)),
