@@ -1,0 +1,52 @@
+"""GPU parity cases added after the last GB300 run: marked non-strict xfail
+until a GPU run has passed them, so that their outcome is reported either
+way.  The file sorts last, so that a failure here cannot stop or disturb the
+GPU tests that already passed."""
+import numpy as np
+import pytest
+
+import helpers as H
+from test_gpu_parity import RTOL, run_gpu
+
+pytestmark = pytest.mark.gpu
+
+
+NOT_YET_ON_GPU = pytest.mark.xfail(reason="not yet run on a GB300", strict=False)
+
+
+@NOT_YET_ON_GPU
+@pytest.mark.parametrize("name", ["small_flat", "example_flat", "example_large"])
+def test_gpu_matches_reference_more_options(bmg, tmp_path, name):
+    """A flat proposal with the beta trace and raw genotypes (small_flat,
+    example_flat), and a model that grows past the 128 columns the move
+    kernel keeps in shared memory (example_large), against the reference's
+    traces."""
+    z = H.golden("ref_" + name)
+    ini = H.materialize(z, tmp_path)
+    opt = bmg.options_from_ini(ini)
+    packed, y, e = bmg.read_plink(opt)
+    ctx, col = run_gpu(bmg, opt, packed, y, e, opt.do_n_iter)
+    for c in range(opt.n_chains):
+        ref = H.ref_chain(z, c)
+        got = col.chain(c)
+        H.compare(ref, got, rtol=RTOL, label="%s chain %d" % (name, c))
+        if "c%d_beta" % c in z.files:
+            np.testing.assert_allclose(got["beta"], z["c%d_beta" % c], rtol=1e-7, atol=1e-10)
+        np.testing.assert_allclose(ctx.rao(c)[0], ref["rao"], rtol=RTOL, atol=1e-12)
+
+
+@NOT_YET_ON_GPU
+def test_cli_writes_the_reference_files(bmg, tmp_path):
+    """bmagwa-gb300 INIFILE end to end: the trace files equal the reference's."""
+    import os
+    import subprocess
+    z = H.golden("ref_small")
+    ini = H.materialize(z, tmp_path)
+    cli = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "bmagwa_gb300", "_build",
+                       "bmagwa-gb300")
+    r = subprocess.run([cli, ini], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    import oracle.port as op
+    for c in range(2):
+        out = op.read_ref_outputs(str(tmp_path / "out" / "chain"), c, 7)
+        H.compare(H.ref_chain(z, c), out, rtol=RTOL, label="cli chain %d" % c)
