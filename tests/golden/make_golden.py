@@ -231,6 +231,11 @@ def cases():
         "small_types_dr_missing": (small_miss, dict(n=30, p=7, iters=2000, n_rao=10, burnin=20, thin=2, nst=6,
                                                     chains=2, seeds="3,4", types="A,AH", e_qg=2, var_qg=2,
                                                     indiv=1, maxms=5, nbh=3, dr=5, adaptation=1, acpt=0.3)),
+        # individual tau2 with all five effect types: the scan's per-SNP tau2
+        # draws then cover four terms
+        "example_types_indiv": (files, dict(n=n, p=p, iters=300, n_rao=10, burnin=5, thin=5, nst=8, chains=1,
+                                            seeds="23", types="A,H,D,R,AH", e_qg=20, var_qg=300, m_e=2, indiv=1,
+                                            **efiles)),
         # a prior that puts most mass on ~600 of the 1500 SNPs: the model grows
         # past 128 columns (A,AH terms), where the GPU keeps its Cholesky
         # factors in global memory instead of shared memory

@@ -309,7 +309,8 @@ def test_rb_closed_form(bmg, oracle):
 
 @pytest.mark.parametrize("name", ["small", "small_types", "example", "example_types", "small_dr", "example_dr",
                                   "small_types_dr", "small_types_missing", "example_missing", "small_flat",
-                                  "example_flat", "small_types_dr_missing", "example_large"])
+                                  "example_flat", "small_types_dr_missing", "example_large",
+                                  "example_types_indiv"])
 def test_oracle_matches_reference_traces(bmg, oracle, tmp_path, name):
     """The oracle reproduces the compiled reference's traces bit for bit (the
     *_dr cases with delayed rejection on, the *_missing cases with missing

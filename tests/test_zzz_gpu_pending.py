@@ -15,11 +15,12 @@ NOT_YET_ON_GPU = pytest.mark.xfail(reason="not yet run on a GB300", strict=False
 
 
 @NOT_YET_ON_GPU
-@pytest.mark.parametrize("name", ["small_flat", "example_flat", "example_large"])
+@pytest.mark.parametrize("name", ["small_flat", "example_flat", "example_large", "example_types_indiv"])
 def test_gpu_matches_reference_more_options(bmg, tmp_path, name):
     """A flat proposal with the beta trace and raw genotypes (small_flat,
-    example_flat), and a model that grows past the 128 columns the move
-    kernel keeps in shared memory (example_large), against the reference's
+    example_flat), a model that grows past the 128 columns the move kernel
+    keeps in shared memory (example_large), and individual tau2 draws over
+    four terms in the scan (example_types_indiv), against the reference's
     traces."""
     z = H.golden("ref_" + name)
     ini = H.materialize(z, tmp_path)
