@@ -29,18 +29,12 @@ sys.path.insert(0, ROOT)
 
 import numpy as np
 
-WORKLOADS = {
-    "scan": dict(n=10000, p=500000, chains=32, n_rao=1, ld_block=50, causal=30, types="A"),
-    "batched": dict(n=5000, p=50000, chains=8, n_rao=500, ld_block=50, causal=20, types="A,AH"),
-    "plain": dict(n=1000, p=5000, chains=1, n_rao=500, ld_block=0, causal=10, types="A"),
-    # the learned proposal against the plain adaptive one (inclusion ESS/s)
-    "learned": dict(n=10000, p=200000, chains=16, n_rao=1, ld_block=100, causal=50, types="A,AH", dominance=10,
-                    burnin=600, sample=1500),
-    # many phenotypes of uneven sample size: one chain per phenotype, each
-    # fitted to the individuals its missingness mask keeps (8k-20k)
-    "phenotypes": dict(n=20000, p=1000000, chains=256, n_rao=1, ld_block=50, causal=(5, 100), beta_sd=0.1,
-                       types="A", keep=(0.4, 1.0)),
-}
+from bmagwa_gb300.workloads import WORKLOADS, make_data, options, scan_terms  # noqa: E402
+
+# sizes of the inclusion-ESS leg per workload: burn-in iterations, then
+# sampled iterations (thinned samples = sampled / thin)
+ESS_LEG = {"scan": (1000, 2000), "batched": (10000, 20000), "plain": (10000, 20000)}
+
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM = 6800.0
 FALLBACK_BF16_SUSTAINED = 1700.0
@@ -49,53 +43,6 @@ FALLBACK_BF16_SUSTAINED = 1700.0
 def env_rank():
     from bmagwa_gb300 import replicas
     return replicas.rank_info()
-
-
-def options(bg, wl, seed0, iters):
-    from bmagwa_gb300 import abi
-    o = bg.default_options()
-    o.n, o.m_g, o.m_e = wl["n"], wl["p"], 0
-    types = [abi.TYPE_NAMES[t] for t in wl["types"].split(",")]
-    o.n_types = len(types)
-    for i, t in enumerate(sorted(types)):
-        o.types[i] = t
-    o.do_n_iter = iters
-    o.n_rao = wl["n_rao"]
-    o.thin = 1 if wl["n_rao"] < 10 else 10
-    o.n_rao_burnin = max(1, iters // (2 * wl["n_rao"]))
-    o.n_sample_tau2_and_missing = 10
-    o.max_move_size = 20
-    o.max_SNP_neighborhood_size = 20
-    o.p_move_size, o.p_move_size_nbs, o.p_move_size_nbc = 0.2, 0.7, 0.25
-    o.e_qg, o.var_qg, o.nu_sigma2, o.R2mode_sigma2, o.mu_alpha = 20, 300, 1, 0.2, 1
-    o.inv_tau2_e_const_val, o.inv_tau2_e_val = 0.0, 0.001
-    for t in range(4):
-        o.nu_tau2[t], o.s2_tau2[t] = 5, 0.05
-    o.max_model_size = 256
-    o.graph_iters = 64
-    o.quiet = 1
-    bg.set_seeds(o, [seed0 + 1000 * c for c in range(wl["chains"])])
-    return o
-
-
-def make_data(wl, seed, device):
-    """Packed genotypes and the phenotype (or, with wl["keep"], one
-    phenotype per chain and the masks of the individuals each keeps)."""
-    from bmagwa_gb300 import synth
-    counts, _ = synth.genotypes(wl["n"], wl["p"], wl["ld_block"], seed, device=device)
-    if "keep" in wl:
-        rng = np.random.default_rng(seed + 101)
-        ys, masks = [], []
-        for k in range(wl["chains"]):
-            yk, _, _ = synth.phenotype(counts, wl["causal"], wl["beta_sd"], 0, seed + 1000 * k, device=device)
-            ys.append(yk)
-            masks.append((rng.random(wl["n"]) < rng.uniform(*wl["keep"])).astype(np.uint8))
-        y = (np.stack(ys), np.stack(masks))
-    else:
-        y, _, _ = synth.phenotype(counts, wl["causal"], 0.2, wl.get("dominance", 0), seed, device=device)
-    packed = synth.pack(counts).cpu().numpy().reshape(-1)
-    del counts
-    return packed, y
 
 
 def set_pheno(ctx, y):
@@ -168,14 +115,6 @@ def peak_bf16_sustained():
         return FALLBACK_BF16_SUSTAINED, "fallback (sustained)"
 
 
-def scan_terms(types):
-    """Coding rows per SNP in the scan's GEMM (A, H, D, R; AH uses A and H)."""
-    rows = set()
-    for t in types.split(","):
-        rows |= {"A": {0}, "H": {1}, "D": {2}, "R": {3}, "AH": {0, 1}}[t]
-    return len(rows)
-
-
 def scan_traffic_per_launch(workload):
     """DRAM bytes per scan launch from the committed ncu summary, if present."""
     path = os.path.join(ROOT, "profiles", "scan_%s_ncu.md" % workload)
@@ -188,18 +127,76 @@ def scan_traffic_per_launch(workload):
     return None
 
 
-def cpu_sample(wl, packed, y, threads, iters, seed0):
-    """The oracle on the host cores: `threads` chains for `iters` iterations each."""
-    import bmagwa_gb300 as bg
+# iterations of each chain in the CPU leg: the scan workload's FP64 scan of
+# 500,000 SNPs takes seconds per iteration on a core, the move-bound
+# workloads run >= 1,000 iterations including RB steps
+CPU_ITERS = {"scan": 1, "batched": 1000, "plain": 3000}
+
+
+def cpu_sample(wl, workload, packed, y, threads, seed0):
+    """The oracle on the host cores: `threads` chains (one pthread each) of
+    the same workload for CPU_ITERS[workload] iterations; returns
+    (chain-iterations/s, seconds, iterations)."""
     import oracle.port as op
-    o = options(bg, wl, seed0, iters)
+    iters = CPU_ITERS.get(workload, 1)
+    o = options(wl, seed0, iters, chains=threads)
     o.max_model_size = 1024
-    bg.set_seeds(o, [seed0 + 1000 * c for c in range(threads)])
     port = op.Port(o, packed, y)
     t0 = time.perf_counter()
     port.run(iters, threads=threads)
     dt = time.perf_counter() - t0
-    return threads * iters / dt, dt
+    return threads * iters / dt, dt, iters
+
+
+def ess_leg_gpu(bg, wl, workload, packed, y, seed, scan_impl):
+    """Inclusion-indicator ESS of the sampling phase after a burn-in, outside
+    the timed value: ESS_LEG[workload] = (burn-in, sampled iterations), ESS
+    (Geyer) over SNPs with 0.05 < PIP < 0.95 per chain, per second of device
+    time of the sampled iterations."""
+    import torch
+    from bmagwa_gb300 import ess
+    burn, samp = ESS_LEG[workload]
+    o = options(wl, seed + 29, burn + samp)
+    o.scan_impl = scan_impl
+    o.n_rao_burnin = max(1, burn // wl["n_rao"])
+    ctx = bg.Context(o)
+    ctx.load_bed(packed)
+    set_pheno(ctx, y)
+    ctx.set_covariates(None)
+    ctx.precompute()
+    ctx.run(burn, collect=False)
+    torch.cuda.synchronize()
+    ctx.reset_timings()
+    col = ctx.run(samp, collect=True)
+    sec = ctx.timings()[3] / 1000.0
+    tr = [col.chain(c) for c in range(wl["chains"])]
+    ctx.close()
+    out = ess.summarize([(t["modelsize"], t["loci"]) for t in tr], sec)
+    out.update(burnin_iters=burn, sample_iters=samp, samples_per_chain=int(len(tr[0]["modelsize"])),
+               seconds=sec, chains=wl["chains"])
+    return out
+
+
+def ess_leg_cpu(wl, workload, packed, y, seed, threads):
+    """The same ESS leg on the oracle: min(chains, threads) chains, one
+    pthread each, seconds = wall time of the sampled iterations."""
+    import oracle.port as op
+    from bmagwa_gb300 import ess
+    burn, samp = ESS_LEG[workload]
+    chains = max(1, min(wl["chains"], threads))
+    o = options(wl, seed + 29, burn + samp, chains=chains)
+    o.n_rao_burnin = max(1, burn // wl["n_rao"])
+    o.max_model_size = 1024
+    port = op.Port(o, packed, y)
+    port.run(burn, threads=chains)
+    t0 = time.perf_counter()
+    col = port.run(samp, threads=chains)
+    sec = time.perf_counter() - t0
+    tr = [col.chain(c) for c in range(chains)]
+    out = ess.summarize([(t["modelsize"], t["loci"]) for t in tr], sec)
+    out.update(burnin_iters=burn, sample_iters=samp, samples_per_chain=int(len(tr[0]["modelsize"])),
+               seconds=sec, chains=chains, cores=chains)
+    return out
 
 
 def run_gb300(args, wl):
@@ -214,7 +211,7 @@ def run_gb300(args, wl):
     seed = 1 + 7919 * rank
     packed, y = make_data(wl, seed, "cuda")
     iters_total = args.warmup + args.steps
-    o = options(bg, wl, seed, iters_total)
+    o = options(wl, seed, iters_total)
     o.scan_impl = args.scan
     ctx = bg.Context(o)
     ctx.load_bed(packed)
@@ -254,7 +251,7 @@ def run_gb300(args, wl):
     ctx.close()
     e2e = None
     if args.e2e:
-        o2 = options(bg, wl, seed + 17, iters_total)
+        o2 = options(wl, seed + 17, iters_total)
         o2.scan_impl = args.scan
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -285,12 +282,6 @@ def run_gb300(args, wl):
         e2e = {"value": args.steps * wl["chains"] * world / e2e_s, "unit": "iter/s",
                "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
                "seconds": breakdown}
-        # inclusion-indicator ESS of the same run (Geyer initial monotone
-        # sequence over the thinned trace of each chain)
-        from bmagwa_gb300 import ess
-        tr = [col.chain(c) for c in range(wl["chains"])]
-        e2e["inclusion_ess"] = dict(ess.summarize([(t["modelsize"], t["loci"]) for t in tr if t], e2e_s),
-                                    samples_per_chain=int(len(tr[0]["modelsize"])) if tr[0] else 0)
     # roofline of the scan kernel
     p, n, C = wl["p"], wl["n"], wl["chains"]
     scan_ms = ms[1] / max(1, n_scans)
@@ -338,12 +329,16 @@ def run_gb300(args, wl):
                              "frac": (hbm_gbs / peak_h) if hbm_gbs else None, "peak_kind": peak_h_kind}},
         "clocks": clocks.summary(),
     }
+    if rank == 0 and args.ess and args.workload in ESS_LEG:
+        out["inclusion_ess"] = ess_leg_gpu(bg, wl, args.workload, packed, y, seed, args.scan)
     if rank == 0 and args.cpu_baseline:
         threads = max(1, min(C, os.cpu_count() or 1))
-        cv, cdt = cpu_sample(wl, packed, y, threads, 1, seed)
+        cv, cdt, citers = cpu_sample(wl, args.workload, packed, y, threads, seed)
         out["cpu_baseline"] = {"value": cv, "unit": "iter/s", "cores": threads, "kind": "port",
-                               "sample": "%d chains x 1 iteration of the same workload (%.1f s)"
-                                         % (threads, cdt)}
+                               "sample": "%d chains x %d iterations of the same workload (%.1f s)"
+                                         % (threads, citers, cdt)}
+        if args.ess and args.workload in ("plain", "batched"):
+            out["cpu_baseline"]["inclusion_ess"] = ess_leg_cpu(wl, args.workload, packed, y, seed, threads)
     if rank == 0:
         print(json.dumps(out))
     if world > 1:
@@ -364,7 +359,7 @@ def run_learned_compare(args, wl):
     burn, samp = wl["burnin"], wl["sample"]
     out = {}
     for name, mode in (("plain", 0), ("learned", 1)):
-        o = options(bg, wl, seed, burn + samp)
+        o = options(wl, seed, burn + samp)
         o.n_rao_burnin = burn // wl["n_rao"]
         o.proposal = mode
         ctx = bg.Context(o)
@@ -395,31 +390,34 @@ def run_learned_compare(args, wl):
 
 
 def run_reference(args, wl):
+    """The reference's CPU path (the oracle port, bit-identical to the
+    compiled reference) on the host cores: one pthread per chain, as many
+    chains as cores (at most the workload's), the same workload and options.
+    Only oracle/ libraries are loaded here; the options come from the
+    library-free mirror of the defaults."""
     rank, world, _ = env_rank()
     if rank != 0:
         return
-    import bmagwa_gb300 as bg
     import oracle.port as op
-    bg.build()
     op.build()
     seed = 1
     packed, y = make_data(wl, seed, "cpu")
     threads = max(1, min(wl["chains"], os.cpu_count() or 1))
-    o = options(bg, wl, seed, args.warmup + args.steps)
+    per_step = CPU_ITERS.get(args.workload, 1)
+    o = options(wl, seed, (args.warmup + args.steps) * per_step, chains=threads)
     o.max_model_size = 1024
-    bg.set_seeds(o, [seed + 1000 * c for c in range(threads)])
     port = op.Port(o, packed, y)
     if args.warmup:
-        port.run(1, threads=threads)
-    # each step is one iteration of `threads` chains; stop after about a minute
+        port.run(per_step if per_step > 1 else 1, threads=threads)
+    # each step is per_step iterations of `threads` chains; stop after about a minute
     done, dt = 0, 0.0
     while done < args.steps and (done == 0 or dt < 60.0):
         t0 = time.perf_counter()
-        port.run(1, threads=threads)
+        port.run(per_step, threads=threads)
         dt += time.perf_counter() - t0
         done += 1
     args.steps = done
-    v = done * threads / dt
+    v = done * per_step * threads / dt
     print(json.dumps({
         "impl": "reference",
         "metric": "MCMC chain-iterations/s (RB scan of all SNPs every iteration)",
@@ -429,7 +427,8 @@ def run_reference(args, wl):
         "config": {"workload": args.workload, "n": wl["n"], "p": wl["p"], "chains": threads,
                    "n_rao": wl["n_rao"], "types": wl["types"]},
         "cpu_baseline": {"value": v, "unit": "iter/s", "cores": threads, "kind": "port",
-                         "sample": "%d chains x %d iterations (one pthread per chain)" % (threads, args.steps)},
+                         "sample": "%d chains x %d iterations (one pthread per chain)"
+                                   % (threads, args.steps * per_step)},
         "e2e": {"value": v, "unit": "iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
 
@@ -447,6 +446,8 @@ def main():
     ap.add_argument("--n", type=int, default=None, help="override the individuals (profiling)")
     ap.add_argument("--chains", type=int, default=None, help="override the chains (profiling)")
     ap.add_argument("--no-e2e", dest="e2e", action="store_false")
+    ap.add_argument("--no-ess", dest="ess", action="store_false",
+                    help="skip the inclusion-ESS leg (burn-in + sampled iterations after the timed region)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

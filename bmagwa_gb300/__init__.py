@@ -69,6 +69,8 @@ def lib():
         L.bmg_precompute_noalloc.argtypes = [vp, u64, u64, C.c_int32, C.POINTER(C.c_int32), u32, vp,
                                              C.POINTER(u32), vp, vp]
         L.bmg_precompute_noalloc.restype = C.c_int
+        L.bmg_scan_yhat.argtypes = [vp, vp, C.c_double, vp, vp]
+        L.bmg_scan_yhat.restype = C.c_int
         L.bmg_get_last_scan.argtypes = [vp, u32, vp, vp]
         L.bmg_get_data_stats.argtypes = [vp, vp]
         L.bmg_get_launch_count.argtypes = [vp, C.POINTER(u64)]
@@ -118,11 +120,7 @@ def options_from_ini(path, quiet=True):
 
 
 def set_seeds(opt, seeds):
-    arr = (C.c_uint32 * len(seeds))(*[int(s) for s in seeds])
-    opt.seeds = C.cast(arr, C.POINTER(C.c_uint32))
-    opt.n_chains = len(seeds)
-    opt._seeds = arr
-    return opt
+    return abi.set_seeds(opt, seeds)
 
 
 def read_plink(opt):
@@ -143,6 +141,7 @@ class Context:
 
     def __init__(self, opt):
         self.opt = opt
+        self.n = int(opt.n)
         self.m_g = int(opt.m_g)
         self.n_types = int(opt.n_types)
         self.n_chains = int(opt.n_chains)
@@ -220,6 +219,18 @@ class Context:
         lo = np.zeros(self.n_chains * self.m_g)
         self._check(lib().bmg_scan_logodds(self.h, _ptr(lo)))
         return lo.reshape(self.n_chains, self.m_g)
+
+    def scan_yhat(self, y_hat, sigma2):
+        """RB scan of every chain against the given fitted values (n doubles)
+        and sigma2 (which becomes every chain's sigma2): (p_r, log odds), each
+        (chains, m_g)."""
+        yh = np.ascontiguousarray(y_hat, dtype=np.float64)
+        if yh.size != self.n:
+            raise ValueError("y_hat must have n entries")
+        pr = np.zeros(self.n_chains * self.m_g)
+        lo = np.zeros(self.n_chains * self.m_g)
+        self._check(lib().bmg_scan_yhat(self.h, _ptr(yh), float(sigma2), _ptr(pr), _ptr(lo)))
+        return pr.reshape(self.n_chains, self.m_g), lo.reshape(self.n_chains, self.m_g)
 
     def scan_schur(self):
         """(chains, m_g, terms) exact change of each chain's log marginal

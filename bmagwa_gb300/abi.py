@@ -176,6 +176,44 @@ def set_path(opt, field, value):
     setattr(opt, field, b)
 
 
+def default_options():
+    """The reference's defaults of every optional key (src/options.hpp:138-321)
+    and the library's defaults of its own knobs, filled without loading the
+    library: the same values bmg_options_default() writes (a CPU test checks
+    them field by field), for callers that drive only the oracle."""
+    o = Options()
+    o.sampler_type = 0
+    o.max_move_size = 20
+    o.max_SNP_neighborhood_size = 10
+    o.p_move_size = o.p_move_size_nbs = o.p_move_size_nbc = 0.2
+    o.adapt_p_move_size = 1
+    o.p_move_size_acpt_goal = 0.0
+    o.basename = b"chain"
+    o.n_chains = 1
+    for t in range(5):
+        o.types_prior[t] = 1.0
+    o.max_model_size = 1024
+    o.scan_limbs = 6
+    o.scan_impl = SCAN_TCGEN05
+    o.proposal = PROPOSAL_ADAPTIVE
+    o.graph_iters = 64
+    o.learned_mix = 0.3
+    o.learned_topk = 1024
+    o.learned_every = 10
+    o.learned_steps = 4
+    o.learned_lr = 1e-3
+    return o
+
+
+def set_seeds(opt, seeds):
+    """Point opt.seeds at a new array of the given seeds (kept alive with the struct)."""
+    arr = (C.c_uint32 * len(seeds))(*[int(s) for s in seeds])
+    opt.seeds = C.cast(arr, C.POINTER(C.c_uint32))
+    opt.n_chains = len(seeds)
+    opt._seeds = arr
+    return opt
+
+
 def bind_common(lib):
     """Argument types of the entry points that need no device."""
     lib.bmg_options_default.argtypes = [C.POINTER(Options)]

@@ -41,7 +41,8 @@ extern "C" __global__ void bmg_pre_kernel(const int32_t* cnt, uint64_t p, uint32
 extern "C" __global__ void bmg_gsum_kernel(const uint8_t* geno, uint64_t n, uint64_t p, uint32_t gs,
                                            const int64_t* yint, const int64_t* eint, uint32_t nv, int64_t* gsum);
 extern "C" __global__ void bmg_init_kernel(DevConst K);
-extern "C" __global__ void bmg_rbprep_kernel(DevConst K);
+extern "C" __global__ void bmg_rbprep_kernel(DevConst K, int from_yhat, double yhat_absmax);
+extern "C" __global__ void bmg_set_sigma2_kernel(DevConst K, double sigma2);
 extern "C" __global__ void bmg_move_kernel(DevConst K, int max_iters);
 extern "C" __global__ void bmg_scan_simt_kernel(DevConst K, const int64_t* resid_t);
 extern "C" __global__ void bmg_resid_transpose_kernel(DevConst K, int64_t* resid_t);
@@ -143,6 +144,8 @@ struct bmg_ctx {
   std::vector<Segment> graph_segs;             // ... and its segment pattern
   uint64_t graph_launches = 0;                 // kernels in the captured chunk
   double* lml_buf = nullptr;                   // per-SNP log odds of the scans (bmg_scan_logodds, learned proposal)
+  double* yhat_given = nullptr;                // chains x n fitted values of bmg_scan_yhat
+  uint32_t wait_limit = 0;                     // main-loop wait bound of the tensor-core scan (0: default)
   int32_t* adam_t = nullptr;                   // learned proposal: optimiser step counter (device)
   uint64_t rb_steps = 0;                       // RB steps issued by bmg_run
   double* schur_out = nullptr;                 // bmg_scan_schur output on the device
@@ -302,8 +305,10 @@ static void device_error_check(bmg_ctx* ctx)
 
 // ---------------------------------------------------------------- create
 
-// message of the last failed bmg_create on this thread (no context holds it)
+// message of the last failed call without a context on this thread
 static thread_local std::string g_create_error;
+
+void bmg_host::set_thread_error(const std::string& msg) { g_create_error = msg; }
 
 extern "C" bmg_status bmg_create(const bmg_options* opt, bmg_ctx** out)
 {
@@ -354,6 +359,10 @@ extern "C" bmg_status bmg_create(const bmg_options* opt, bmg_ctx** out)
     c->sync_check = sc && sc[0] && sc[0] != '0';
     const char* eg = std::getenv("BMG_EAGER");
     c->eager = eg && eg[0] && eg[0] != '0';
+    // BMG_WAIT_LIMIT=<polls>: a shorter bound on the tensor-core scan's
+    // main-loop waits (a test makes them run out and checks BMG_ETIMEOUT)
+    const char* wl = std::getenv("BMG_WAIT_LIMIT");
+    if (wl && wl[0]) c->wait_limit = (uint32_t)std::max(1L, std::atol(wl));
     const char* sv = std::getenv("BMG_SCAN_VARIANT");
     if (sv && sv[0]) c->tc_forced = std::max(0, std::min(bmg_scan_tc_variants() - 1, std::atoi(sv)));
     c->ch_h.resize(c->C);
@@ -1028,6 +1037,7 @@ extern "C" bmg_status bmg_precompute(bmg_ctx* ctx)
   CK(cudaMemsetAsync(K.model_inds, 0xff, 4 * pc, ctx->stream));
   K.n_pad = ctx->n_pad;
   K.limbs_n = ctx->L;
+  K.wait_limit = ctx->wait_limit;
   K.resid = ctx->dalloc<int64_t>((size_t)C * ctx->n_pad);
   K.yhat = ctx->dalloc<double>((size_t)C * n);
   K.limbs = ctx->dalloc<uint16_t>((size_t)C * ctx->L * ctx->n_pad);
@@ -1484,13 +1494,55 @@ extern "C" bmg_status bmg_scan(bmg_ctx* ctx, double* p_r, double* p_r_types)
   API_BEGIN
   check_ready(ctx);
   DevConst& K = ctx->K;
-  bmg_rbprep_kernel<<<ctx->C, BMG_MOVE_THREADS, ctx->move_smem, ctx->stream>>>(K);
+  bmg_rbprep_kernel<<<ctx->C, BMG_MOVE_THREADS, ctx->move_smem, ctx->stream>>>(K, 0, 0.0);
   LAUNCHED(ctx, "bmg_rbprep_kernel");
   launch_scan(ctx);
   const size_t pc = (size_t)ctx->p * ctx->C;
   if (p_r) CK(cudaMemcpyAsync(p_r, K.p_r, 8 * pc, cudaMemcpyDeviceToHost, ctx->stream));
   if (p_r_types && ctx->opt.n_types > 1)
     CK(cudaMemcpyAsync(p_r_types, K.p_r_types, 8 * pc * ctx->opt.n_types, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  device_error_check(ctx);
+  return BMG_OK;
+  API_END
+}
+
+extern "C" bmg_status bmg_scan_yhat(bmg_ctx* ctx, const double* y_hat, double sigma2, double* p_r,
+                                    double* logodds)
+{
+  if (!ctx || !y_hat) return BMG_EINVAL;
+  API_BEGIN
+  check_ready(ctx);
+  if (!(sigma2 > 0) || !std::isfinite(sigma2)) throw bmg_error(BMG_EINVAL, "sigma2 must be positive and finite");
+  DevConst& K = ctx->K;
+  const size_t pc = (size_t)ctx->p * ctx->C;
+  double amax = 0;
+  for (uint64_t i = 0; i < ctx->n; ++i) {
+    if (!std::isfinite(y_hat[i])) throw bmg_error(BMG_EINVAL, "y_hat must be finite");
+    amax = std::max(amax, std::fabs(y_hat[i]));
+  }
+  if (!ctx->yhat_given) ctx->yhat_given = ctx->dalloc<double>((size_t)ctx->n * ctx->C, false);
+  for (uint32_t c = 0; c < ctx->C; ++c)
+    CK(cudaMemcpyAsync(ctx->yhat_given + (size_t)c * ctx->n, y_hat, 8 * ctx->n, cudaMemcpyHostToDevice,
+                       ctx->stream));
+  if (logodds && !ctx->lml_buf) ctx->lml_buf = ctx->dalloc<double>(pc, false);
+  bmg_set_sigma2_kernel<<<(ctx->C + 127) / 128, 128, 0, ctx->stream>>>(K, sigma2);
+  LAUNCHED(ctx, "bmg_set_sigma2_kernel");
+  DevConst Ky = K;
+  Ky.yhat = ctx->yhat_given;
+  bmg_rbprep_kernel<<<ctx->C, BMG_MOVE_THREADS, ctx->move_smem, ctx->stream>>>(Ky, 1, amax);
+  LAUNCHED(ctx, "bmg_rbprep_kernel");
+  double* const before = K.p_lml;
+  if (logodds) K.p_lml = ctx->lml_buf;
+  try {
+    launch_scan(ctx);
+  } catch (...) {
+    K.p_lml = before;
+    throw;
+  }
+  K.p_lml = before;
+  if (p_r) CK(cudaMemcpyAsync(p_r, K.p_r, 8 * pc, cudaMemcpyDeviceToHost, ctx->stream));
+  if (logodds) CK(cudaMemcpyAsync(logodds, ctx->lml_buf, 8 * pc, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   device_error_check(ctx);
   return BMG_OK;
@@ -1508,7 +1560,7 @@ extern "C" bmg_status bmg_scan_logodds(bmg_ctx* ctx, double* logodds)
   double* const before = K.p_lml;
   K.p_lml = ctx->lml_buf;
   try {
-    bmg_rbprep_kernel<<<ctx->C, BMG_MOVE_THREADS, ctx->move_smem, ctx->stream>>>(K);
+    bmg_rbprep_kernel<<<ctx->C, BMG_MOVE_THREADS, ctx->move_smem, ctx->stream>>>(K, 0, 0.0);
     LAUNCHED(ctx, "bmg_rbprep_kernel");
     launch_scan(ctx);
   } catch (...) {

@@ -15,6 +15,11 @@ struct bmg_error : public std::runtime_error {
   bmg_error(bmg_status s, const std::string& msg) : std::runtime_error(msg), status(s) {}
 };
 
+// Message returned by bmg_last_error(NULL) on the calling thread: set by the
+// entry points that fail without a context (bmg_create,
+// bmg_precompute_noalloc).
+void set_thread_error(const std::string& msg);
+
 }  // namespace bmg_host
 
 #endif

@@ -12,13 +12,16 @@
 // process exits.  Every call shares it, so two calls that overlap on the GPU
 // (different streams, or different host threads on one device) race on it;
 // calls on one stream, one after another, are safe.
+#include <atomic>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <string>
 
 #include <cuda_runtime.h>
 
 #include "bmg.h"
+#include "bmg_internal.h"
 
 // per SNP: #heterozygous, #homozygous-alternate, #missing after the recode
 #define BMG_NOALLOC_MAX_SNPS (1u << 20)
@@ -28,7 +31,15 @@ static __device__ __align__(256) int32_t g_noalloc_counts[3 * BMG_NOALLOC_MAX_SN
 namespace {
 
 constexpr int kMaxDevices = 64;
-int32_t* g_counts_addr[kMaxDevices] = {nullptr};
+// device address of the working array, per device; host threads that make
+// their first call at the same time look it up twice and store the same value
+std::atomic<int32_t*> g_counts_addr[kMaxDevices];
+
+bmg_status fail(bmg_status st, const char* msg)
+{
+  bmg_host::set_thread_error(std::string("bmg_precompute_noalloc: ") + msg);
+  return st;
+}
 
 // one warp per SNP; rows have the PLINK stride ceil(n/4) and need no padding
 __global__ void noalloc_count_kernel(const uint8_t* packed, uint64_t n, uint64_t p, int recode,
@@ -93,13 +104,16 @@ extern "C" bmg_status bmg_precompute_noalloc(const uint8_t* d_packed, uint64_t n
                                              const int32_t* types, uint32_t n_types, double* d_out,
                                              uint32_t* offset_out, int32_t* d_flag, void* stream)
 {
-  if (!d_packed || !types || !d_out || !d_flag || n == 0 || p == 0 || n_types == 0 || n_types > 5)
-    return BMG_EINVAL;
-  if (p > BMG_NOALLOC_MAX_SNPS) return BMG_EINVAL;  // more SNPs than the fixed working array holds
+  if (!d_packed || !types || !d_out || !d_flag) return fail(BMG_EINVAL, "null argument");
+  if (n == 0 || p == 0 || n_types == 0 || n_types > 5) return fail(BMG_EINVAL, "n, p and n_types (1..5) must be positive");
+  // more SNPs than the fixed working array holds
+  if (p > BMG_NOALLOC_MAX_SNPS) return fail(BMG_EINVAL, "p above 2^20 SNPs, the size of the working array");
+  // the per-SNP counts are 32-bit
+  if (n > 0x7FFFFFFFull) return fail(BMG_EINVAL, "n above 2^31 - 1 individuals");
   int allow_types[5] = {0, 0, 0, 0, 0};
   int allow_mask = 0;
   for (uint32_t t = 0; t < n_types; ++t) {
-    if (types[t] < 0 || types[t] > 4) return BMG_EINVAL;
+    if (types[t] < 0 || types[t] > 4) return fail(BMG_EINVAL, "effect type outside 0..4");
     allow_types[types[t]] = 1;
     if (types[t] == BMG_TYPE_AH) allow_mask |= 3;
     else allow_mask |= 1 << types[t];
@@ -108,18 +122,21 @@ extern "C" bmg_status bmg_precompute_noalloc(const uint8_t* d_packed, uint64_t n
   const int offset = 2 * (int)n_types + (ah ? 1 : 0) * (1 + ((a && h) ? -2 : 0) + ((a || h) ? 0 : 2));
   if (offset_out) *offset_out = (uint32_t)offset;
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return BMG_ECUDA;
-  if (!g_counts_addr[dev]) {
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return fail(BMG_ECUDA, "no current device");
+  int32_t* counts = g_counts_addr[dev].load(std::memory_order_acquire);
+  if (!counts) {
     // once per device, with that device current: the device address of the
     // working array (its host-side name is not a device address)
     void* addr = nullptr;
-    if (cudaGetSymbolAddress(&addr, g_noalloc_counts) != cudaSuccess) return BMG_ECUDA;
-    g_counts_addr[dev] = static_cast<int32_t*>(addr);
+    if (cudaGetSymbolAddress(&addr, g_noalloc_counts) != cudaSuccess)
+      return fail(BMG_ECUDA, "cudaGetSymbolAddress of the working array failed");
+    counts = static_cast<int32_t*>(addr);
+    g_counts_addr[dev].store(counts, std::memory_order_release);
   }
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  if (cudaMemsetAsync(d_flag, 0, sizeof(int32_t), s) != cudaSuccess) return BMG_ECUDA;
+  if (cudaMemsetAsync(d_flag, 0, sizeof(int32_t), s) != cudaSuccess) return fail(BMG_ECUDA, "cudaMemsetAsync failed");
   unsigned blocks = (unsigned)((p + 7) / 8 < 152 * 16 ? (p + 7) / 8 : 152 * 16);
-  noalloc_count_kernel<<<blocks, 256, 0, s>>>(d_packed, n, p, recode, g_counts_addr[dev]);
-  noalloc_pre_kernel<<<blocks, 256, 0, s>>>(g_counts_addr[dev], n, p, allow_mask, ah, offset, d_out, d_flag);
-  return cudaGetLastError() == cudaSuccess ? BMG_OK : BMG_ECUDA;
+  noalloc_count_kernel<<<blocks, 256, 0, s>>>(d_packed, n, p, recode, counts);
+  noalloc_pre_kernel<<<blocks, 256, 0, s>>>(counts, n, p, allow_mask, ah, offset, d_out, d_flag);
+  return cudaGetLastError() == cudaSuccess ? BMG_OK : fail(BMG_ECUDA, "kernel launch failed");
 }

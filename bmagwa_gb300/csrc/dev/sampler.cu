@@ -32,6 +32,50 @@
 
 #define LOG_HALF_D -0.69314718055994528622676398299518041312694549560546875
 
+// Phase probes of the move kernel, compiled in only with -DBMG_MOVE_PROF (a
+// profiling build; the library itself is built without them): thread 0 of
+// chain c adds the SM cycles of each phase to g_move_prof[c][slot] and counts
+// its entries in g_move_prof[c][32 + slot].
+#ifdef BMG_MOVE_PROF
+#define PROF_CHAINS 256
+enum {
+  PF_ITER, PF_MOVE, PF_BETA, PF_BULK, PF_NS, PF_RB, PF_ADD, PF_XX, PF_TRSV, PF_REM, PF_DCHEX, PF_REMSOLVE,
+  PF_COPY, PF_ASAMP, PF_RSAMP, PF_FLIP, PF_ACCEPT, PF_ADAPT, PF_REBUILD, PF_LIK, PF_BACKQ, PF_PREPQ, PF_NSLOTS
+};
+__device__ unsigned long long g_move_prof[PROF_CHAINS][64];
+struct ProfScope {
+  int slot;
+  long long t0;
+  __device__ explicit ProfScope(int s) : slot(s), t0(0)
+  {
+#ifdef __CUDA_ARCH__
+    t0 = clock64();
+#endif
+  }
+  __device__ ~ProfScope()
+  {
+#ifdef __CUDA_ARCH__
+    if (threadIdx.x == 0 && blockIdx.x < PROF_CHAINS) {
+      g_move_prof[blockIdx.x][slot] += (unsigned long long)(clock64() - t0);
+      g_move_prof[blockIdx.x][32 + slot] += 1ull;
+    }
+#endif
+  }
+};
+#define PROF_SCOPE(slot) ProfScope prof_scope_(slot)
+extern "C" cudaError_t bmg_move_prof_read(unsigned long long* host, int chains)
+{
+  return cudaMemcpyFromSymbol(host, g_move_prof, sizeof(unsigned long long) * 64 * (chains < PROF_CHAINS ? chains : PROF_CHAINS));
+}
+extern "C" cudaError_t bmg_move_prof_reset()
+{
+  static unsigned long long zero[PROF_CHAINS][64];
+  return cudaMemcpyToSymbol(g_move_prof, zero, sizeof(zero));
+}
+#else
+#define PROF_SCOPE(slot)
+#endif
+
 // Cholesky factors and v of both models stay in shared memory while their
 // order is at most SMK; larger models live in global memory (same packed
 // upper-triangular layout: column c holds rows 0..c at c (c + 1) / 2).
@@ -79,6 +123,7 @@ struct MoveShared {
   double bulk_b0;       // constant-term coefficient
   long long bulk_b0i;
   double bulk_e[8];     // covariate coefficients (m_e <= 8 in bulk phases)
+  double yhat_given_max;  // max |y_hat| of a residual from given fitted values (BULK_YHAT)
 };
 
 // genotype columns of the bulk phase: snp, term, fixed-point coefficient
@@ -244,6 +289,7 @@ struct Warp {
   /* src/model.hpp:115-162: copy the active parts of a model */
   __device__ void copy_model(DevModel* d, const DevModel* src)
   {
+    PROF_SCOPE(PF_COPY);
     int xc = src->xcols, ll = src->llen;
     if (ll > SMK || src->vlen > SMK) spill(d);
     for (int col = 0; col < xc; ++col)
@@ -297,6 +343,7 @@ struct Warp {
   // solve U' x = b in place (forward substitution), U = first len of L
   __device__ void trsv_T(const DevModel* M, double* x, int len)
   {
+    PROF_SCOPE(PF_TRSV);
     const double* lb = Lb(M);
     for (int j = 0; j < len; ++j) {
       const double* colj = lb + TRI(0, j);
@@ -335,6 +382,7 @@ struct Warp {
   /* src/model.hpp:199-237, src/model.hpp:558-576 (Cholesky: LAPACK dpotf2, 'U') */
   __device__ void compute_log_likelihood(DevModel* M)
   {
+    PROF_SCOPE(PF_LIK);
     int m = M->xcols;
     if (m < 1) {
       if (lane == 0) M->ll = NAN;
@@ -466,6 +514,7 @@ struct Warp {
   // four rows' loads are independent.  Exact integer popcounts.
   __device__ void cross_cols(const DevModel* M, int r0, int r1, uint32_t snp, int term, double* out)
   {
+    PROF_SCOPE(PF_XX);
     const uint64_t* rb = (const uint64_t*)(K.geno + (size_t)snp * K.gs);
     const unsigned nw64 = K.gs / 8;
     const uint64_t m5 = 0x5555555555555555ull;
@@ -517,6 +566,7 @@ struct Warp {
   /* src/model.hpp:432-506 with src/symmmatrix.cpp:144-164 */
   __device__ void upd_add(DevModel* M, uint32_t snp, int mi, int term, bool is2, double invv, bool update)
   {
+    PROF_SCOPE(PF_ADD);
     int col = M->xcols;
     if (col + 1 > SMK) spill(M);
     if (lane == 0) {
@@ -622,6 +672,7 @@ struct Warp {
   /* src/dchex.f:130-220 (job 2) on L with k = x_ind + 1, l = p = order */
   __device__ void dchex_left(DevModel* M, int x_ind, int order, double* cs, double* sn)
   {
+    PROF_SCOPE(PF_DCHEX);
     // one lane: the rotation chain is sequential
     if (order <= SMK) { cs = s.cs; sn = s.sn; }
     if (lane == 0) {
@@ -675,6 +726,7 @@ struct Warp {
   /* src/model.hpp:508-556 with src/symmmatrix.cpp:126-195 */
   __device__ void upd_rem(DevModel* M, int x_ind, double* cs, double* sn)
   {
+    PROF_SCOPE(PF_REM);
     int len = M->xcols;
     double invv = M->inv[x_ind];
     __syncwarp();
@@ -921,6 +973,7 @@ struct Warp {
   // dd_add zero state toggles (src/discrete_distribution.hpp:156-199)
   __device__ void add_set_zero(uint32_t snp, bool zero)
   {
+    PROF_SCOPE(PF_FLIP);
     int at;
     bool in_list = pend_find(snp, &at);
     bool zeroed = base_zero(snp) != in_list;
@@ -1036,6 +1089,7 @@ struct Warp {
   /* src/discrete_distribution.hpp:125-153 on the in-order prefix */
   __device__ uint32_t add_sample()
   {
+    PROF_SCOPE(PF_ASAMP);
     long long totali = add_total_int();
     double total = (double)totali * ldexp(1.0, -K.qs);
     double r = u01() * total;
@@ -1128,6 +1182,7 @@ struct Warp {
   }
   __device__ uint32_t rs_sample()
   {
+    PROF_SCOPE(PF_RSAMP);
     double total = rs_total();
     double r = u01() * total;
     double acc = 0;
@@ -1156,6 +1211,7 @@ struct Warp {
   // commit the proposed model as the current one (Model::operator=)
   __device__ void accept_model()
   {
+    PROF_SCOPE(PF_ACCEPT);
     // membership map of the current model: clear old, set new
     int32_t* mi = K.model_inds + (size_t)c * K.p;
     uint32_t* ib = K.inbits + (size_t)c * ((K.p + 31) / 32);
@@ -1177,6 +1233,7 @@ struct Warp {
   /* src/sampler.hpp:1126-1165 */
   __device__ int prepare_addrem(double& lqf, int ms)
   {
+    PROF_SCOPE(PF_PREPQ);
     long long max_adds = (long long)K.p - cur->k, max_rems = cur->k;
     int nrem = 0;
     for (int i = 0; i < ms; ++i) {
@@ -1260,6 +1317,7 @@ struct Warp {
   /* src/sampler.hpp:1168-1202 */
   __device__ void backward_prepare_addrem(double& lqb, int ms)
   {
+    PROF_SCOPE(PF_BACKQ);
     long long max_adds = (long long)K.p - nm->k, max_rems = nm->k;
     double w_add = add_total(), w_rem = rs_total();
     long long wmb = s.w_m;
@@ -1523,6 +1581,7 @@ struct Warp {
   /* src/sampler.hpp:1715-1769 */
   __device__ void adapt_move_size()
   {
+    PROF_SCOPE(PF_ADAPT);
     double* q_p0 = K.q_p0_ms + (size_t)c * 256;
     const double* rs = K.r_ms_sum + (size_t)c * 256;
     const double* rn = K.r_ms_n + (size_t)c * 256;
@@ -1600,6 +1659,7 @@ struct Warp {
 #define BULK_PVE 1
 #define BULK_ALPHA 2
 #define BULK_RESID 4
+#define BULK_YHAT 8   // with BULK_RESID: the residual is y - K.yhat, the fitted values given
 
 __device__ void bulk_phase(const DevConst& K, int c, MoveShared& s, BulkCols& bc)
 {
@@ -1615,7 +1675,7 @@ __device__ void bulk_phase(const DevConst& K, int c, MoveShared& s, BulkCols& bc
   // adding E beta_E when the model has no genotype term and there are
   // covariates, so y_hat then accumulates; the scan reads that y_hat
   // (src/sampler.cpp:735).  The same update is reproduced here.
-  const bool stale = (nt == 0) && (me > 1);
+  const bool stale = (mode & BULK_YHAT) || ((nt == 0) && (me > 1));
   double* yhat = K.yhat + (size_t)c * K.n;
   const int dsh = P.sy - sh;
   // a thread takes 16 individuals at a time: one 32-bit word of every model
@@ -1745,7 +1805,7 @@ __device__ void bulk_setup(Warp& W, BulkCols& bc, int mode)
   const DevConst& K = W.K;
   int me = K.m_e, bl = M->blen, xc = M->xcols;
   int nt = min(bl, xc) - me;
-  if (nt < 0) nt = 0;
+  if (nt < 0 || (mode & BULK_YHAT)) nt = 0;
   double bound = 0;
   for (int j = 0; j < nt; ++j) bound += 2.0 * fabs(M->beta[me + j]);
   int sh;
@@ -1755,7 +1815,8 @@ __device__ void bulk_setup(Warp& W, BulkCols& bc, int mode)
     double eb = 0;
     for (int e = 0; e < me && e < bl; ++e) eb += K.e_absmax[e] * fabs(M->beta[e]);
     double tot = bound + W.P.y_absmax + eb + 1e-300;
-    if (nt == 0 && me > 1) tot += W.ch->yhat_absmax;  // the accumulated y_hat
+    if (mode & BULK_YHAT) tot = W.P.y_absmax + W.s.yhat_given_max + 1e-300;
+    else if (nt == 0 && me > 1) tot += W.ch->yhat_absmax;  // the accumulated y_hat
     int e2 = (int)ceil(log2(tot));
     sh = (int)(8 * K.limbs_n - 3) - e2;
   } else {
@@ -1786,6 +1847,7 @@ __device__ void bulk_setup(Warp& W, BulkCols& bc, int mode)
    With scan_only the flags ask for p_r only and no counter moves. */
 __device__ void prep_rb(Warp& W, bool scan_only)
 {
+  PROF_SCOPE(PF_RB);
   const DevConst& K = W.K;
   DevChain* ch = W.ch;
   RbParams* rp = K.rb + W.c;
@@ -1974,18 +2036,23 @@ bmg_init_kernel(DevConst K)
 }
 
 // Residual limbs and RbParams of every chain at its current beta, for a scan
-// requested outside the MCMC loop (bmg_scan).
+// requested outside the MCMC loop (bmg_scan).  With from_yhat the residual is
+// y - K.yhat instead (K.yhat then holds the caller's fitted values for each
+// chain, yhat_absmax their largest magnitude; bmg_scan_yhat).
 extern "C" __global__ void __launch_bounds__(BMG_MOVE_THREADS, 1)
-bmg_rbprep_kernel(DevConst K)
+bmg_rbprep_kernel(DevConst K, int from_yhat, double yhat_absmax)
 {
   MoveShared& s = move_smem().s;
   BulkCols& bc = move_smem().bc;
   const int c = blockIdx.x, tid = threadIdx.x;
   load_state(K, c, s);
-  if (tid == 0) s.err = 0;
+  if (tid == 0) {
+    s.err = 0;
+    s.yhat_given_max = yhat_absmax;
+  }
   __syncthreads();
   Warp W(K, c, s);
-  if (tid < 32) bulk_setup(W, bc, BULK_RESID);
+  if (tid < 32) bulk_setup(W, bc, BULK_RESID | (from_yhat ? BULK_YHAT : 0));
   __syncthreads();
   bulk_phase(K, c, s, bc);
   if (tid < 32) {
@@ -1993,6 +2060,13 @@ bmg_rbprep_kernel(DevConst K)
     if (W.lane == 0) s.chs.rng = W.rng;
   }
   store_state(K, c, s);
+}
+
+// Every chain's current sigma2 (bmg_scan_yhat)
+extern "C" __global__ void bmg_set_sigma2_kernel(DevConst K, double sigma2)
+{
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < K.n_chains) K.cur[c].sigma2 = sigma2;
 }
 
 // Runs iterations of chain blockIdx.x until `max_iters` are done or an RB
@@ -2049,8 +2123,10 @@ bmg_move_kernel(DevConst K, int max_iters)
   for (int it = 0; it < max_iters; ++it) {
     __syncthreads();
     if (s.err || s.iter_stop) break;
+    PROF_SCOPE(PF_ITER);
     // room for one more move's flips of dd_add, else rebuild its prefix here
     if (s.n_pend > BMG_PEND_MAX - 2 * (int)K.max_move_size - 2) {
+      PROF_SCOPE(PF_REBUILD);
       if (tid == 0) ch->n_pend = 0;
       rebuild_chain(K, c, part, ch);
       if (tid == 0) s.n_pend = 0;
@@ -2061,6 +2137,7 @@ bmg_move_kernel(DevConst K, int max_iters)
     const bool thin_step = ((iter + 1) % K.thin) == 0;
     const bool rb_step = ((iter + 1) % K.n_rao) == 0;
     if (ns_step) {
+      PROF_SCOPE(PF_NS);
       /* src/sampler.cpp:628-635 */
       if (tid < 32) bulk_setup(W, bc, BULK_ALPHA);
       __syncthreads();
@@ -2084,6 +2161,9 @@ bmg_move_kernel(DevConst K, int max_iters)
       for (int i = 1; i < 7; ++i) pcs[i] = pcs[i - 1] + pm[i];
       int move = W.sample_naive(pcs, 7);
       int jd = 0;
+#ifdef BMG_MOVE_PROF
+      ProfScope move_scope(PF_MOVE);
+#endif
       switch (move) {
         case 0: jd = W.do_addrem_move(cs_buf, sn_buf); break;
         case 1:
@@ -2122,6 +2202,7 @@ bmg_move_kernel(DevConst K, int max_iters)
     }
     __syncthreads();
     if (thin_step) {
+      PROF_SCOPE(PF_BULK);
       bulk_phase(K, c, s, bc);
       if (tid < 32) {
         /* src/sampler.cpp:691-727, src/model.hpp:345-392 */

@@ -77,7 +77,7 @@ bmg_scan_tc_kernel(DevConst K, TcParams P, const __grid_constant__ CUtensorMap m
       // the same number of named-barrier steps
       if (e == 0) {
         bool ok = false;
-        if (lane == 0) ok = !ctl.abort_flag && mbar_wait(&ctl.acc_full[b], u & 1);
+        if (lane == 0) ok = !ctl.abort_flag && mbar_wait(&ctl.acc_full[b], u & 1, P.wait_limit);
         ok = __shfl_sync(0xffffffffu, ok, 0);
         if (lane == 0) {
           epi_ok = ok;
@@ -187,6 +187,7 @@ static bool tc_plan(const DevConst* K, TcParams* P, uint32_t ct_cap, uint32_t n_
   for (uint32_t u = 0; u < 4; ++u) P->term_of_row[u] = (u < T) ? K->term_of[u] : -1;
   const uint32_t L = K->limbs_n;
   if (K->n_pad % TC_BK != 0 || K->n >= 65536) return false;  // exact FP32 sums need n < 2^16
+  P->wait_limit = K->wait_limit;
   P->k_chunks = K->n_pad / TC_BK;
   P->pk_bytes = P->snps_per_tile * (TC_BK / 4);
   // widest chain tile whose accumulator fits one TMEM buffer and whose stages

@@ -129,7 +129,7 @@ bmg_schur_tc_kernel(DevConst K, TcParams P, uint32_t KB, uint32_t n_terms, doubl
       const uint32_t b = i % P.n_acc, u = i / P.n_acc;
       if (e == 0) {
         bool ok = false;
-        if (lane == 0) ok = !ctl.abort_flag && mbar_wait(&ctl.acc_full[b], u & 1);
+        if (lane == 0) ok = !ctl.abort_flag && mbar_wait(&ctl.acc_full[b], u & 1, P.wait_limit);
         ok = __shfl_sync(0xffffffffu, ok, 0);
         if (lane == 0) {
           epi_ok = ok;

@@ -304,6 +304,7 @@ struct DevConst {
   uint16_t* limbs;      // (chains * L) x n_pad bf16 residual limbs (scan B operand)
   uint32_t n_pad;       // individuals padded to the scan's K multiple
   uint32_t limbs_n;     // L
+  uint32_t wait_limit;  // polls of a main-loop mbarrier wait of the tensor-core scan (0: the default)
   DevTrace tr;
 };
 

@@ -46,10 +46,14 @@ __device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity)
   return ok != 0;
 }
 
-// bounded wait: false after WAIT_LIMIT polls
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity)
+// bounded wait: false after `limit` polls (0: WAIT_LIMIT).  The main loops
+// take their limit from the launch (a shorter one makes a test's wait run
+// out); the waits that drain a CTA's own asynchronous copies and MMAs before
+// it frees tensor memory and exits always use WAIT_LIMIT.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit = WAIT_LIMIT)
 {
-  for (uint32_t it = 0; it < WAIT_LIMIT; ++it)
+  if (limit == 0) limit = WAIT_LIMIT;
+  for (uint32_t it = 0; it < limit; ++it)
     if (mbar_try(bar, parity)) return true;
   return false;
 }

@@ -70,6 +70,7 @@ struct TcParams {
   uint32_t acc_cols;       // TMEM column stride of the accumulators
   uint32_t a_tmem;         // 1: A slot t at TMEM column n_acc acc_cols + t TC_A_COLS
   int32_t term_of_row[4];  // term of row u of a SNP (-1: unused)
+  uint32_t wait_limit = 0;  // polls of a main-loop mbarrier wait (0: WAIT_LIMIT)
 };
 
 // Where the accumulators and A go: A in TMEM when n_acc accumulators of n_mma
@@ -175,7 +176,7 @@ __device__ __forceinline__ void tc_main_roles(const TcParams& P, TcCtl& ctl, uin
         bool ok = true;
         for (uint32_t k = 0; k < nk; ++k) {
           if (issued >= S) {  // the slot's last reader is the MMA of stage g - S
-            if (!mbar_wait(&done_bar[done.i], done.ph)) { ok = false; break; }
+            if (!mbar_wait(&done_bar[done.i], done.ph, P.wait_limit)) { ok = false; break; }
             done.next(R);
           }
           uint8_t* sp = smem + slot.i * P.stage_bytes;
@@ -203,12 +204,13 @@ __device__ __forceinline__ void tc_main_roles(const TcParams& P, TcCtl& ctl, uin
       uint32_t dn = 0;     // done_bar slot of this stage
       for (uint32_t i = 0; i < my_tiles && !ctl.abort_flag; ++i) {
         const uint32_t b = i % P.n_acc, u = i / P.n_acc;
-        if (u >= 1 && !mbar_wait(&ctl.acc_empty[b], (u - 1) & 1)) { ctl.abort_flag = 1; break; }
+        if (u >= 1 && !mbar_wait(&ctl.acc_empty[b], (u - 1) & 1, P.wait_limit)) { ctl.abort_flag = 1; break; }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t d = tmem + b * P.acc_cols;
         bool ok = true;
         for (uint32_t k = 0; k < nk; ++k) {
-          if (!mbar_wait(&full_bar[full.i], full.ph) || !mbar_wait(&aready_bar[aslot.i], aslot.ph)) {
+          if (!mbar_wait(&full_bar[full.i], full.ph, P.wait_limit) ||
+              !mbar_wait(&aready_bar[aslot.i], aslot.ph, P.wait_limit)) {
             ok = false;
             break;
           }
@@ -259,8 +261,8 @@ __device__ __forceinline__ void tc_main_roles(const TcParams& P, TcCtl& ctl, uin
       const bool need_slot = P.a_tmem && g >= SA;
       bool ok = false;
       if (lane == 0)
-        ok = !ctl.abort_flag && mbar_wait(&full_bar[full.i], full.ph) &&
-             (!need_slot || mbar_wait(&done_bar[done.i], done.ph));
+        ok = !ctl.abort_flag && mbar_wait(&full_bar[full.i], full.ph, P.wait_limit) &&
+             (!need_slot || mbar_wait(&done_bar[done.i], done.ph, P.wait_limit));
       ok = __shfl_sync(0xffffffffu, ok, 0);
       __syncwarp();
       if (!ok) {

@@ -221,6 +221,15 @@ bmg_status bmg_scan(bmg_ctx* ctx, double* p_r, double* p_r_types);
  * oracle is the one the parity tests bound. */
 bmg_status bmg_scan_logodds(bmg_ctx* ctx, double* logodds);
 
+/* The Rao-Blackwellised scan of every chain against fitted values the caller
+ * gives instead of the model's (no counterpart entry point in the reference:
+ * RaoBlackwellizer::p_raoblackwell, src/sampler.cpp:32-261, called with this
+ * y_hat and sigma2; a parity aid).  y_hat: n doubles, the same for every
+ * chain.  Every chain's current sigma2 is set to sigma2 (> 0) and stays so.
+ * p_r and logodds (either may be NULL) receive chains x m_g values as
+ * bmg_scan and bmg_scan_logodds write them. */
+bmg_status bmg_scan_yhat(bmg_ctx* ctx, const double* y_hat, double sigma2, double* p_r, double* logodds);
+
 /* The exact change of every chain's log marginal likelihood from adding each
  * single term of each SNP outside its model (no counterpart entry point in
  * the reference: Model::update_likelihood_on_add, src/model.hpp:432-506,
@@ -333,16 +342,18 @@ bmg_status bmg_get_scan_shape_name(int32_t shape, char* name, size_t name_len);
  * count as 0, as in the reference's precomputation).  `stream` is a
  * cudaStream_t or NULL.  Working memory is a fixed array inside the library
  * of 3 x 2^20 int32 (12 MB per device, kept until the process exits); p above
- * 2^20 returns BMG_EINVAL.  The first call on each device looks up that
- * array's device address, so make the first call before capturing a stream.
- * Calls that overlap on the GPU share the array and race; calls ordered on
- * one stream do not. */
+ * 2^20, or n above 2^31 - 1, returns BMG_EINVAL.  The first call on each
+ * device looks up that array's device address, so make the first call before
+ * capturing a stream.  Calls that overlap on the GPU share the array and
+ * race; calls ordered on one stream do not.  A failed call leaves its message
+ * for bmg_last_error(NULL) on the calling thread. */
 bmg_status bmg_precompute_noalloc(const uint8_t* d_packed, uint64_t n, uint64_t p, int32_t recode,
                                   const int32_t* types, uint32_t n_types, double* d_out,
                                   uint32_t* offset_out, int32_t* d_flag, void* stream);
 
 /* Message of the last failed call on ctx; with ctx NULL, the message of the
- * last failed bmg_create on the calling thread (which returns no context). */
+ * last failed call on the calling thread that has no context (bmg_create,
+ * bmg_precompute_noalloc). */
 const char* bmg_last_error(const bmg_ctx* ctx);
 const char* bmg_status_string(bmg_status s);
 void bmg_destroy(bmg_ctx* ctx);

@@ -1,7 +1,7 @@
-"""GPU parity cases added after the last GB300 run: marked non-strict xfail
-until a GPU run has passed them, so that their outcome is reported either
-way.  The file sorts last, so that a failure here cannot stop or disturb the
-GPU tests that already passed."""
+"""GPU parity against the reference's traces for the options the main parity
+file does not cover: the flat proposal with the beta trace and raw
+genotypes, a model past the 128 columns kept in shared memory, individual
+tau2 over five effect types, and the command-line entry end to end."""
 import numpy as np
 import pytest
 
@@ -11,10 +11,6 @@ from test_gpu_parity import RTOL, run_gpu
 pytestmark = pytest.mark.gpu
 
 
-NOT_YET_ON_GPU = pytest.mark.xfail(reason="not yet run on a GB300", strict=False)
-
-
-@NOT_YET_ON_GPU
 @pytest.mark.parametrize("name", ["small_flat", "example_flat", "example_large", "example_types_indiv"])
 def test_gpu_matches_reference_more_options(bmg, tmp_path, name):
     """A flat proposal with the beta trace and raw genotypes (small_flat,
@@ -36,7 +32,6 @@ def test_gpu_matches_reference_more_options(bmg, tmp_path, name):
         np.testing.assert_allclose(ctx.rao(c)[0], ref["rao"], rtol=RTOL, atol=1e-12)
 
 
-@NOT_YET_ON_GPU
 def test_cli_writes_the_reference_files(bmg, tmp_path):
     """bmagwa-gb300 INIFILE end to end: the trace files equal the reference's."""
     import os

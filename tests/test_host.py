@@ -229,6 +229,14 @@ def test_options_struct_matches_the_library():
     assert o.learned_topk == 1024 and o.learned_mix == pytest.approx(0.3)
 
 
+def test_library_free_defaults_equal_the_library_defaults():
+    """abi.default_options (used where only the oracle runs) fills every
+    field as bmg_options_default does."""
+    from bmagwa_gb300 import abi
+    a, b = abi.default_options(), bg.default_options()
+    assert C.string_at(C.addressof(a), C.sizeof(a)) == C.string_at(C.addressof(b), C.sizeof(b))
+
+
 def _option_cases():
     with open(os.path.join(os.path.dirname(__file__), "golden", "options_ref.json")) as f:
         return json.load(f)
