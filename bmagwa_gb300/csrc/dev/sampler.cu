@@ -32,50 +32,6 @@
 
 #define LOG_HALF_D -0.69314718055994528622676398299518041312694549560546875
 
-// Phase probes of the move kernel, compiled in only with -DBMG_MOVE_PROF (a
-// profiling build; the library itself is built without them): thread 0 of
-// chain c adds the SM cycles of each phase to g_move_prof[c][slot] and counts
-// its entries in g_move_prof[c][32 + slot].
-#ifdef BMG_MOVE_PROF
-#define PROF_CHAINS 256
-enum {
-  PF_ITER, PF_MOVE, PF_BETA, PF_BULK, PF_NS, PF_RB, PF_ADD, PF_XX, PF_TRSV, PF_REM, PF_DCHEX, PF_REMSOLVE,
-  PF_COPY, PF_ASAMP, PF_RSAMP, PF_FLIP, PF_ACCEPT, PF_ADAPT, PF_REBUILD, PF_LIK, PF_BACKQ, PF_PREPQ, PF_NSLOTS
-};
-__device__ unsigned long long g_move_prof[PROF_CHAINS][64];
-struct ProfScope {
-  int slot;
-  long long t0;
-  __device__ explicit ProfScope(int s) : slot(s), t0(0)
-  {
-#ifdef __CUDA_ARCH__
-    t0 = clock64();
-#endif
-  }
-  __device__ ~ProfScope()
-  {
-#ifdef __CUDA_ARCH__
-    if (threadIdx.x == 0 && blockIdx.x < PROF_CHAINS) {
-      g_move_prof[blockIdx.x][slot] += (unsigned long long)(clock64() - t0);
-      g_move_prof[blockIdx.x][32 + slot] += 1ull;
-    }
-#endif
-  }
-};
-#define PROF_SCOPE(slot) ProfScope prof_scope_(slot)
-extern "C" cudaError_t bmg_move_prof_read(unsigned long long* host, int chains)
-{
-  return cudaMemcpyFromSymbol(host, g_move_prof, sizeof(unsigned long long) * 64 * (chains < PROF_CHAINS ? chains : PROF_CHAINS));
-}
-extern "C" cudaError_t bmg_move_prof_reset()
-{
-  static unsigned long long zero[PROF_CHAINS][64];
-  return cudaMemcpyToSymbol(g_move_prof, zero, sizeof(zero));
-}
-#else
-#define PROF_SCOPE(slot)
-#endif
-
 // Cholesky factors and v of both models stay in shared memory while their
 // order is at most SMK; larger models live in global memory (same packed
 // upper-triangular layout: column c holds rows 0..c at c (c + 1) / 2).
@@ -124,6 +80,13 @@ struct MoveShared {
   long long bulk_b0i;
   double bulk_e[8];     // covariate coefficients (m_e <= 8 in bulk phases)
   double yhat_given_max;  // max |y_hat| of a residual from given fitted values (BULK_YHAT)
+  // n-wide products of warp 0's move, handed to all eight warps (help jobs)
+  int job_kind;
+  int job_r0, job_r1, job_term;
+  uint32_t job_snp;
+  const DevModel* job_M;
+  double* job_out;
+  long long job_part[BMG_MOVE_THREADS / 32];
 };
 
 // genotype columns of the bulk phase: snp, term, fixed-point coefficient
@@ -136,6 +99,108 @@ struct BulkCols {
 
 // ------------------------------------------------------------------ helpers
 
+#define HELP_BAR 1  // named barrier of warp 0 and its seven helper warps
+enum { HJ_EXIT = 0, HJ_CROSS = 1, HJ_XY = 2 };
+
+__device__ __forceinline__ void bar_sync_all()
+{
+  asm volatile("bar.sync %0, %1;" ::"r"(HELP_BAR), "r"(BMG_MOVE_THREADS) : "memory");
+}
+
+// Exact sum_i x_t(g_a,i) x_u(g_snp,i) between the new genotype column
+// (snp, term) and the model's genotype columns r0 <= r < r1, four columns at
+// a time: warp `wid` of `nwarps` takes the groups wid, wid + nwarps, ...; a
+// word of the new column is loaded once per four model columns and the four
+// rows' loads are independent.  Exact integer popcounts.
+__device__ void cross_cols_part(const DevConst& K, const DevPheno& P, const DevModel* M, int r0, int r1,
+                                uint32_t snp, int term, double* out, int wid, int nwarps)
+{
+  const int lane = threadIdx.x & 31;
+  const uint64_t* rb = (const uint64_t*)(K.geno + (size_t)snp * K.gs);
+  const unsigned nw64 = K.gs / 8;
+  const uint64_t m5 = 0x5555555555555555ull;
+  const int cHu = coefH(term), cRu = coefR(term);
+  for (int r = r0 + 4 * wid; r < r1; r += 4 * nwarps) {
+    const int cnt = min(4, r1 - r);
+    const uint64_t* ra[4];
+    int cH[4], cR[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int idx = r + min(q, cnt - 1);
+      ra[q] = (const uint64_t*)(K.geno + (size_t)M->xc_snp[idx] * K.gs);
+      cH[q] = coefH(M->xc_type[idx]);
+      cR[q] = coefR(M->xc_type[idx]);
+    }
+    int hh[4] = {0, 0, 0, 0}, hr[4] = {0, 0, 0, 0}, rh[4] = {0, 0, 0, 0}, rr[4] = {0, 0, 0, 0};
+#pragma unroll 4
+    for (unsigned w = lane; w < nw64; w += 32) {
+      const uint64_t y = rb[w];
+      const uint64_t yh = (y >> 1) & (P.mask2 ? P.mask2[w] : m5), yl = y & m5;
+      const uint64_t Hy = yh & ~yl, Ry = yh & yl;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const uint64_t x = ra[q][w];
+        const uint64_t xh = (x >> 1) & m5, xl = x & m5;
+        const uint64_t Hx = xh & ~xl, Rx = xh & xl;
+        hh[q] += __popcll(Hx & Hy);
+        hr[q] += __popcll(Hx & Ry);
+        rh[q] += __popcll(Rx & Hy);
+        rr[q] += __popcll(Rx & Ry);
+      }
+    }
+    long long v[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      v[q] = (long long)cH[q] * cHu * hh[q] + (long long)cH[q] * cRu * hr[q] +
+             (long long)cR[q] * cHu * rh[q] + (long long)cR[q] * cRu * rr[q];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) v[q] += __shfl_xor_sync(FULL_MASK, v[q], o);
+    }
+    if (lane == 0)
+      for (int q = 0; q < cnt; ++q) out[r + q] = (double)v[q];
+  }
+}
+
+// sum_i x_term(g_snp,i) yint_i over the words of thread t of nth (the
+// phenotype is zero outside the sample); the caller reduces
+__device__ long long geno_dot_part(const DevConst& K, const DevPheno& P, uint32_t snp, int term, int t, int nth)
+{
+  const uint32_t* row = reinterpret_cast<const uint32_t*>(K.geno + (size_t)snp * K.gs);
+  const long long cH = coefH(term), cR = coefR(term);
+  long long acc = 0;
+  for (uint32_t w = t; w < (uint32_t)(K.gs / 4); w += nth) {
+    const uint32_t code = row[w];
+    if (!code) continue;
+    for (int q = 0; q < 16; ++q) {
+      const uint32_t c2 = (code >> (2 * q)) & 3u;
+      if (c2 >= 2u) acc += (c2 == 2u ? cH : cR) * P.yint[(size_t)16 * w + q];
+    }
+  }
+  return acc;
+}
+
+// Warps 1-7 while warp 0 runs a move: wait for a job, do this warp's share,
+// meet again; until warp 0 posts HJ_EXIT.
+__device__ void help_loop(const DevConst& K, MoveShared& s)
+{
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (;;) {
+    bar_sync_all();
+    const int kind = s.job_kind;
+    if (kind == HJ_EXIT) break;
+    if (kind == HJ_CROSS) {
+      cross_cols_part(K, s.phs, s.job_M, s.job_r0, s.job_r1, s.job_snp, s.job_term, s.job_out, wid,
+                      BMG_MOVE_THREADS / 32);
+    } else if (kind == HJ_XY) {
+      const long long a = warp_sum_ll(geno_dot_part(K, s.phs, s.job_snp, s.job_term, threadIdx.x, BMG_MOVE_THREADS));
+      if (lane == 0) s.job_part[wid] = a;
+    }
+    bar_sync_all();
+  }
+}
+
 struct Warp {
   const DevConst& K;
   const DevPheno& P;    // the chain's sample (shared-memory copy)
@@ -147,6 +212,7 @@ struct Warp {
   int lane;
   bmg_rng_t rng;
   unsigned km;
+  bool helpers = false;  // warps 1-7 wait in help_loop for n-wide jobs
 
   __device__ Warp(const DevConst& k, int chain, MoveShared& sh)
   : K(k), P(sh.phs), c(chain), ch(&sh.chs), cur(&sh.mod[0]), nm(&sh.mod[1]), s(sh),
@@ -289,7 +355,6 @@ struct Warp {
   /* src/model.hpp:115-162: copy the active parts of a model */
   __device__ void copy_model(DevModel* d, const DevModel* src)
   {
-    PROF_SCOPE(PF_COPY);
     int xc = src->xcols, ll = src->llen;
     if (ll > SMK || src->vlen > SMK) spill(d);
     for (int col = 0; col < xc; ++col)
@@ -343,7 +408,6 @@ struct Warp {
   // solve U' x = b in place (forward substitution), U = first len of L
   __device__ void trsv_T(const DevModel* M, double* x, int len)
   {
-    PROF_SCOPE(PF_TRSV);
     const double* lb = Lb(M);
     for (int j = 0; j < len; ++j) {
       const double* colj = lb + TRI(0, j);
@@ -382,7 +446,6 @@ struct Warp {
   /* src/model.hpp:199-237, src/model.hpp:558-576 (Cholesky: LAPACK dpotf2, 'U') */
   __device__ void compute_log_likelihood(DevModel* M)
   {
-    PROF_SCOPE(PF_LIK);
     int m = M->xcols;
     if (m < 1) {
       if (lane == 0) M->ll = NAN;
@@ -463,18 +526,23 @@ struct Warp {
     }
     // the phenotype from the codes (no covariates in this case): 16
     // individuals per 32-bit word, the phenotype is zero outside the sample
-    const uint32_t* row = reinterpret_cast<const uint32_t*>(K.geno + (size_t)snp * K.gs);
-    const long long cH = coefH(term), cR = coefR(term);
-    long long acc = 0;
-    for (uint32_t w = lane; w < (uint32_t)(K.gs / 4); w += 32) {
-      const uint32_t code = row[w];
-      if (!code) continue;
-      for (int q = 0; q < 16; ++q) {
-        const uint32_t c2 = (code >> (2 * q)) & 3u;
-        if (c2 >= 2u) acc += (c2 == 2u ? cH : cR) * P.yint[(size_t)16 * w + q];
+    if (helpers) {
+      if (lane == 0) {
+        s.job_kind = HJ_XY;
+        s.job_snp = snp;
+        s.job_term = term;
       }
+      __syncwarp();
+      bar_sync_all();
+      const long long a = warp_sum_ll(geno_dot_part(K, P, snp, term, threadIdx.x, BMG_MOVE_THREADS));
+      if (lane == 0) s.job_part[0] = a;
+      bar_sync_all();
+      long long t = 0;
+      for (int w = 0; w < BMG_MOVE_THREADS / 32; ++w) t += s.job_part[w];
+      __syncwarp();
+      return t;
     }
-    return warp_sum_ll(acc);
+    return warp_sum_ll(geno_dot_part(K, P, snp, term, lane, 32));
   }
   // exact sum_i x_t(g_a,i) x_u(g_b,i) from the 2-bit codes
   __device__ long long geno_cross(uint32_t a, int t, uint32_t b, int u)
@@ -509,64 +577,43 @@ struct Warp {
     }
     return (double)geno_cross(M->xc_snp[r], M->xc_type[r], snp, term);
   }
-  // The same for the genotype columns r0 <= r < r1, four at a time: each
-  // word of the new column is loaded once per four model columns, and the
-  // four rows' loads are independent.  Exact integer popcounts.
+  // The same for the genotype columns r0 <= r < r1: on all eight warps while
+  // they help warp 0 (a move), else on warp 0 alone
   __device__ void cross_cols(const DevModel* M, int r0, int r1, uint32_t snp, int term, double* out)
   {
-    PROF_SCOPE(PF_XX);
-    const uint64_t* rb = (const uint64_t*)(K.geno + (size_t)snp * K.gs);
-    const unsigned nw64 = K.gs / 8;
-    const uint64_t m5 = 0x5555555555555555ull;
-    const int cHu = coefH(term), cRu = coefR(term);
-    for (int r = r0; r < r1; r += 4) {
-      const int cnt = min(4, r1 - r);
-      const uint64_t* ra[4];
-      int cH[4], cR[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int idx = r + min(q, cnt - 1);
-        ra[q] = (const uint64_t*)(K.geno + (size_t)M->xc_snp[idx] * K.gs);
-        cH[q] = coefH(M->xc_type[idx]);
-        cR[q] = coefR(M->xc_type[idx]);
+    if (r1 <= r0) return;
+    if (helpers) {
+      if (lane == 0) {
+        s.job_kind = HJ_CROSS;
+        s.job_M = M;
+        s.job_r0 = r0;
+        s.job_r1 = r1;
+        s.job_snp = snp;
+        s.job_term = term;
+        s.job_out = out;
       }
-      int hh[4] = {0, 0, 0, 0}, hr[4] = {0, 0, 0, 0}, rh[4] = {0, 0, 0, 0}, rr[4] = {0, 0, 0, 0};
-#pragma unroll 4
-      for (unsigned w = lane; w < nw64; w += 32) {
-        const uint64_t y = rb[w];
-        const uint64_t yh = (y >> 1) & (P.mask2 ? P.mask2[w] : m5), yl = y & m5;
-        const uint64_t Hy = yh & ~yl, Ry = yh & yl;
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const uint64_t x = ra[q][w];
-          const uint64_t xh = (x >> 1) & m5, xl = x & m5;
-          const uint64_t Hx = xh & ~xl, Rx = xh & xl;
-          hh[q] += __popcll(Hx & Hy);
-          hr[q] += __popcll(Hx & Ry);
-          rh[q] += __popcll(Rx & Hy);
-          rr[q] += __popcll(Rx & Ry);
-        }
-      }
-      long long v[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q)
-        v[q] = (long long)cH[q] * cHu * hh[q] + (long long)cH[q] * cRu * hr[q] +
-               (long long)cR[q] * cHu * rh[q] + (long long)cR[q] * cRu * rr[q];
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-#pragma unroll
-        for (int q = 0; q < 4; ++q) v[q] += __shfl_xor_sync(FULL_MASK, v[q], o);
-      }
-      if (lane == 0)
-        for (int q = 0; q < cnt; ++q) out[r + q] = (double)v[q];
+      __syncwarp();
+      bar_sync_all();
+      cross_cols_part(K, P, M, r0, r1, snp, term, out, 0, BMG_MOVE_THREADS / 32);
+      bar_sync_all();
+      return;
     }
+    cross_cols_part(K, P, M, r0, r1, snp, term, out, 0, 1);
+  }
+  // end of the helpers' service (warp 0, after a move)
+  __device__ void help_exit()
+  {
+    if (!helpers) return;
+    if (lane == 0) s.job_kind = HJ_EXIT;
+    __syncwarp();
+    bar_sync_all();
+    helpers = false;
   }
 
   // --------------------------------------------------------- model updates
   /* src/model.hpp:432-506 with src/symmmatrix.cpp:144-164 */
   __device__ void upd_add(DevModel* M, uint32_t snp, int mi, int term, bool is2, double invv, bool update)
   {
-    PROF_SCOPE(PF_ADD);
     int col = M->xcols;
     if (col + 1 > SMK) spill(M);
     if (lane == 0) {
@@ -672,7 +719,6 @@ struct Warp {
   /* src/dchex.f:130-220 (job 2) on L with k = x_ind + 1, l = p = order */
   __device__ void dchex_left(DevModel* M, int x_ind, int order, double* cs, double* sn)
   {
-    PROF_SCOPE(PF_DCHEX);
     // one lane: the rotation chain is sequential
     if (order <= SMK) { cs = s.cs; sn = s.sn; }
     if (lane == 0) {
@@ -726,7 +772,6 @@ struct Warp {
   /* src/model.hpp:508-556 with src/symmmatrix.cpp:126-195 */
   __device__ void upd_rem(DevModel* M, int x_ind, double* cs, double* sn)
   {
-    PROF_SCOPE(PF_REM);
     int len = M->xcols;
     double invv = M->inv[x_ind];
     __syncwarp();
@@ -973,7 +1018,6 @@ struct Warp {
   // dd_add zero state toggles (src/discrete_distribution.hpp:156-199)
   __device__ void add_set_zero(uint32_t snp, bool zero)
   {
-    PROF_SCOPE(PF_FLIP);
     int at;
     bool in_list = pend_find(snp, &at);
     bool zeroed = base_zero(snp) != in_list;
@@ -1089,7 +1133,6 @@ struct Warp {
   /* src/discrete_distribution.hpp:125-153 on the in-order prefix */
   __device__ uint32_t add_sample()
   {
-    PROF_SCOPE(PF_ASAMP);
     long long totali = add_total_int();
     double total = (double)totali * ldexp(1.0, -K.qs);
     double r = u01() * total;
@@ -1182,7 +1225,6 @@ struct Warp {
   }
   __device__ uint32_t rs_sample()
   {
-    PROF_SCOPE(PF_RSAMP);
     double total = rs_total();
     double r = u01() * total;
     double acc = 0;
@@ -1211,7 +1253,6 @@ struct Warp {
   // commit the proposed model as the current one (Model::operator=)
   __device__ void accept_model()
   {
-    PROF_SCOPE(PF_ACCEPT);
     // membership map of the current model: clear old, set new
     int32_t* mi = K.model_inds + (size_t)c * K.p;
     uint32_t* ib = K.inbits + (size_t)c * ((K.p + 31) / 32);
@@ -1233,7 +1274,6 @@ struct Warp {
   /* src/sampler.hpp:1126-1165 */
   __device__ int prepare_addrem(double& lqf, int ms)
   {
-    PROF_SCOPE(PF_PREPQ);
     long long max_adds = (long long)K.p - cur->k, max_rems = cur->k;
     int nrem = 0;
     for (int i = 0; i < ms; ++i) {
@@ -1317,7 +1357,6 @@ struct Warp {
   /* src/sampler.hpp:1168-1202 */
   __device__ void backward_prepare_addrem(double& lqb, int ms)
   {
-    PROF_SCOPE(PF_BACKQ);
     long long max_adds = (long long)K.p - nm->k, max_rems = nm->k;
     double w_add = add_total(), w_rem = rs_total();
     long long wmb = s.w_m;
@@ -1581,7 +1620,6 @@ struct Warp {
   /* src/sampler.hpp:1715-1769 */
   __device__ void adapt_move_size()
   {
-    PROF_SCOPE(PF_ADAPT);
     double* q_p0 = K.q_p0_ms + (size_t)c * 256;
     const double* rs = K.r_ms_sum + (size_t)c * 256;
     const double* rn = K.r_ms_n + (size_t)c * 256;
@@ -1847,7 +1885,6 @@ __device__ void bulk_setup(Warp& W, BulkCols& bc, int mode)
    With scan_only the flags ask for p_r only and no counter moves. */
 __device__ void prep_rb(Warp& W, bool scan_only)
 {
-  PROF_SCOPE(PF_RB);
   const DevConst& K = W.K;
   DevChain* ch = W.ch;
   RbParams* rp = K.rb + W.c;
@@ -2123,10 +2160,8 @@ bmg_move_kernel(DevConst K, int max_iters)
   for (int it = 0; it < max_iters; ++it) {
     __syncthreads();
     if (s.err || s.iter_stop) break;
-    PROF_SCOPE(PF_ITER);
     // room for one more move's flips of dd_add, else rebuild its prefix here
     if (s.n_pend > BMG_PEND_MAX - 2 * (int)K.max_move_size - 2) {
-      PROF_SCOPE(PF_REBUILD);
       if (tid == 0) ch->n_pend = 0;
       rebuild_chain(K, c, part, ch);
       if (tid == 0) s.n_pend = 0;
@@ -2137,7 +2172,6 @@ bmg_move_kernel(DevConst K, int max_iters)
     const bool thin_step = ((iter + 1) % K.thin) == 0;
     const bool rb_step = ((iter + 1) % K.n_rao) == 0;
     if (ns_step) {
-      PROF_SCOPE(PF_NS);
       /* src/sampler.cpp:628-635 */
       if (tid < 32) bulk_setup(W, bc, BULK_ALPHA);
       __syncthreads();
@@ -2161,9 +2195,7 @@ bmg_move_kernel(DevConst K, int max_iters)
       for (int i = 1; i < 7; ++i) pcs[i] = pcs[i - 1] + pm[i];
       int move = W.sample_naive(pcs, 7);
       int jd = 0;
-#ifdef BMG_MOVE_PROF
-      ProfScope move_scope(PF_MOVE);
-#endif
+      W.helpers = true;
       switch (move) {
         case 0: jd = W.do_addrem_move(cs_buf, sn_buf); break;
         case 1:
@@ -2177,6 +2209,7 @@ bmg_move_kernel(DevConst K, int max_iters)
           break;
         default: W.fail(BMG_DERR_NAN); break;
       }
+      W.help_exit();
       if (W.lane == 0) {
         ch->n_moves[move]++;
         ch->n_acpt[move] += (jd > 0);
@@ -2199,10 +2232,11 @@ bmg_move_kernel(DevConst K, int max_iters)
       }
       __syncwarp();
       if (thin_step) bulk_setup(W, bc, BULK_PVE | (rb_step ? BULK_RESID : 0));
+    } else {
+      help_loop(K, s);
     }
     __syncthreads();
     if (thin_step) {
-      PROF_SCOPE(PF_BULK);
       bulk_phase(K, c, s, bc);
       if (tid < 32) {
         /* src/sampler.cpp:691-727, src/model.hpp:345-392 */

@@ -56,6 +56,7 @@ def lib():
         L.bmgport_schur.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]
         L.bmgport_scan_yhat.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_double, C.c_void_p,
                                         C.c_void_p]
+        L.bmgport_scan_yhat_logodds.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_double, C.c_void_p]
         L.bmgport_get_state.argtypes = [C.c_void_p, C.c_uint32, C.POINTER(abi.ChainState),
                                         C.c_void_p, C.c_void_p, C.c_uint32]
         L.bmgport_get_rao.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]
@@ -158,6 +159,14 @@ class Port:
         if lib().bmgport_scan_yhat(self.h, chain, _ptr(yh), float(sigma2), _ptr(pr), _ptr(prt)) != 0:
             raise RuntimeError("oracle scan failed")
         return pr, (prt.reshape(self.m_g, self.n_types) if prt is not None else None)
+
+    def scan_yhat_logodds(self, y_hat, sigma2, chain=0):
+        """Per-SNP log posterior odds of the RB scan against y_hat and sigma2."""
+        lo = np.zeros(self.m_g)
+        yh = np.ascontiguousarray(y_hat, dtype=np.float64)
+        if lib().bmgport_scan_yhat_logodds(self.h, chain, _ptr(yh), float(sigma2), _ptr(lo)) != 0:
+            raise RuntimeError("oracle scan failed")
+        return lo
 
     def state(self, chain=0, cap=4096):
         st = abi.ChainState()

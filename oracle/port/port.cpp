@@ -2602,6 +2602,25 @@ extern "C" int bmgport_scan_yhat(bmgport* P, uint32_t chain, const double* y_hat
   }
 }
 
+/* The log posterior odds of the same scan (the per-SNP Bayes factor with its
+   prior odds, src/sampler.cpp:193-195) against the given y_hat and sigma2. */
+extern "C" int bmgport_scan_yhat_logodds(bmgport* P, uint32_t chain, const double* y_hat, double sigma2,
+                                         double* logodds)
+{
+  try {
+    Sampler* s = P->p.chains.at(chain);
+    std::vector<double> yh(y_hat, y_hat + s->data->n);
+    s->cur->sigma2 = sigma2;
+    std::vector<double> pr(s->m_g), prt(s->use_types ? s->m_g * s->n_types : 1);
+    s->logodds_out = logodds;
+    s->p_raoblackwell(yh, pr.data(), prt.data());
+    s->logodds_out = nullptr;
+    return 0;
+  } catch (...) {
+    return 1;
+  }
+}
+
 extern "C" int bmgport_get_state(bmgport* P, uint32_t chain, bmg_chain_state* st, uint32_t* loci,
                                  uint8_t* type_inds, uint32_t cap)
 {

@@ -38,6 +38,7 @@ int bmgport_schur(bmgport* P, uint32_t chain, double* dlml, double* itv);
 /* RB scan of one chain against y - y_hat with sigma2 replaced (known-answer tests) */
 int bmgport_scan_yhat(bmgport* P, uint32_t chain, const double* y_hat, double sigma2,
                       double* p_r, double* p_r_types);
+int bmgport_scan_yhat_logodds(bmgport* P, uint32_t chain, const double* y_hat, double sigma2, double* logodds);
 int bmgport_get_state(bmgport* P, uint32_t chain, bmg_chain_state* st,
                       uint32_t* loci, uint8_t* type_inds, uint32_t cap);
 /* the prior's shared 1/(tau2 alpha^2) per term type (A, H, D, R) */
