@@ -146,6 +146,7 @@ struct bmg_ctx {
   double* lml_buf = nullptr;                   // per-SNP log odds of the scans (bmg_scan_logodds, learned proposal)
   double* yhat_given = nullptr;                // chains x n fitted values of bmg_scan_yhat
   uint32_t wait_limit = 0;                     // main-loop wait bound of the tensor-core scan (0: default)
+  uint32_t dr = 0;                             // delayed rejection: largest move enumerated (0: off)
   int32_t* adam_t = nullptr;                   // learned proposal: optimiser step counter (device)
   uint64_t rb_steps = 0;                       // RB steps issued by bmg_run
   double* schur_out = nullptr;                 // bmg_scan_schur output on the device
@@ -323,8 +324,6 @@ extern "C" bmg_status bmg_create(const bmg_options* opt, bmg_ctx** out)
     c->opt.seeds = c->seeds.data();
     if (opt->sampler_type != 0)
       throw bmg_error(BMG_EUNSUPPORTED, "only the PMV sampler runs on the GPU path");
-    if (opt->delay_rejection != 0)
-      throw bmg_error(BMG_EUNSUPPORTED, "delayed rejection is not on the GPU path (set delay_rejection = 0)");
     if (opt->proposal != BMG_PROPOSAL_ADAPTIVE && opt->proposal != BMG_PROPOSAL_LEARNED)
       throw bmg_error(BMG_EINVAL, "proposal must be BMG_PROPOSAL_ADAPTIVE or BMG_PROPOSAL_LEARNED");
     if (opt->proposal == BMG_PROPOSAL_LEARNED &&
@@ -348,6 +347,12 @@ extern "C" bmg_status bmg_create(const bmg_options* opt, bmg_ctx** out)
     c->L = opt->scan_limbs ? opt->scan_limbs : 6;
     if (c->L < 3 || c->L > 7) throw bmg_error(BMG_EINVAL, "scan_limbs must be 3..7");
     c->max_ms = (int)std::min<uint64_t>(std::min<uint64_t>(c->p, 255), opt->max_move_size);
+    // delayed rejection enumerates 2^m sub-models of a rejected move of m
+    // SNPs (src/sampler.hpp:163-169: m <= min(delay_rejection, max_move_size))
+    c->dr = (uint32_t)std::min<uint64_t>((uint64_t)c->max_ms, opt->delay_rejection);
+    if (c->dr > BMG_DR_MAX)
+      throw bmg_error(BMG_EUNSUPPORTED, "delayed rejection above " + std::to_string(BMG_DR_MAX) +
+                                            " SNPs per move is not on the GPU path");
     if (c->km + (uint32_t)c->max_ms > BMG_REMSET_MAX)
       throw bmg_error(BMG_EINVAL, "max_model_size + max_move_size exceeds the device limit");
     if (c->km < opt->m_e + 3) throw bmg_error(BMG_EINVAL, "max_model_size too small");
@@ -1043,6 +1048,16 @@ extern "C" bmg_status bmg_precompute(bmg_ctx* ctx)
   K.limbs = ctx->dalloc<uint16_t>((size_t)C * ctx->L * ctx->n_pad);
   ctx->resid_t = ctx->dalloc<int64_t>((size_t)C * ctx->n_pad);
   K.scratch = ctx->dalloc<double>((size_t)C * 2 * km);
+  K.dr = ctx->dr;
+  if (ctx->dr) {
+    K.dr_l = ctx->dalloc<double>((size_t)C * km * (km + 1) / 2);
+    K.dr_v = ctx->dalloc<double>((size_t)C * km);
+    K.dr_inv = ctx->dalloc<double>((size_t)C * km);
+    K.dr_ti = ctx->dalloc<uint8_t>((size_t)C * km);
+    K.dr_x1 = ctx->dalloc<uint32_t>((size_t)C * km);
+    K.dr_x2 = ctx->dalloc<uint32_t>((size_t)C * km);
+    K.dr_pm = ctx->dalloc<double>((size_t)C << ctx->dr);
+  }
   // trace buffers of one chunk
   uint32_t gi = o.graph_iters ? o.graph_iters : 64;
   ctx->opt.graph_iters = gi;

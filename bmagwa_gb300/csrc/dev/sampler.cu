@@ -18,6 +18,7 @@
 
 #include "common.cuh"
 #include "df64.h"
+#include "flog.h"
 
 #define TAB_ADD_A 0
 #define TAB_REM_A 1
@@ -66,6 +67,7 @@ struct MoveShared {
   uint8_t rs_on[BMG_REMSET_MAX];
   // bulk phase exchange
   long long bl[8][2];
+  unsigned long long bi[8][4];  // per warp: 128-bit sums of the integer bulk phase (lo, hi pairs)
   double bd[8][6];
   double bsum[6];
   long long bsuml[2];
@@ -87,6 +89,12 @@ struct MoveShared {
   const DevModel* job_M;
   double* job_out;
   long long job_part[BMG_MOVE_THREADS / 32];
+  // delayed rejection: the exhaustive model's scalars and, per moved SNP
+  // (bit order), its proposal weights
+  int dr_ms, dr_vs, dr_llen, dr_Ns[5];
+  double dr_syx, dr_ldq, dr_ldqx, dr_lmp;
+  double dr_qa[BMG_DR_MAX], dr_qr[BMG_DR_MAX], dr_lqt[BMG_DR_MAX];
+  int dr_b2o[BMG_DR_MAX];
 };
 
 // genotype columns of the bulk phase: snp, term, fixed-point coefficient
@@ -405,36 +413,122 @@ struct Warp {
   }
 
   // ------------------------------------------------------- linear algebra
+  // An FP64 instruction occupies a GB300 SM sub-partition's FP64 pipe for
+  // about 64 cycles whatever the number of active lanes (a dependent DFMA
+  // takes 31 ns, a division 0.2 us, a log 1 us), so the solves below keep the
+  // solution in registers, one element per lane and chunk of 32, and work
+  // column by column: a step is one multiplication by the reciprocal of the
+  // diagonal (all reciprocals taken up front, lane-parallel), a broadcast and
+  // one FMA per chunk.  Orders beyond REG_N keep the memory-resident loops.
+  static constexpr int REG_Q = 4;
+  static constexpr int REG_N = 32 * REG_Q;
+
   // solve U' x = b in place (forward substitution), U = first len of L
   __device__ void trsv_T(const DevModel* M, double* x, int len)
   {
     const double* lb = Lb(M);
-    for (int j = 0; j < len; ++j) {
-      const double* colj = lb + TRI(0, j);
-      double part = 0.0;
-      for (int i = lane; i < j; i += 32) part += colj[i] * x[i];
-      part = warp_sum_d(part);
-      double xj = (x[j] - part) / colj[j];
-      __syncwarp();
-      if (lane == 0) x[j] = xj;
-      __syncwarp();
+    if (len > REG_N) {
+      for (int j = 0; j < len; ++j) {
+        const double* colj = lb + TRI(0, j);
+        double part = 0.0;
+        for (int i = lane; i < j; i += 32) part += colj[i] * x[i];
+        part = warp_sum_d(part);
+        double xj = (x[j] - part) / colj[j];
+        __syncwarp();
+        if (lane == 0) x[j] = xj;
+        __syncwarp();
+      }
+      return;
     }
+    double xr[REG_Q], rd[REG_Q];
+#pragma unroll
+    for (int q = 0; q < REG_Q; ++q) {
+      const int i = lane + 32 * q;
+      xr[q] = (i < len) ? x[i] : 0.0;
+      rd[q] = 0.0;
+      if (32 * q < len) rd[q] = 1.0 / ((i < len) ? lb[TRI(i, i)] : 1.0);
+    }
+#pragma unroll
+    for (int qc = 0; qc < REG_Q; ++qc) {
+      if (32 * qc >= len) break;
+      const int jend = min(32, len - 32 * qc);
+      for (int jj = 0; jj < jend; ++jj) {
+        const int j = 32 * qc + jj;
+        const double xj = __shfl_sync(FULL_MASK, xr[qc] * rd[qc], jj);
+        if (lane == jj) xr[qc] = xj;
+#pragma unroll
+        for (int qq = qc; qq < REG_Q; ++qq) {
+          if (32 * qq >= len) break;
+          const int i = lane + 32 * qq;
+          if (i > j && i < len) xr[qq] = fma(-lb[TRI(j, i)], xj, xr[qq]);
+        }
+      }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < REG_Q; ++q) {
+      const int i = lane + 32 * q;
+      if (i < len) x[i] = xr[q];
+    }
+    __syncwarp();
   }
   // solve U x = b in place (back substitution, column sweep)
   __device__ void trsv_N(const DevModel* M, double* x, int len)
   {
     const double* lb = Lb(M);
-    for (int j = len - 1; j >= 0; --j) {
-      const double* colj = lb + TRI(0, j);
-      double xj = x[j];
-      __syncwarp();
-      if (xj != 0.0) {
-        xj = xj / colj[j];
-        for (int i = lane; i < j; i += 32) x[i] -= xj * colj[i];
-        if (lane == 0) x[j] = xj;
+    if (len > REG_N) {
+      for (int j = len - 1; j >= 0; --j) {
+        const double* colj = lb + TRI(0, j);
+        double xj = x[j];
+        __syncwarp();
+        if (xj != 0.0) {
+          xj = xj / colj[j];
+          for (int i = lane; i < j; i += 32) x[i] -= xj * colj[i];
+          if (lane == 0) x[j] = xj;
+        }
+        __syncwarp();
       }
-      __syncwarp();
+      return;
     }
+    double xr[REG_Q], rd[REG_Q];
+#pragma unroll
+    for (int q = 0; q < REG_Q; ++q) {
+      const int i = lane + 32 * q;
+      xr[q] = (i < len) ? x[i] : 0.0;
+      rd[q] = 0.0;
+      if (32 * q < len) rd[q] = 1.0 / ((i < len) ? lb[TRI(i, i)] : 1.0);
+    }
+#pragma unroll
+    for (int qc = REG_Q - 1; qc >= 0; --qc) {
+      if (32 * qc >= len) continue;
+      const int jend = min(32, len - 32 * qc);
+      for (int jj = jend - 1; jj >= 0; --jj) {
+        const int j = 32 * qc + jj;
+        const double* colj = lb + TRI(0, j);
+        const double xj = __shfl_sync(FULL_MASK, xr[qc] * rd[qc], jj);
+        if (lane == jj) xr[qc] = xj;
+#pragma unroll
+        for (int qq = 0; qq <= qc; ++qq) {
+          const int i = lane + 32 * qq;
+          if (i < j) xr[qq] = fma(-colj[i], xj, xr[qq]);
+        }
+      }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < REG_Q; ++q) {
+      const int i = lane + 32 * q;
+      if (i < len) x[i] = xr[q];
+    }
+    __syncwarp();
+  }
+  // sum of log(L_ii) over lo <= i < hi, one log per lane
+  __device__ double sum_log_diag(const DevModel* M, int lo, int hi)
+  {
+    const double* lb = Lb(M);
+    double acc = 0.0;
+    for (int i = lo + lane; i < hi; i += 32) acc += flog(lb[TRI(i, i)]);
+    return warp_sum_d(acc);
   }
   __device__ double dot(const double* a, const double* b, int len)
   {
@@ -460,11 +554,11 @@ struct Warp {
       for (int r = lane; r <= col; r += 32) lb[TRI(r, col)] = M->xx[(size_t)col * km + r];
     __syncwarp();
     double log_sum_2 = 0;
-    if (lane == 0) lb[0] += M->inv[0];
-    for (int i = 1; i < m; ++i) {
-      if (lane == 0) lb[TRI(i, i)] += M->inv[i];
-      log_sum_2 += log(M->inv[i]);
+    for (int i = lane; i < m; i += 32) {
+      lb[TRI(i, i)] += M->inv[i];
+      if (i > 0) log_sum_2 += flog(M->inv[i]);
     }
+    log_sum_2 = warp_sum_d(log_sum_2);
     __syncwarp();
     double ldq = 0.5 * log_sum_2;
     bool ok = true;
@@ -501,14 +595,13 @@ struct Warp {
     __syncwarp();
     trsv_T(M, vb, m);
     double vv = dot(vb, vb, m);
-    double ldqx = 0;
-    for (int i = 0; i < m; ++i) ldqx += log(lb[TRI(i, i)]);
+    double ldqx = sum_log_diag(M, 0, m);
     double syx = P.nus2_plus_yy - vv;
     if (lane == 0) {
       M->vlen = m;
       M->syx = syx;
       M->ldqx = ldqx;
-      M->ll = ldq - ldqx + P.minus_n_plus_nu_2 * log(syx);
+      M->ll = ldq - ldqx + P.minus_n_plus_nu_2 * flog(syx);
       M->mu_beta_computed = 0;
     }
     __syncwarp();
@@ -665,8 +758,8 @@ struct Warp {
     double vm2 = M->xy[col] - dot(lcol, vb, col);
     double vc = vm2 / lcc;
     double syx = M->syx - vc * vc;
-    double ldq = M->ldq + 0.5 * log(invv);
-    double ldqx = M->ldqx + log(lcc);
+    double ldq = M->ldq + 0.5 * flog(invv);
+    double ldqx = M->ldqx + flog(lcc);
     __syncwarp();
     if (lane == 0) {
       lcol[col] = lcc;
@@ -675,7 +768,7 @@ struct Warp {
       M->syx = syx;
       M->ldq = ldq;
       M->ldqx = ldqx;
-      M->ll = ldq - ldqx + P.minus_n_plus_nu_2 * log(syx);
+      M->ll = ldq - ldqx + P.minus_n_plus_nu_2 * flog(syx);
     }
     __syncwarp();
   }
@@ -716,56 +809,85 @@ struct Warp {
     }
   }
 
-  /* src/dchex.f:130-220 (job 2) on L with k = x_ind + 1, l = p = order */
+  /* src/dchex.f:130-220 (job 2) on L with k = x_ind + 1, l = p = order:
+     column k moves to the end and the left shift's subdiagonal is removed by
+     Givens rotations.  Rotation ii acts on rows k + ii - 1 and k + ii of
+     every later column and is made from column k + ii - 1 once that column
+     has taken rotations 1 .. ii - 1.  Here lane t holds column k + t and the
+     rotations run as a wavefront (lane t applies rotation q of its group at
+     step t + q and makes its own at step 2t + 1), 32 columns at a time, so
+     the chain of FP64 instructions grows with the order instead of its
+     square.  Each element takes the reference's rotations in the reference's
+     order; the rotations come from the same inputs, formed with one
+     reciprocal square root instead of dchex's scaled divisions. */
   __device__ void dchex_left(DevModel* M, int x_ind, int order, double* cs, double* sn)
   {
-    // one lane: the rotation chain is sequential
     if (order <= SMK) { cs = s.cs; sn = s.sn; }
-    if (lane == 0) {
-      const int k = x_ind + 1, l = order, p = order;
-      const int km1 = k - 1, lmk = l - k;
-      double* r = Lb(M);
+    const int k = x_ind + 1, l = order;
+    const int km1 = k - 1, lmk = l - k;
+    double* r = Lb(M);
 #define R_(i, j) r[TRI((i) - 1, (j) - 1)]
-      for (int i = 1; i <= k; ++i) sn[lmk + i - 1] = R_(i, k);
-      for (int j = k; j <= l - 1; ++j) {
-        for (int i = 1; i <= j; ++i) R_(i, j) = R_(i, j + 1);
-        sn[j - km1 - 1] = R_(j + 1, j + 1);
-      }
-      for (int i = 1; i <= k; ++i) R_(i, l) = sn[lmk + i - 1];
-      for (int i = k + 1; i <= l; ++i) R_(i, l) = 0.0;
-      for (int j = k; j <= p; ++j) {
-        if (j != k) {
-          int iu = min(j - 1, l - 1);
-          for (int i = k; i <= iu; ++i) {
-            int ii = i - k + 1;
-            double t = cs[ii - 1] * R_(i, j) + sn[ii - 1] * R_(i + 1, j);
-            R_(i + 1, j) = cs[ii - 1] * R_(i + 1, j) - sn[ii - 1] * R_(i, j);
-            R_(i, j) = t;
-          }
-        }
-        if (j < l) {
-          int jj = j - k + 1;
-          // drotg(r(j,j), s(jj)) -> c(jj), s(jj), netlib semantics
-          double sa = R_(j, j), sb = sn[jj - 1];
-          double roe = (fabs(sa) > fabs(sb)) ? sa : sb;
-          double scale = fabs(sa) + fabs(sb);
-          double rr, cc, ss;
-          if (scale == 0.0) {
-            cc = 1.0; ss = 0.0; rr = 0.0;
-          } else {
-            double ta = sa / scale, tb = sb / scale;
-            rr = scale * sqrt(ta * ta + tb * tb);
-            if (roe < 0.0) rr = -rr;
-            cc = sa / rr;
-            ss = sb / rr;
-          }
-          R_(j, j) = rr;
-          cs[jj - 1] = cc;
-          sn[jj - 1] = ss;
-        }
-      }
-#undef R_
+    // column k is kept aside at sn[lmk ..], the columns after it move left
+    // and their diagonals, now below the diagonal, wait in sn[0 .. lmk - 1]
+    for (int i = 1 + lane; i <= k; i += 32) sn[lmk + i - 1] = R_(i, k);
+    __syncwarp();
+    for (int j = k; j <= l - 1; ++j) {
+      // column j's slots end where column j + 1's begin: the copy never
+      // overwrites a source element
+      for (int i = 1 + lane; i <= j; i += 32) R_(i, j) = R_(i, j + 1);
+      if (lane == 0) sn[j - km1 - 1] = R_(j + 1, j + 1);
+      __syncwarp();
     }
+    for (int i = 1 + lane; i <= k; i += 32) R_(i, l) = sn[lmk + i - 1];
+    for (int i = k + 1 + lane; i <= l; i += 32) R_(i, l) = 0.0;
+    __syncwarp();
+    const int ncols = l - k + 1;  // columns k .. l
+    for (int g0 = 0; g0 < ncols; g0 += 32) {
+      const int t = g0 + lane;
+      const bool mine = t < ncols;
+      const int j = k + t;
+      // rotations of earlier groups, in order
+      for (int rr = 1; rr <= g0; ++rr) {
+        if (mine) {
+          const double c = cs[rr - 1], sg = sn[rr - 1];
+          const int i = k + rr - 1;
+          const double a = R_(i, j), bb = R_(i + 1, j);
+          R_(i + 1, j) = c * bb - sg * a;
+          R_(i, j) = c * a + sg * bb;
+        }
+      }
+      __syncwarp();
+      for (int step = 1; step < 64; ++step) {
+        const int q = step - lane;
+        const int rr = g0 + q;
+        if (mine && q >= 1) {
+          if (rr <= t && rr <= lmk) {
+            const double c = cs[rr - 1], sg = sn[rr - 1];
+            const int i = k + rr - 1;
+            const double a = R_(i, j), bb = R_(i + 1, j);
+            R_(i + 1, j) = c * bb - sg * a;
+            R_(i, j) = c * a + sg * bb;
+          } else if (rr == t + 1 && j < l) {
+            // drotg(r(j,j), s(jj)): r takes the sign of the larger input
+            const double sa = R_(j, j), sb = sn[rr - 1];
+            const double h2 = sa * sa + sb * sb;
+            double rv = 0.0, c = 1.0, sg = 0.0;
+            if (h2 > 0.0) {
+              const double sgn = (fabs(sa) > fabs(sb) ? sa : sb) < 0.0 ? -1.0 : 1.0;
+              const double ri = rsqrt(h2) * sgn;
+              rv = h2 * ri;
+              c = sa * ri;
+              sg = sb * ri;
+            }
+            R_(j, j) = rv;
+            cs[rr - 1] = c;
+            sn[rr - 1] = sg;
+          }
+        }
+        __syncwarp();
+      }
+    }
+#undef R_
     __syncwarp();
   }
 
@@ -793,7 +915,7 @@ struct Warp {
     if (x_ind == xc) {
       double lxx = L(M, x_ind, x_ind);
       double vx = Vb(M)[x_ind];
-      double ldqx = M->ldqx - log(lxx);
+      double ldqx = M->ldqx - flog(lxx);
       double syx = M->syx + vx * vx;
       __syncwarp();
       if (lane == 0) {
@@ -807,18 +929,26 @@ struct Warp {
       int order = M->llen;
       dchex_left(M, x_ind, order, cs, sn);
       int nl = order - 1;
-      for (int i = x_ind; i < nl; ++i) {
-        if (L(M, i, i) < 0) {
-          for (int j = i + lane; j < nl; j += 32) L(M, i, j) *= -1;
+      // rows whose diagonal came out negative change sign (a sign flip, the
+      // reference's multiplication by -1); the diagonal tests are lane-parallel
+      for (int base = x_ind; base < nl; base += 32) {
+        const int i0 = base + lane;
+        unsigned neg = __ballot_sync(FULL_MASK, i0 < nl && L(M, i0, i0) < 0);
+        while (neg) {
+          const int i = base + __ffs(neg) - 1;
+          neg &= neg - 1;
+          for (int j = i + lane; j < nl; j += 32) {
+            double& e = L(M, i, j);
+            e = __longlong_as_double(__double_as_longlong(e) ^ (long long)0x8000000000000000ull);
+          }
+          __syncwarp();
         }
-        __syncwarp();
       }
       double* vb = Vb(M);
       for (int i = lane; i < xc; i += 32) vb[i] = M->xy[i];
       __syncwarp();
       trsv_T(M, vb, nl);
-      double ldqx = 0;
-      for (int i = 0; i < nl; ++i) ldqx += log(L(M, i, i));
+      double ldqx = sum_log_diag(M, 0, nl);
       double syx = P.nus2_plus_yy - dot(vb, vb, xc);
       if (lane == 0) {
         M->llen = nl;
@@ -828,8 +958,8 @@ struct Warp {
       }
       __syncwarp();
     }
-    double ldq = M->ldq - 0.5 * log(invv);
-    double ll = ldq - M->ldqx + P.minus_n_plus_nu_2 * log(M->syx);
+    double ldq = M->ldq - 0.5 * flog(invv);
+    double ll = ldq - M->ldqx + P.minus_n_plus_nu_2 * flog(M->syx);
     __syncwarp();
     if (lane == 0) {
       M->ldq = ldq;
@@ -983,7 +1113,7 @@ struct Warp {
     double a = ch->alpha;
     for (int t = 0; t < 64; ++t) {
       if (nterms > 0) {
-        if ((a <= 0.0) || log(u01()) <= -2.0 * K.mu_alpha * a) a = -a;
+        if ((a <= 0.0) || flog(u01()) <= -2.0 * K.mu_alpha * a) a = -a;
         double as2 = a * M->sigma2;
         double var = 1.0 / (1.0 + xbxb / (a * as2));
         double mu = var * (K.mu_alpha - ebxb / as2);
@@ -1293,10 +1423,10 @@ struct Warp {
           ind = learned ? mlp_sample(wm) : add_sample();
           double q = (1.0 - eps) * qadd(ind) / tot;
           if (eps > 0) q += eps * (double)mlp_wint(ind) / (double)wm;
-          lqf += log(q);
+          lqf += flog(q);
         } else {
           ind = add_sample();
-          lqf += log(qadd(ind)) - log(tot);
+          lqf += flog(qadd(ind)) - flog(tot);
         }
         add_set_zero(ind, true);
         if (lane == 0) { s.move_isadd[i] = 1; s.move_inds[i] = ind; s.move_map[i] = ind; }
@@ -1305,7 +1435,7 @@ struct Warp {
         --max_rems;
         double tot = rs_total();
         ind = rs_sample();
-        lqf += log(qrem(ind)) - log(tot);
+        lqf += flog(qrem(ind)) - flog(tot);
         rs_set(ind, false);
         if (lane == 0) { s.move_isadd[i] = 0; s.move_inds[i] = ind; s.move_map[i] = -1; }
       }
@@ -1332,7 +1462,7 @@ struct Warp {
       if (K.n_types > 1) {
         double qa[5], qc[5];
         qtypes(ind, qa, qc);
-        lqb += log(qa[t_ind] / qc[K.n_types - 1]);
+        lqb += flog(qa[t_ind] / qc[K.n_types - 1]);
       }
       remove_term(nm, mi, cs, sn);
     }
@@ -1349,7 +1479,7 @@ struct Warp {
       }
       int type = K.types[t_ind];
       lmpc += lchange_add(nm->Ns, nm->k, type);
-      if (K.n_types > 1) lqf += log(qa[t_ind] / qc[K.n_types - 1]);
+      if (K.n_types > 1) lqf += flog(qa[t_ind] / qc[K.n_types - 1]);
       prepare_add(ind, type, itv, true);
       add_term(nm, ind, t_ind, itv);
     }
@@ -1370,7 +1500,7 @@ struct Warp {
         ind = (uint32_t)s.move_map[last_rem];
         --last_rem;
         double q = qrem(ind);
-        lqb += log(q) - log(w_rem);
+        lqb += flog(q) - flog(w_rem);
         w_rem -= q;
       } else {
         --max_adds;
@@ -1381,10 +1511,10 @@ struct Warp {
           const long long wi = mlp_wint(ind);
           double qm = (1.0 - eps) * q / w_add;
           if (eps > 0) qm += eps * (double)wi / (double)wmb;
-          lqb += log(qm);
+          lqb += flog(qm);
           wmb -= wi;
         } else {
-          lqb += log(q) - log(w_add);
+          lqb += flog(q) - flog(w_add);
         }
         w_add -= q;
       }
@@ -1398,21 +1528,26 @@ struct Warp {
     __syncwarp();
     double lqf = 0, lqb = 0, lmpc = 0;
     rs_build_from(cur);
-    prepare_addrem(lqf, ms);
+    const int nrem = prepare_addrem(lqf, ms);
     do_addrem(lqf, lqb, lmpc, ms, cs, sn);
     backward_prepare_addrem(lqb, ms);
     double log_r = lqb - lqf;
     log_r += lmpc + nm->ll - cur->ll;
     double* rs = K.r_ms_sum + (size_t)c * 256;
     double* rn = K.r_ms_n + (size_t)c * 256;
-    double addv = (log_r >= 0 ? 1.0 : exp(log_r));
+    // with delayed rejection the acceptance statistic counts moved SNPs
+    // (src/sampler.hpp:1001-1005, 1080)
+    const double addv = K.dr ? 0.0 : (log_r >= 0 ? 1.0 : exp(log_r));
     __syncwarp();
     if (lane == 0) { rs[ms - 1] += addv; rn[ms - 1] += 1.0; }
     __syncwarp();
-    if (log_r >= 0 || log(u01()) <= log_r) {
+    if (log_r >= 0 || flog(u01()) <= log_r) {
+      if (K.dr && lane == 0) rs[ms - 1] += 1.0;
+      __syncwarp();
       accept_model();
       return ms;
     }
+    if (ms <= (int)K.dr && ms > 1) return delayed_rejection(ms, nrem, cs, sn);
     copy_model(nm, cur);
     for (int i = 0; i < ms; ++i) {
       uint32_t ind = s.move_inds[i];
@@ -1508,7 +1643,7 @@ struct Warp {
       __syncwarp();
     }
     double log_r = nm->ll - cur->ll;
-    if (log_r >= 0 || log(u01()) <= log_r) {
+    if (log_r >= 0 || flog(u01()) <= log_r) {
       accept_model();
       for (int im = 0; im < ms; ++im) {
         add_set_zero(s.move_rem[im], false);
@@ -1577,13 +1712,14 @@ struct Warp {
       add_term(nm, ind_add, t_ind, itv);
     }
     double log_r = lmpc + nm->ll - cur->ll;
-    log_r += log((double)cur->k) - log((double)nm->k);
-    if (log_r >= 0 || log(u01()) <= log_r) {
+    log_r += flog((double)cur->k) - flog((double)nm->k);
+    if (log_r >= 0 || flog(u01()) <= log_r) {
       accept_model();
       for (int im = 0; im < nadd; ++im) add_set_zero(s.move_add[im], true);
       for (int im = 0; im < nrem; ++im) add_set_zero(s.move_rem[im], false);
       return ms;
     }
+    if (ms <= (int)K.dr && ms > 1) return delayed_rejection_statechange(ms, nadd, nrem, cs, sn);
     copy_model(nm, cur);
     return 0;
   }
@@ -1608,13 +1744,581 @@ struct Warp {
     prepare_add(ind, type_add, itv, false);
     add_term(nm, ind, ta, itv);
     double r = lchange_swi(cur->Ns, type_add, type_rem) + nm->ll - cur->ll -
-               log(qa[ta] / tmp[nt - 1]) + log(qa[tr] / (qc[nt - 1] - qa[ta]));
-    if (r >= 0 || log(u01()) <= r) {
+               flog(qa[ta] / tmp[nt - 1]) + flog(qa[tr] / (qc[nt - 1] - qa[ta]));
+    if (r >= 0 || flog(u01()) <= r) {
       accept_model();
       return 1;
     }
     copy_model(nm, cur);
     return 0;
+  }
+
+  // ------------------------------------------------- delayed rejection
+  // src/sampler.cpp:882-1049 (exhaustive sub-model set, second-stage
+  // proposal), src/sampler.hpp:929-1098 and 1547-1618 (the two second stages),
+  // src/model.hpp:585-844 (ExhModel), src/symmmatrix.cpp:220-264 (adjacent
+  // column swap of a Cholesky factor).  The exhaustive model lives in the
+  // chain's slices of K.dr_*; its scalars in shared memory.
+  __device__ size_t tri_n() const { return (size_t)km * (km + 1) / 2; }
+  __device__ double* drL() const { return K.dr_l + (size_t)c * tri_n(); }
+  __device__ double* drV() const { return K.dr_v + (size_t)c * km; }
+  __device__ double* drInv() const { return K.dr_inv + (size_t)c * km; }
+  __device__ uint8_t* drTi() const { return K.dr_ti + (size_t)c * km; }
+  __device__ uint32_t* drX1() const { return K.dr_x1 + (size_t)c * km; }
+  __device__ uint32_t* drX2() const { return K.dr_x2 + (size_t)c * km; }
+  __device__ double* drPm() const { return K.dr_pm + ((size_t)c << K.dr); }
+
+  /* ExhModel::update_to_model: the proposed model with its first const_loci
+     loci fixed; returns its log probability */
+  __device__ double dr_update_to_model(int const_loci)
+  {
+    const DevModel* M = nm;
+    {
+      const double* ls = Lb(M);
+      double* ld = drL();
+      const size_t tri = TRI(0, M->llen);
+      for (size_t q = lane; q < tri; q += 32) ld[q] = ls[q];
+      const double* vs = Vb(M);
+      for (int i = lane; i < M->vlen; i += 32) drV()[i] = vs[i];
+      for (int i = lane; i < M->xcols; i += 32) drInv()[i] = M->inv[i];
+      for (int i = lane; i < M->k; i += 32) {
+        drTi()[i] = M->type_inds[i];
+        drX1()[i] = M->x_ind1[i];
+        drX2()[i] = M->x_ind2[i];
+      }
+    }
+    __syncwarp();
+    int vsz = (int)K.m_e;
+    if (const_loci > 0) {
+      const int ti = drTi()[const_loci - 1];
+      vsz = (int)(K.types[ti] == 4 ? drX2()[const_loci - 1] : drX1()[const_loci - 1]) + 1;
+    }
+    const double* v = drV();
+    const double* L0 = drL();
+    const double syx = P.nus2_plus_yy - dot(v, v, vsz);
+    double a = 0.0, b = 0.0;
+    for (int i = lane; i < vsz; i += 32) {
+      a += flog(L0[TRI(i, i)]);
+      if (i >= 1 && i < (int)K.m_e) b += flog(K.inv_tau2_e[i]);
+      else if (i >= (int)K.m_e) b += flog(drInv()[i]);
+    }
+    const double ldqx = warp_sum_d(a);
+    const double ldq = 0.5 * warp_sum_d(b);
+    int Ns[5] = {0, 0, 0, 0, 0};
+    for (int i = 0; i < const_loci; ++i) ++Ns[K.types[drTi()[i]]];
+    __syncwarp();
+    if (lane == 0) {
+      s.dr_ms = const_loci;
+      s.dr_vs = vsz;
+      s.dr_llen = M->llen;
+      s.dr_syx = syx;
+      s.dr_ldq = ldq;
+      s.dr_ldqx = ldqx;
+      s.dr_lmp = 0.0;
+      for (int t = 0; t < 5; ++t) s.dr_Ns[t] = Ns[t];
+    }
+    __syncwarp();
+    return ldq - ldqx + P.minus_n_plus_nu_2 * flog(syx);
+  }
+
+  /* ExhModel::update_on_add: the next term joins the leading sub-model */
+  __device__ double dr_on_add()
+  {
+    const double* v = drV();
+    const double* Lx = drL();
+    const int ms = s.dr_ms;
+    const int type = K.types[drTi()[ms]];
+    int vs = s.dr_vs;
+    double syx = s.dr_syx, ldq = s.dr_ldq, ldqx = s.dr_ldqx;
+    for (int t = 0; t < (type == 4 ? 2 : 1); ++t) {
+      syx -= v[vs] * v[vs];
+      ldq += 0.5 * flog(drInv()[vs]);
+      ldqx += flog(Lx[TRI(vs, vs)]);
+      ++vs;
+    }
+    int Ns[5];
+    for (int t = 0; t < 5; ++t) Ns[t] = s.dr_Ns[t];
+    const double lmp = s.dr_lmp + lchange_add(Ns, ms, type);
+    __syncwarp();
+    if (lane == 0) {
+      s.dr_vs = vs;
+      s.dr_syx = syx;
+      s.dr_ldq = ldq;
+      s.dr_ldqx = ldqx;
+      s.dr_lmp = lmp;
+      s.dr_Ns[type]++;
+      s.dr_ms = ms + 1;
+    }
+    __syncwarp();
+    return ldq - ldqx + P.minus_n_plus_nu_2 * flog(syx) + lmp;
+  }
+
+  /* SymmMatrix::cholesky_swapadj: columns col and col + 1 trade places, one
+     rotation of rows col, col + 1 restores the triangle (and v) */
+  __device__ void dr_swapadj(int col)
+  {
+    double* Lx = drL();
+    double* v = drV();
+    const double b = Lx[TRI(col + 1, col + 1)];
+    __syncwarp();
+    for (int r = lane; r <= col; r += 32) {
+      const double x = Lx[TRI(r, col)], y = Lx[TRI(r, col + 1)];
+      Lx[TRI(r, col)] = y;
+      Lx[TRI(r, col + 1)] = x;
+    }
+    __syncwarp();
+    if (lane == 0) Lx[TRI(col + 1, col + 1)] = 0.0;
+    __syncwarp();
+    const double a = Lx[TRI(col, col)];
+    // drotg(a, b) with r taking the sign of the larger input, then the
+    // reference's flip to a positive diagonal
+    double rv = 0.0, cc = 1.0, ss = 0.0;
+    const double h2 = a * a + b * b;
+    if (h2 > 0.0) {
+      const double sgn = (fabs(a) > fabs(b) ? a : b) < 0.0 ? -1.0 : 1.0;
+      const double ri = rsqrt(h2) * sgn;
+      rv = h2 * ri;
+      cc = a * ri;
+      ss = b * ri;
+    }
+    if (rv < 0.0) {
+      rv = -rv;
+      ss = -ss;
+      cc = -cc;
+    }
+    const int llen = s.dr_llen;
+    for (int i = col + 1 + lane; i < llen; i += 32) {
+      const double x = Lx[TRI(col, i)], y = Lx[TRI(col + 1, i)];
+      Lx[TRI(col, i)] = y * ss + x * cc;
+      Lx[TRI(col + 1, i)] = x * ss - y * cc;
+    }
+    if (lane == 0) {
+      Lx[TRI(col, col)] = rv;
+      const double x = v[col], y = v[col + 1];
+      v[col] = y * ss + x * cc;
+      v[col + 1] = x * ss - y * cc;
+    }
+    __syncwarp();
+  }
+  __device__ void dr_swap_inv(uint32_t a, uint32_t b)
+  {
+    if (lane == 0) {
+      double* iv = drInv();
+      const double t = iv[a];
+      iv[a] = iv[b];
+      iv[b] = t;
+    }
+    __syncwarp();
+  }
+
+  /* ExhModel::update_on_moveleft: the last term of the leading sub-model
+     trades places with the one before it, which leaves the sub-model */
+  __device__ double dr_on_moveleft()
+  {
+    const double* v = drV();
+    int ms = s.dr_ms - 1;
+    const int ind_keep = ms, ind_rem = ms - 1;
+    uint8_t* ti = drTi();
+    uint32_t* x1 = drX1();
+    uint32_t* x2 = drX2();
+    const int type_keep = K.types[ti[ind_keep]], type_rem = K.types[ti[ind_rem]];
+    int vs = s.dr_vs;
+    double syx = s.dr_syx, ldq = s.dr_ldq, ldqx = s.dr_ldqx;
+    {
+      const double* Lx = drL();
+      --vs;
+      syx += v[vs] * v[vs];
+      ldqx -= flog(Lx[TRI(vs, vs)]);
+      if (type_keep == 4) {
+        --vs;
+        syx += v[vs] * v[vs];
+        ldqx -= flog(Lx[TRI(vs, vs)]);
+      }
+      --vs;
+      syx += v[vs] * v[vs];
+      ldq -= 0.5 * flog(drInv()[vs]);
+      ldqx -= flog(Lx[TRI(vs, vs)]);
+      if (type_rem == 4) {
+        --vs;
+        syx += v[vs] * v[vs];
+        ldq -= 0.5 * flog(drInv()[vs]);
+        ldqx -= flog(Lx[TRI(vs, vs)]);
+      }
+    }
+    __syncwarp();
+    if (lane == 0) {
+      const uint8_t t = ti[ind_keep];
+      ti[ind_keep] = ti[ind_rem];
+      ti[ind_rem] = t;
+    }
+    __syncwarp();
+    const uint32_t k1 = x1[ind_keep], k2 = x2[ind_keep], r1 = x1[ind_rem], r2 = x2[ind_rem];
+    if (type_rem == 4) {
+      if (type_keep == 4) {
+        int si = (int)r2;
+        dr_swapadj(si);
+        ++si;
+        dr_swapadj(si);
+        si -= 2;
+        dr_swapadj(si);
+        ++si;
+        dr_swapadj(si);
+        dr_swap_inv(k1, r2);
+        dr_swap_inv(k1, k2);
+        dr_swap_inv(r1, r2);
+        dr_swap_inv(k1, r2);
+      } else {
+        int si = (int)r2;
+        dr_swapadj(si);
+        --si;
+        dr_swapadj(si);
+        dr_swap_inv(r2, k1);
+        dr_swap_inv(r1, r2);
+        if (lane == 0) {
+          x2[ind_keep] = k1;
+          x1[ind_keep] = k1 - 1;
+        }
+      }
+    } else {
+      if (type_keep == 4) {
+        int si = (int)r1;
+        dr_swapadj(si);
+        ++si;
+        dr_swapadj(si);
+        dr_swap_inv(r1, k1);
+        dr_swap_inv(k1, k2);
+        if (lane == 0) {
+          x2[ind_rem] = k1;
+          x1[ind_keep] = k2;
+        }
+      } else {
+        dr_swapadj((int)r1);
+        dr_swap_inv(k1, r1);
+      }
+    }
+    __syncwarp();
+    {
+      const double* Lx = drL();
+      syx -= v[vs] * v[vs];
+      ldqx += flog(Lx[TRI(vs, vs)]);
+      ++vs;
+      if (type_keep == 4) {
+        syx -= v[vs] * v[vs];
+        ldqx += flog(Lx[TRI(vs, vs)]);
+        ++vs;
+      }
+    }
+    int Ns[5];
+    for (int t = 0; t < 5; ++t) Ns[t] = s.dr_Ns[t];
+    const double lmp = s.dr_lmp + lchange_rem(Ns, ms + 1, type_rem);
+    __syncwarp();
+    if (lane == 0) {
+      s.dr_ms = ms;
+      s.dr_vs = vs;
+      s.dr_syx = syx;
+      s.dr_ldq = ldq;
+      s.dr_ldqx = ldqx;
+      s.dr_lmp = lmp;
+      s.dr_Ns[type_rem]--;
+    }
+    __syncwarp();
+    return ldq - ldqx + P.minus_n_plus_nu_2 * flog(syx) + lmp;
+  }
+
+  __device__ void dr_put(double* pm, unsigned idx, double v, double& mx)
+  {
+    if (lane == 0) pm[idx] = v;
+    if (v > mx) mx = v;
+  }
+
+  /* compute_exhaustive_modelset (src/sampler.cpp:882-978): the log
+     probability of each of the 2^n sub-models of the last n terms, bit i of
+     the index = term i of the block in the model */
+  __device__ double dr_exhaustive(int n_inds, double* pm)
+  {
+    int ci[BMG_DR_MAX];
+    for (int i = 0; i < n_inds; ++i) ci[i] = i;
+    unsigned cb = 0;
+    int msz = 0;
+    double mx = -INFINITY;
+    dr_put(pm, 0, dr_update_to_model(s.dr_ms), mx);
+    for (int i = 0; i < n_inds; ++i) {
+      ++msz;
+      if (i > 1) {
+        ++msz;
+        dr_on_add();
+      }
+      cb = (1u << msz) - 1;
+      dr_put(pm, cb, dr_on_add(), mx);
+      for (int j = 0; j < i; ++j) {
+        --msz;
+        const int t = ci[msz - 1];
+        ci[msz - 1] = ci[msz];
+        ci[msz] = t;
+        cb &= ~(1u << t);
+        dr_put(pm, cb, dr_on_moveleft(), mx);
+      }
+      const unsigned nmodels = (1u << i) - i - 1;
+      unsigned jj = 0, nK = 0;
+      int do_lefts = 0;
+      while (jj < nmodels) {
+        if (do_lefts < 2) {
+          ++msz;
+          const int t = ci[msz];
+          ci[msz] = ci[msz - 1];
+          ci[msz - 1] = t;
+          cb |= (1u << t);
+          dr_on_add();
+          dr_on_add();
+          dr_put(pm, cb, dr_on_moveleft(), mx);
+          ++jj;
+          ++do_lefts;
+        } else {
+          ++nK;
+          int Kb = 0;
+          while (((nK >> Kb) & 1u) == 0) ++Kb;
+          for (int k2 = 0; k2 <= Kb; ++k2) {
+            --msz;
+            const int t = ci[msz - 1];
+            ci[msz - 1] = ci[msz];
+            ci[msz] = t;
+            cb &= ~(1u << t);
+            dr_put(pm, cb, dr_on_moveleft(), mx);
+            ++jj;
+          }
+          do_lefts = 0;
+        }
+      }
+    }
+    __syncwarp();
+    return mx;
+  }
+
+  /* compute_proposal_probs_for_exh_modelset (src/sampler.cpp:980-1049): the
+     log probability of proposing each sub-model from the model without the
+     block's terms (adds in order, removals in reverse), one sub-model per
+     lane at a time */
+  __device__ void dr_proposal_probs(int n_inds, double z_add, double z_rem, long long const_loci, double* pm)
+  {
+    const unsigned nmodels = 1u << n_inds;
+    const bool use_types = K.n_types > 1;
+    for (unsigned i = lane; i < nmodels; i += 32) {
+      long long max_adds = (long long)K.p - const_loci, max_rems = const_loci;
+      double z_a = z_add, z_r = z_rem;
+      unsigned isadd = 0;
+      for (int j = 0; j < n_inds; ++j) {
+        const int nind = s.dr_b2o[j];
+        if ((i >> j) & 1u) {
+          z_a -= s.dr_qa[nind];
+          z_r += s.dr_qr[nind];
+          ++max_rems;
+          --max_adds;
+        } else {
+          isadd |= 1u << nind;
+        }
+      }
+      double lp = 0.0;
+      int last_rem = n_inds - 1;
+      for (int j = 0; j < n_inds; ++j) {
+        if (max_adds > 0 && max_rems > 0) lp += LOG_HALF_D;
+        if ((isadd >> j) & 1u) {
+          --max_adds;
+          lp += flog(s.dr_qa[j]) - flog(z_a);
+          z_a -= s.dr_qa[j];
+          if (use_types) lp += s.dr_lqt[j];
+        } else {
+          --max_rems;
+          while ((isadd >> last_rem) & 1u) --last_rem;
+          lp += flog(s.dr_qr[last_rem]) - flog(z_r);
+          z_r -= s.dr_qr[last_rem];
+          --last_rem;
+        }
+      }
+      pm[i] += lp;
+    }
+    __syncwarp();
+  }
+
+  /* src/sampler.hpp:1009-1028: each sub-model below 2^(n-1) is paired with
+     its complement; the pair's weight (the difference of their
+     probabilities) goes to the likelier one.  A pair is drawn by its
+     cumulative weight (one uniform, src/utils.cpp:73-101) and the sub-model
+     carrying it is returned. */
+  __device__ unsigned dr_sample_pair(int n, double mx, double* pm)
+  {
+    const unsigned nmodels = 1u << n, mask = nmodels - 1, half = nmodels >> 1;
+    double carry = 0.0;
+    for (unsigned base = 0; base < half; base += 32) {
+      const unsigned i = base + lane;
+      double w = 0.0;
+      if (i < half) {
+        const unsigned j = (~i) & mask;
+        const double a = pm[j] - pm[i];
+        if (a > 0) {
+          w = exp(pm[j] - mx) * (1 - exp(-a));
+          pm[j] = -1.0;
+        } else {
+          w = exp(pm[i] - mx) * (1 - exp(a));
+          pm[j] = 1.0;
+        }
+      }
+      // inclusive prefix within the chunk, then the running total
+      for (int o = 1; o < 32; o <<= 1) {
+        const double t = __shfl_up_sync(FULL_MASK, w, o);
+        if (lane >= o) w += t;
+      }
+      w += carry;
+      if (i < half) pm[i] = w;
+      carry = __shfl_sync(FULL_MASK, w, 31);
+    }
+    __syncwarp();
+    const double rr = u01() * pm[half - 1];
+    unsigned pick = half - 1;
+    for (unsigned base = 0; base < half; base += 32) {
+      const unsigned i = base + lane;
+      const unsigned hit = __ballot_sync(FULL_MASK, i < half && rr < pm[i]);
+      if (hit) {
+        pick = base + __ffs(hit) - 1;
+        break;
+      }
+    }
+    const unsigned comp = (~pick) & mask;
+    if (pm[comp] < 0) pick = comp;
+    __syncwarp();
+    return pick;
+  }
+
+  // re-add a SNP of the current model to nm with the current model's precision
+  __device__ void dr_readd(uint32_t ind)
+  {
+    const int cmi = K.model_inds[(size_t)c * K.p + ind];
+    const int t_ind = cur->type_inds[cmi];
+    double itv[2];
+    itv[0] = cur->inv[cur->x_ind1[cmi]];
+    itv[1] = (K.types[t_ind] == 4) ? cur->inv[cur->x_ind2[cmi]] : 0.0;
+    add_term(nm, ind, t_ind, itv);
+  }
+  // keep the sub-model `sampled` of nm's last n terms: drop the others
+  __device__ void dr_keep(unsigned sampled, int n, int const_loci, double* cs, double* sn)
+  {
+    unsigned rem = sampled;
+    for (int i = 0; i < n; ++i) {
+      if ((rem & 1u) == 0) {
+        remove_term(nm, const_loci + i, cs, sn);
+        --const_loci;
+      }
+      rem >>= 1;
+    }
+  }
+
+  /* src/sampler.hpp:929-1098: the second stage after a rejected multi-SNP
+     add/remove move */
+  __device__ int delayed_rejection(int ms, int ms_rem, double* cs, double* sn)
+  {
+    const int const_loci = cur->k - ms_rem;
+    const int ms_add = ms - ms_rem;
+    double z_add = add_total(), z_rem = rs_total();
+    const unsigned newmodel = (1u << ms_add) - 1;
+    for (int i = 0; i < ms; ++i) {
+      const uint32_t ind = s.move_inds[i];
+      if (s.move_isadd[i]) {
+        z_add += qadd(ind);
+        z_rem -= qrem(ind);
+      } else {
+        dr_readd(ind);
+      }
+    }
+    for (int i = 0; i < ms; ++i) {
+      const uint32_t ind = (uint32_t)s.move_map[i];
+      const int mi = find_locus(nm, ind);
+      double lqt = 0.0;
+      if (K.n_types > 1) {
+        double qa[5], qc[5];
+        qtypes(ind, qa, qc);
+        lqt = flog(qa[nm->type_inds[mi]] / qc[K.n_types - 1]);
+      }
+      const double qa1 = qadd(ind), qr1 = qrem(ind);
+      __syncwarp();
+      if (lane == 0) {
+        s.dr_b2o[mi - const_loci] = i;
+        s.dr_qa[i] = qa1;
+        s.dr_qr[i] = qr1;
+        s.dr_lqt[i] = lqt;
+      }
+      __syncwarp();
+    }
+    double* pm = drPm();
+    if (lane == 0) s.dr_ms = const_loci;
+    __syncwarp();
+    const double mx = dr_exhaustive(ms, pm);
+    dr_proposal_probs(ms, z_add, z_rem, const_loci, pm);
+    const unsigned mask = (1u << ms) - 1;
+    const unsigned sampled = dr_sample_pair(ms, mx, pm);
+    if (sampled == ((~newmodel) & mask)) {
+      copy_model(nm, cur);
+      for (int i = 0; i < ms; ++i) {
+        const uint32_t ind = s.move_inds[i];
+        add_set_zero(ind, !s.move_isadd[i]);
+      }
+      return 0;
+    }
+    int moved = 0;
+    for (int i = 0; i < ms; ++i) {
+      const bool in_new = (newmodel >> i) & 1u;
+      const uint32_t ind = (uint32_t)s.move_map[s.dr_b2o[i]];
+      if ((sampled >> i) & 1u) {
+        if (!in_new) add_set_zero(ind, true);
+        else ++moved;
+      } else {
+        if (in_new) add_set_zero(ind, false);
+        else ++moved;
+      }
+    }
+    dr_keep(sampled, ms, const_loci, cs, sn);
+    double* rsum = K.r_ms_sum + (size_t)c * 256;
+    __syncwarp();
+    if (lane == 0) rsum[ms - 1] += (double)moved / (double)ms;
+    __syncwarp();
+    accept_model();
+    return moved;
+  }
+
+  /* src/sampler.hpp:1547-1618: the second stage after a rejected state
+     change; each sub-model's probability includes the choice of the central
+     SNP among its loci */
+  __device__ int delayed_rejection_statechange(int ms, int ms_add, int ms_rem, double* cs, double* sn)
+  {
+    const int const_loci = cur->k - ms_rem;
+    const unsigned newmodel = (1u << ms_add) - 1;
+    for (int i = 0; i < ms_rem; ++i) dr_readd(s.move_rem[i]);
+    double* pm = drPm();
+    if (lane == 0) s.dr_ms = const_loci;
+    __syncwarp();
+    const double mx = dr_exhaustive(ms, pm);
+    const unsigned nmodels = 1u << ms, mask = nmodels - 1;
+    for (unsigned i = lane; i < nmodels; i += 32) pm[i] -= flog((double)(const_loci + __popc(i)));
+    __syncwarp();
+    const unsigned sampled = dr_sample_pair(ms, mx, pm);
+    if (sampled == ((~newmodel) & mask)) {
+      copy_model(nm, cur);
+      return 0;
+    }
+    int moved = 0;
+    for (int i = 0; i < ms; ++i) {
+      const bool in_new = (newmodel >> i) & 1u;
+      if ((sampled >> i) & 1u) {
+        if (in_new) {
+          ++moved;
+          add_set_zero(s.move_add[i], true);
+        }
+      } else if (!in_new) {
+        ++moved;
+        add_set_zero(s.move_rem[i - ms_add], false);
+      }
+    }
+    dr_keep(sampled, ms, const_loci, cs, sn);
+    accept_model();
+    return moved;
   }
 
   /* src/sampler.hpp:1715-1769 */
@@ -1699,6 +2403,16 @@ struct Warp {
 #define BULK_RESID 4
 #define BULK_YHAT 8   // with BULK_RESID: the residual is y - K.yhat, the fitted values given
 
+// a 128-bit integer as the nearest-ish double (two roundings: relative error
+// below 2^-52)
+__device__ __forceinline__ double i128_to_double(__int128 v)
+{
+  const bool neg = v < 0;
+  const unsigned __int128 u = neg ? (unsigned __int128)(-v) : (unsigned __int128)v;
+  const double d = (double)(unsigned long long)(u >> 64) * 18446744073709551616.0 + (double)(unsigned long long)u;
+  return neg ? -d : d;
+}
+
 __device__ void bulk_phase(const DevConst& K, int c, MoveShared& s, BulkCols& bc)
 {
   const DevPheno& P = s.phs;
@@ -1714,6 +2428,12 @@ __device__ void bulk_phase(const DevConst& K, int c, MoveShared& s, BulkCols& bc
   // covariates, so y_hat then accumulates; the scan reads that y_hat
   // (src/sampler.cpp:735).  The same update is reproduced here.
   const bool stale = (mode & BULK_YHAT) || ((nt == 0) && (me > 1));
+  // Without covariates the PVE pass needs only sum x'b and sum (x'b)^2 over
+  // the sample (the covariate part is the constant), and nothing reads y_hat
+  // back: both sums are taken exactly in 128-bit integers from the
+  // fixed-point fitted values, with no FP64 instruction per individual.
+  const bool ifast = (me <= 1) && (mode & BULK_PVE) && !(mode & (BULK_YHAT | BULK_ALPHA));
+  __int128 ia = 0, ia2 = 0;
   double* yhat = K.yhat + (size_t)c * K.n;
   const int dsh = P.sy - sh;
   // a thread takes 16 individuals at a time: one 32-bit word of every model
@@ -1743,21 +2463,26 @@ __device__ void bulk_phase(const DevConst& K, int c, MoveShared& s, BulkCols& bc
       const bool live = i < K.n && (!P.mask2 || ((P.mask2[i >> 5] >> (2 * (i & 31))) & 1ull));
       const long long yg = yg16[q];
       double ye = 0;
-      if (live) {
+      if (ifast) {
+        if (live) {
+          ia += yg;
+          ia2 += (__int128)yg * yg;
+        }
+      } else if (live) {
         if (me > 1) {
           for (int e = 0; e < me; ++e) ye += K.e[(size_t)e * K.n + i] * s.bulk_e[e];
         } else {
           ye = s.bulk_b0;
         }
       }
-      const double ygd = (double)yg * sc;
+      const double ygd = ifast ? 0.0 : (double)yg * sc;
       double yh = 0;
-      if (live && (mode & BULK_PVE)) {
+      if (!ifast && live && (mode & BULK_PVE)) {
         yh = stale ? yhat[i] + ye : ygd + ye;
         yhat[i] = yh;
         ymax = fmax(ymax, fabs(yh));
       }
-      if (live && (mode & (BULK_PVE | BULK_ALPHA))) {
+      if (!ifast && live && (mode & (BULK_PVE | BULK_ALPHA))) {
         s1g += ygd;
         s2g += ygd * ygd;
         if (mode & BULK_ALPHA) {
@@ -1807,27 +2532,64 @@ __device__ void bulk_phase(const DevConst& K, int c, MoveShared& s, BulkCols& bc
     }
   }
   // block reduction
-  double v6[6] = {s1g, s2g, s1e, s2e, s1t, s2t};
   const int w = tid >> 5, ln = tid & 31;
-  for (int q = 0; q < 6; ++q) {
-    double r = warp_sum_d(v6[q]);
-    if (ln == 0) s.bd[w][q] = r;
+  if (ifast) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long a0 = __shfl_xor_sync(FULL_MASK, (unsigned long long)ia, o);
+      const unsigned long long a1 = __shfl_xor_sync(FULL_MASK, (unsigned long long)(ia >> 64), o);
+      const unsigned long long b0 = __shfl_xor_sync(FULL_MASK, (unsigned long long)ia2, o);
+      const unsigned long long b1 = __shfl_xor_sync(FULL_MASK, (unsigned long long)(ia2 >> 64), o);
+      ia += (__int128)(((unsigned __int128)a1 << 64) | a0);
+      ia2 += (__int128)(((unsigned __int128)b1 << 64) | b0);
+    }
+    if (ln == 0) {
+      s.bi[w][0] = (unsigned long long)ia;
+      s.bi[w][1] = (unsigned long long)(ia >> 64);
+      s.bi[w][2] = (unsigned long long)ia2;
+      s.bi[w][3] = (unsigned long long)(ia2 >> 64);
+    }
+  } else {
+    double v6[6] = {s1g, s2g, s1e, s2e, s1t, s2t};
+    for (int q = 0; q < 6; ++q) {
+      double r = warp_sum_d(v6[q]);
+      if (ln == 0) s.bd[w][q] = r;
+    }
+    for (int o = 16; o > 0; o >>= 1) ymax = fmax(ymax, __shfl_xor_sync(FULL_MASK, ymax, o));
+    if (ln == 0) s.bmax[w] = ymax;
   }
   long long rs = warp_sum_ll(rsum);
   if (ln == 0) s.bl[w][0] = rs;
-  for (int o = 16; o > 0; o >>= 1) ymax = fmax(ymax, __shfl_xor_sync(FULL_MASK, ymax, o));
-  if (ln == 0) s.bmax[w] = ymax;
   __syncthreads();
   if (tid == 0) {
-    for (int q = 0; q < 6; ++q) {
-      double t = 0;
-      for (int ww = 0; ww < (nth >> 5); ++ww) t += s.bd[ww][q];
-      s.bsum[q] = t;
+    if (ifast) {
+      __int128 ta = 0, tb = 0;
+      for (int ww = 0; ww < (nth >> 5); ++ww) {
+        ta += (__int128)(((unsigned __int128)s.bi[ww][1] << 64) | s.bi[ww][0]);
+        tb += (__int128)(((unsigned __int128)s.bi[ww][3] << 64) | s.bi[ww][2]);
+      }
+      // sum x'b and sum (x'b)^2 at the scales 2^-sh and 2^-2sh; the
+      // covariate part is the constant b0 on each of the sample's n
+      const double s1 = i128_to_double(ta) * sc, s2 = i128_to_double(tb) * (sc * sc);
+      const double b0 = s.bulk_b0, nn = P.n;
+      s.bsum[0] = s1;
+      s.bsum[1] = s2;
+      s.bsum[2] = nn * b0;
+      s.bsum[3] = nn * b0 * b0;
+      s.bsum[4] = s1 + nn * b0;
+      s.bsum[5] = s2 + 2.0 * b0 * s1 + nn * b0 * b0;
+      s.bmax[0] = 0.0;
+    } else {
+      for (int q = 0; q < 6; ++q) {
+        double t = 0;
+        for (int ww = 0; ww < (nth >> 5); ++ww) t += s.bd[ww][q];
+        s.bsum[q] = t;
+      }
     }
     long long t = 0;
     for (int ww = 0; ww < (nth >> 5); ++ww) t += s.bl[ww][0];
     s.bsuml[0] = t;
-    if (mode & BULK_PVE) {
+    if ((mode & BULK_PVE) && !ifast) {
       double m = 0;
       for (int ww = 0; ww < (nth >> 5); ++ww) m = fmax(m, s.bmax[ww]);
       s.chs.yhat_absmax = m;
@@ -1934,7 +2696,7 @@ __device__ void prep_rb(Warp& W, bool scan_only)
     rp->mr = (double)W.s.bsuml[0] * ldexp(1.0, -W.s.bulk_s) / W.P.n;
     for (int t = 0; t < 4; ++t) {
       rp->itv[t] = ch->inv_t2a2[t];
-      rp->nlog_itv[t] = -log(ch->inv_t2a2[t]);
+      rp->nlog_itv[t] = -flog(ch->inv_t2a2[t]);
     }
     // the same constants as FP32 pairs for the double-float posterior
     rp->scale_f = (float)rp->scale;

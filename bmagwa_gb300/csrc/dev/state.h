@@ -26,6 +26,7 @@
 #define BMG_REBUILD_TILE 4096    /* in-order positions per CTA of the prefix rebuild */
 #define BMG_MAX_MS 255
 #define BMG_REMSET_MAX 1280      /* in-model SNPs + moved SNPs for dd_rem */
+#define BMG_DR_MAX 16            /* delayed rejection: largest move whose 2^m sub-models are enumerated */
 
 // One model (bmagwa::Model, src/model.hpp:394-423) of one chain.
 // Matrices are column-major with leading dimension km (max_model_size).
@@ -305,6 +306,18 @@ struct DevConst {
   uint32_t n_pad;       // individuals padded to the scan's K multiple
   uint32_t limbs_n;     // L
   uint32_t wait_limit;  // polls of a main-loop mbarrier wait of the tensor-core scan (0: the default)
+  // delayed rejection (src/sampler.cpp:882-1049, src/model.hpp:585-844): the
+  // exhaustive model of each chain (a copy of the proposed model whose last m
+  // terms are permuted to visit all 2^m sub-models) and the sub-models' log
+  // probabilities
+  uint32_t dr;          // min(delay_rejection, max_move_size); 0: off
+  double* dr_l;         // chains x km (km + 1) / 2: packed upper factor
+  double* dr_v;         // chains x km
+  double* dr_inv;       // chains x km: prior precision per column
+  uint8_t* dr_ti;       // chains x km: type index per locus
+  uint32_t* dr_x1;      // chains x km: first column of each locus
+  uint32_t* dr_x2;      // chains x km: second column (AH)
+  double* dr_pm;        // chains x 2^dr
   DevTrace tr;
 };
 

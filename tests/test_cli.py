@@ -3,6 +3,7 @@
 option and data errors with the reference's messages, and options the GPU
 path does not run, all reported before a CUDA call is made."""
 import os
+import re
 import subprocess
 
 import pytest
@@ -45,11 +46,18 @@ def test_data_error_is_the_reference_message(tmp_path):
 
 
 def test_unsupported_option_stops_before_sampling(tmp_path):
-    z = H.golden("ref_small_dr")
+    """A sampler type other than PMV (the reference's NK, KSC and G samplers
+    are not on this path) stops the command before any trace file is
+    written."""
+    z = H.golden("ref_small")
     ini = H.materialize(z, tmp_path)
+    txt = open(ini).read()
+    txt = re.sub(r"(?m)^type\s*=.*$", "type = NK", txt) if re.search(r"(?m)^type\s*=", txt) else \
+        txt.replace("[sampler]", "[sampler]\ntype = NK", 1)
+    open(ini, "w").write(txt)
     r = run(ini)
     assert r.returncode == 1
-    assert "delayed rejection" in r.stderr
+    assert "PMV" in r.stderr, r.stderr
     assert not any(f.endswith(".dat") for f in os.listdir(tmp_path / "out"))
 
 

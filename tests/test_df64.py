@@ -73,3 +73,20 @@ def test_random_stream(tmp_path):
         assert abs(var - a) < 6 * ((3 * a * a + 6 * a - a * a) / m) ** 0.5, a
     assert f["gamma_nan"] == 0
     assert f["slot_addressable"] == 1
+
+
+def test_table_driven_log_of_the_move_kernel(tmp_path):
+    """flog (bmagwa_gb300/csrc/dev/flog.h), the move kernel's logarithm:
+    within 1.5 ulp of the long-double log over the double range, in [0.5, 2],
+    near 1 and at the table's break points; special values as log()."""
+    cxx = shutil.which("g++")
+    if not cxx:
+        pytest.skip("no C++ compiler")
+    exe = str(tmp_path / "flog_check")
+    subprocess.run([cxx, "-O2", "-std=c++17", "-ffp-contract=off", os.path.join(HERE, "flog_check.cpp"), "-o", exe],
+                   check=True)
+    out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout
+    err = {k: float(v) for k, v in (line.split() for line in out.split("\n") if line.strip())}
+    for k in ("random", "near1", "unit", "breaks"):
+        assert err[k] <= 1.5, (k, out)
+    assert err["special"] == 1, out

@@ -378,17 +378,19 @@ def test_unused_bits_of_a_rows_last_byte_are_ignored(bmg, tmp_path):
             np.testing.assert_array_equal(a.chain(c)[key], b.chain(c)[key])
 
 
-def test_gpu_posterior_matches_exact_enumeration(bmg, oracle):
+@pytest.mark.parametrize("dr", [0, 3], ids=["plain", "delayed_rejection"])
+def test_gpu_posterior_matches_exact_enumeration(bmg, oracle, dr):
     """The GPU sampler's Rao-Blackwellised inclusion probabilities on the 7-SNP
     model space of src/tests/testdata/small_modelspace_tau2.ini (tau2 and
     alpha held after the start) equal the exact posterior over all 2^7 models
     within 0.005 after 200k iterations (SamplerTestsF.SmallModelSpaceWithSharedTau2,
-    src/tests/sampler_tests.hpp:348-446).  The exact posterior is enumerated
-    by the oracle at the precision the chain drew at its start."""
+    src/tests/sampler_tests.hpp:348-446), with and without delayed rejection.
+    The exact posterior is enumerated by the oracle at the precision the chain
+    drew at its start."""
     z = H.golden("data_tests")
     packed, y = z["small_bed"][3:], z["small_y"]
     n_iter = 200000
-    o = H.small_modelspace_opts(bmg, n_iter, 0, 1245)
+    o = H.small_modelspace_opts(bmg, n_iter, dr, 1245)
     port = oracle.Port(o, packed, y)
     port.run(1)
     pip = H.exact_pips(port)

@@ -1,7 +1,10 @@
 """GPU parity against the reference's traces for the options the main parity
 file does not cover: the flat proposal with the beta trace and raw
 genotypes, a model past the 128 columns kept in shared memory, individual
-tau2 over five effect types, and the command-line entry end to end."""
+tau2 over five effect types, delayed rejection (the second stage over all
+sub-models of a rejected multi-SNP or state-change move: one and two effect
+types, and the reference example's delay_rejection = 10 with covariates), and
+the command-line entry end to end."""
 import numpy as np
 import pytest
 
@@ -11,13 +14,15 @@ from test_gpu_parity import RTOL, run_gpu
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("name", ["small_flat", "example_flat", "example_large", "example_types_indiv"])
+@pytest.mark.parametrize("name", ["small_flat", "example_flat", "example_large", "example_types_indiv",
+                                  "small_dr", "example_dr", "small_types_dr"])
 def test_gpu_matches_reference_more_options(bmg, tmp_path, name):
     """A flat proposal with the beta trace and raw genotypes (small_flat,
     example_flat), a model that grows past the 128 columns the move kernel
-    keeps in shared memory (example_large), and individual tau2 draws over
-    four terms in the scan (example_types_indiv), against the reference's
-    traces."""
+    keeps in shared memory (example_large), individual tau2 draws over four
+    terms in the scan (example_types_indiv) and delayed rejection (small_dr,
+    example_dr, small_types_dr: src/sampler.cpp:882-1049,
+    src/sampler.hpp:929-1098, 1547-1618), against the reference's traces."""
     z = H.golden("ref_" + name)
     ini = H.materialize(z, tmp_path)
     opt = bmg.options_from_ini(ini)

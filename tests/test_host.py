@@ -205,7 +205,7 @@ def test_create_rejects_unsupported_options_before_touching_the_device(tmp_path)
     h = C.c_void_p()
     L = bg.lib()
     for field, value, status in [("max_SNP_neighborhood_size", 129, "BMG_EINVAL"),
-                                 ("delay_rejection", 10, "BMG_EUNSUPPORTED"),
+                                 ("delay_rejection", 17, "BMG_EUNSUPPORTED"),
                                  ("sampler_type", 1, "BMG_EUNSUPPORTED")]:
         old = getattr(o, field)
         setattr(o, field, value)
