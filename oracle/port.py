@@ -32,9 +32,22 @@ def build(verbose=False):
     return PORT_LIB
 
 
+def reference_dir():
+    """Where the reference tree is: $BMAGWA_REFERENCE, else the REF default of
+    oracle/Makefile (the recipe that compiles it)."""
+    env = os.environ.get("BMAGWA_REFERENCE")
+    if env:
+        return env
+    with open(os.path.join(HERE, "Makefile")) as f:
+        for line in f:
+            if line.startswith("REF ?="):
+                return line.split("=", 1)[1].strip()
+    return ""
+
+
 def build_reference():
     """Compile the reference sources (needs the reference tree) into oracle/_ref."""
-    subprocess.run(["make", "-s", "-C", HERE, "-j8"], check=True)
+    subprocess.run(["make", "-s", "-C", HERE, "-j8", "REF=" + reference_dir()], check=True)
     return REF_BIN
 
 

@@ -137,11 +137,28 @@ struct Data {
     b = (uint8_t)((b & ~(3 << sh)) | (code << sh));
   }
   /* src/data.cpp:56-138 */
+  /* four individuals per code byte from a table per term (the reference's
+     genotype_tables.hpp lookups); the values are code_value()'s */
   void get_genotypes(int type, size_t snp, double* v) const
   {
+    static double tab[4][256][4];
+    static bool ready = false;
+    if (!ready) {
+      for (int t = 0; t < 4; ++t)
+        for (int b = 0; b < 256; ++b)
+          for (int q = 0; q < 4; ++q) tab[t][b][q] = code_value((b >> (2 * q)) & 3, t);
+      ready = true;
+    }
     const uint8_t* row = &g[stride * snp];
-    for (size_t i = 0; i < n; ++i)
-      v[i] = code_value((row[i / 4] >> (2 * (i % 4))) & 3, type);
+    const size_t full = n / 4;
+    for (size_t w = 0; w < full; ++w) {
+      const double* e = tab[type][row[w]];
+      v[4 * w] = e[0];
+      v[4 * w + 1] = e[1];
+      v[4 * w + 2] = e[2];
+      v[4 * w + 3] = e[3];
+    }
+    for (size_t i = 4 * full; i < n; ++i) v[i] = code_value((row[i / 4] >> (2 * (i % 4))) & 3, type);
   }
 
   Data(size_t n_, size_t m_g_, size_t m_e_, const uint8_t* packed, const double* y_,

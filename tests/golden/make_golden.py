@@ -25,7 +25,12 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+sys.path.insert(0, ROOT)
+from oracle.port import reference_dir  # noqa: E402
+
+# the reference tree: the first argument, else $BMAGWA_REFERENCE, else the
+# oracle recipe's default location
+REF = sys.argv[1] if len(sys.argv) > 1 else reference_dir()
 REF_BIN = os.path.join(ROOT, "oracle", "_ref", "bmagwa_ref")
 REF_PROBE = os.path.join(ROOT, "oracle", "_ref", "ref_probe")
 
