@@ -80,7 +80,7 @@ struct MoveShared {
   int n_done;
   double bulk_b0;       // constant-term coefficient
   long long bulk_b0i;
-  double bulk_e[8];     // covariate coefficients (m_e <= 8 in bulk phases)
+  double bulk_e[BMG_MAX_COV + 1];  // covariate coefficients (the constant first)
   double yhat_given_max;  // max |y_hat| of a residual from given fitted values (BULK_YHAT)
   // n-wide products of warp 0's move, handed to all eight warps (help jobs)
   int job_kind;
@@ -2637,7 +2637,7 @@ __device__ void bulk_setup(Warp& W, BulkCols& bc, int mode)
     W.s.bulk_s = sh;
     W.s.bulk_b0 = (bl > 0) ? M->beta[0] : 0.0;
     W.s.bulk_b0i = __double2ll_rn(W.s.bulk_b0 * scl);
-    for (int e = 0; e < 8; ++e) W.s.bulk_e[e] = (e < me && e < bl) ? M->beta[e] : 0.0;
+    for (int e = 0; e <= BMG_MAX_COV; ++e) W.s.bulk_e[e] = (e < me && e < bl) ? M->beta[e] : 0.0;
   }
   __syncwarp();
 }

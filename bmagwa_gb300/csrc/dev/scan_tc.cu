@@ -67,12 +67,14 @@ bmg_scan_tc_kernel(DevConst K, TcParams P, const __grid_constant__ CUtensorMap m
     const uint32_t c_lo = part * ct / nparts, c_hi = (part + 1) * ct / nparts;
     const uint32_t col_lo = c_lo * L, col_hi = c_hi * L;
     const uint32_t ethreads = 32 * TC_EPI_WARPS;
-    for (uint32_t i = 0; i < my_tiles; ++i) {
+    const uint32_t n_seg = tc_n_seg(P);
+    for (uint32_t job = 0; job < my_tiles * n_seg; ++job) {
+      const uint32_t i = job / n_seg, seg = job % n_seg;
       const uint32_t tile = blockIdx.x + i * gridDim.x;
       const uint32_t snp0 = (tile % P.m_tiles) * P.snps_per_tile;
       const uint32_t chain0 = (tile / P.m_tiles) * ct;
       const uint32_t chains_here = min(ct, K.n_chains - chain0);
-      const uint32_t b = i % P.n_acc, u = i / P.n_acc;
+      const uint32_t b = job % P.n_acc, u = job / P.n_acc;
       // one warp waits; the outcome is shared so that all epilogue warps take
       // the same number of named-barrier steps
       if (e == 0) {
@@ -101,7 +103,9 @@ bmg_scan_tc_kernel(DevConst K, TcParams P, const __grid_constant__ CUtensorMap m
             // |D| < 2^24: an exact float integer, converted through int32
             acc += (long long)__float2int_rn(v[q]) * (1ll << (8 * limb));
             if (++limb == L) {
-              xr_s[row * xs + chain] = acc;
+              // the first K segment sets the exact sum, later ones add to it
+              if (seg == 0) xr_s[row * xs + chain] = acc;
+              else xr_s[row * xs + chain] += acc;
               acc = 0;
               limb = 0;
               ++chain;
@@ -113,6 +117,7 @@ bmg_scan_tc_kernel(DevConst K, TcParams P, const __grid_constant__ CUtensorMap m
       __syncwarp();
       if (lane == 0) mbar_arrive(&ctl.acc_empty[b]);
       named_bar_sync(1, ethreads);
+      if (seg + 1 < n_seg) continue;  // the posterior waits for the tile's last segment
       // one unit per (SNP, chain), SNPs fastest so that a warp's stores to
       // the chain-major running means are contiguous; two units per step
       const uint32_t units = P.snps_per_tile * chains_here;
@@ -186,9 +191,13 @@ static bool tc_plan(const DevConst* K, TcParams* P, uint32_t ct_cap, uint32_t n_
   P->snps_per_tile = TC_BM / P->tpad;
   for (uint32_t u = 0; u < 4; ++u) P->term_of_row[u] = (u < T) ? K->term_of[u] : -1;
   const uint32_t L = K->limbs_n;
-  if (K->n_pad % TC_BK != 0 || K->n >= 65536) return false;  // exact FP32 sums need n < 2^16
+  if (K->n_pad % TC_BK != 0) return false;
   P->wait_limit = K->wait_limit;
   P->k_chunks = K->n_pad / TC_BK;
+  // an FP32 accumulator of products of magnitude <= 256 stays exact over at
+  // most 2^24 / 256 = 65,536 individuals: longer K ranges are closed in
+  // segments of 510 stages (65,280 individuals) and added in int64
+  P->seg_chunks = 65280 / TC_BK;
   P->pk_bytes = P->snps_per_tile * (TC_BK / 4);
   // widest chain tile whose accumulator fits one TMEM buffer and whose stages
   // (at least two) and sums fit shared memory

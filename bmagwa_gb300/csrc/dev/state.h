@@ -26,6 +26,7 @@
 #define BMG_REBUILD_TILE 4096    /* in-order positions per CTA of the prefix rebuild */
 #define BMG_MAX_MS 255
 #define BMG_REMSET_MAX 1280      /* in-model SNPs + moved SNPs for dd_rem */
+#define BMG_MAX_COV 31            /* covariates besides the constant */
 #define BMG_DR_MAX 16            /* delayed rejection: largest move whose 2^m sub-models are enumerated */
 
 // One model (bmagwa::Model, src/model.hpp:394-423) of one chain.

@@ -71,7 +71,22 @@ struct TcParams {
   uint32_t a_tmem;         // 1: A slot t at TMEM column n_acc acc_cols + t TC_A_COLS
   int32_t term_of_row[4];  // term of row u of a SNP (-1: unused)
   uint32_t wait_limit = 0;  // polls of a main-loop mbarrier wait (0: WAIT_LIMIT)
+  // K segments of a tile: each closes its own accumulator (a job), so that
+  // no FP32 partial sum runs over more than seg_chunks stages; the epilogue
+  // adds the segments' exact integers.  0: one segment of all k_chunks.
+  uint32_t seg_chunks = 0;
 };
+
+// stages of a tile's K segment s and the number of segments
+__host__ __device__ inline uint32_t tc_seg_len(const TcParams& P)
+{
+  return (P.seg_chunks && P.seg_chunks < P.k_chunks) ? P.seg_chunks : P.k_chunks;
+}
+__host__ __device__ inline uint32_t tc_n_seg(const TcParams& P)
+{
+  const uint32_t sl = tc_seg_len(P);
+  return (P.k_chunks + sl - 1) / sl;
+}
 
 // Where the accumulators and A go: A in TMEM when n_acc accumulators of n_mma
 // columns (rounded up to 32) leave room for at least two A slots; else A in
@@ -202,13 +217,16 @@ __device__ __forceinline__ void tc_main_roles(const TcParams& P, TcCtl& ctl, uin
       const uint32_t b_half = P.b_bytes / 2;
       TcRing full, aslot;  // this stage's shared-memory slot and A slot
       uint32_t dn = 0;     // done_bar slot of this stage
-      for (uint32_t i = 0; i < my_tiles && !ctl.abort_flag; ++i) {
-        const uint32_t b = i % P.n_acc, u = i / P.n_acc;
+      const uint32_t seg_len = tc_seg_len(P), n_seg = tc_n_seg(P);
+      // job = (tile, K segment): one accumulator each, in walk order
+      for (uint32_t job = 0; job < my_tiles * n_seg && !ctl.abort_flag; ++job) {
+        const uint32_t b = job % P.n_acc, u = job / P.n_acc;
+        const uint32_t k0 = (job % n_seg) * seg_len, k1 = min(nk, k0 + seg_len);
         if (u >= 1 && !mbar_wait(&ctl.acc_empty[b], (u - 1) & 1, P.wait_limit)) { ctl.abort_flag = 1; break; }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t d = tmem + b * P.acc_cols;
         bool ok = true;
-        for (uint32_t k = 0; k < nk; ++k) {
+        for (uint32_t k = k0; k < k1; ++k) {
           if (!mbar_wait(&full_bar[full.i], full.ph, P.wait_limit) ||
               !mbar_wait(&aready_bar[aslot.i], aslot.ph, P.wait_limit)) {
             ok = false;
@@ -221,13 +239,13 @@ __device__ __forceinline__ void tc_main_roles(const TcParams& P, TcCtl& ctl, uin
 #pragma unroll
             for (int kk = 0; kk < TC_BK / 16; ++kk)  // 16 bf16: 8 TMEM columns of A, 2 descriptor units of B
               mma_bf16_tmem_a(d, at + 8 * kk, smem_desc(sp + (kk >> 2) * b_half) + 2 * (kk & 3), idesc,
-                              (k | kk) != 0);
+                              ((k - k0) | kk) != 0);
           } else {
             uint8_t* a = sp + P.b_bytes;
 #pragma unroll
             for (int kk = 0; kk < TC_BK / 16; ++kk)  // 16 bf16 = 32 bytes = 2 descriptor units
               mma_bf16(d, smem_desc(a + (kk >> 2) * TC_A_SUB_BYTES) + 2 * (kk & 3),
-                       smem_desc(sp + (kk >> 2) * b_half) + 2 * (kk & 3), idesc, (k | kk) != 0);
+                       smem_desc(sp + (kk >> 2) * b_half) + 2 * (kk & 3), idesc, ((k - k0) | kk) != 0);
           }
           mma_commit(&done_bar[dn]);
           if (++dn == R) dn = 0;

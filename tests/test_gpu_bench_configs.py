@@ -62,6 +62,7 @@ def test_tc_scan_bitwise_at_the_scan_workload_shape(bmg, monkeypatch):
             monkeypatch.setenv("BMG_SCAN_VARIANT", variant)
         opt = workloads.options(wl, 1, 6)
         opt.scan_impl = scan
+        opt.scan_limbs = 6
         ctx = _ctx(bmg, opt, packed, y)
         col = ctx.run(6)
         if variant == "0":
@@ -77,18 +78,19 @@ def test_tc_scan_bitwise_at_the_scan_workload_shape(bmg, monkeypatch):
             np.testing.assert_array_equal(ref[2][c], got[2][c], err_msg="%s chain %d" % (key, c))
 
 
-def _worst_case_data(n, p, seed, two_valued):
+def _worst_case_data(n, p, seed, two_valued, limbs=6):
     """Genotypes with long runs of code 2 and a phenotype whose fixed-point
     residual has the digit 127 (or -127) in every limb below the top one.
 
     The scan runs against zero fitted values (bmg_scan_yhat), so its residual
-    is y itself, at the scale 2^44 (max |y| in (1, 2], six limbs).
-    y = v + k/16 with v = 1 + 0x7F7F7F7F7F / 2^44 puts 0x7F7F7F7F7F in the low
-    40 bits of every individual's residual: limbs 0-4 are 127 everywhere and
-    only the top limb varies (16 + k).  two_valued gives the second half of
-    the individuals -y instead (digits -127)."""
+    is y itself, at the scale 2^(8 L - 4) for L limbs and max |y| in (1, 2]
+    (2^44 for six limbs).  y = v + k/16 with v = 1 + 0x7F...7F / 2^(8 L - 4)
+    (L - 1 bytes 0x7F) puts 0x7F in every byte of the low 8 (L - 1) bits of
+    every individual's residual: the low limbs are 127 everywhere and only
+    the top limb varies (16 + k).  two_valued gives the second half of the
+    individuals -y instead (digits -127)."""
     rng = np.random.default_rng(seed)
-    v = 1.0 + float(0x7F7F7F7F7F) / 2.0 ** 44
+    v = 1.0 + float(int("7F" * (limbs - 1), 16)) / 2.0 ** (8 * limbs - 4)
     k = rng.integers(-3, 4, n)
     y = v + k / 16.0
     sign = np.ones(n)
@@ -111,8 +113,9 @@ def _worst_case_data(n, p, seed, two_valued):
     return _pack_codes(G), y
 
 
+@pytest.mark.parametrize("limbs", [5, 6])
 @pytest.mark.parametrize("two_valued", [False, True], ids=["one_signed", "two_valued"])
-def test_tc_scan_exact_near_the_fp32_bound(bmg, oracle, two_valued):
+def test_tc_scan_exact_near_the_fp32_bound(bmg, oracle, two_valued, limbs):
     """n = 65,000 (the tensor-core scan takes n below 65,536): with digits of
     magnitude 127 in every low limb, the FP32 partial sums over a column of
     2s reach 2 x 127 x 65,000 = 16,510,000 (2^24 = 16,777,216) for the
@@ -122,13 +125,14 @@ def test_tc_scan_exact_near_the_fp32_bound(bmg, oracle, two_valued):
     same fitted values and sigma2) to 1e-9."""
     from bmagwa_gb300 import workloads
     n, p = 65000, 512
-    packed, y = _worst_case_data(n, p, 3, two_valued)
+    packed, y = _worst_case_data(n, p, 3, two_valued, limbs)
     wl = dict(workloads.WORKLOADS["plain"], n=n, p=p, chains=2, n_rao=1)
     zero = np.zeros(n)
     out = {}
     for scan in (1, 0):
         opt = workloads.options(wl, 5, 1)
         opt.scan_impl = scan
+        opt.scan_limbs = limbs
         ctx = _ctx(bmg, opt, packed, y)
         out[scan] = ctx.scan_yhat(zero, 1.0)
         ctx.close()
@@ -166,6 +170,7 @@ def test_two_n_tiles_of_masked_phenotypes(bmg, oracle, tmp_path):
     for scan in (1, 0):
         opt = workloads.options(wl, 3, iters)
         opt.scan_impl = scan
+        opt.scan_limbs = 6  # 42 chains of 6 limbs fill one N tile
         opt.adapt_p_move_size = 0  # early tuning ties break on last bits of exp
         ctx = _ctx(bmg, opt, packed, Y, masks)
         col = ctx.run(iters)
@@ -206,3 +211,39 @@ def test_gpu_matches_oracle_at_the_measured_workloads(bmg, oracle, name, iters, 
     for c in range(oracle_chains):
         H.compare(colp.chain(c), colg.chain(c), rtol=RTOL, label="%s chain %d" % (name, c))
         np.testing.assert_allclose(rao_g[c], port.rao(c)[0], rtol=RTOL, atol=1e-12)
+
+
+@pytest.mark.parametrize("n", [70000, 140000])
+def test_tc_scan_beyond_65536_individuals(bmg, oracle, n):
+    """Above 65,535 individuals the tensor-core scan closes its FP32
+    accumulator every 65,280 individuals (a K segment) and adds the
+    segments' exact integers in int64: two and three segments here.  The
+    traces and in-loop posteriors equal the SIMT scan's bit for bit and the
+    oracle's chain to 1e-9."""
+    from bmagwa_gb300 import synth, workloads
+    p, iters = 1200, 12
+    wl = dict(workloads.WORKLOADS["plain"], n=n, p=p, chains=2, n_rao=2, ld_block=50)
+    counts, _ = synth.genotypes(n, p, 50, 17, device="cuda")
+    y, _, _ = synth.phenotype(counts, 8, 0.3, 0, 17, device="cuda")
+    packed = synth.pack(counts).cpu().numpy().reshape(-1)
+    del counts
+    res = {}
+    for scan in (1, 0):
+        opt = workloads.options(wl, 7, iters)
+        opt.scan_impl = scan
+        opt.adapt_p_move_size = 0
+        ctx = _ctx(bmg, opt, packed, y)
+        col = ctx.run(iters)
+        res[scan] = ([col.chain(c) for c in range(2)], [ctx.last_scan(c)[0] for c in range(2)],
+                     [ctx.rao(c)[0] for c in range(2)])
+        ctx.close()
+    for c in range(2):
+        H.compare(res[1][0][c], res[0][0][c], rtol=0.0, label="chain %d" % c)
+        np.testing.assert_array_equal(res[1][1][c], res[0][1][c])
+    opt = workloads.options(wl, 7, iters)
+    opt.adapt_p_move_size = 0
+    port = oracle.Port(opt, packed, y)
+    colp = port.run(iters, threads=2)
+    for c in range(2):
+        H.compare(colp.chain(c), res[0][0][c], rtol=RTOL, label="oracle chain %d" % c)
+        np.testing.assert_allclose(res[0][2][c], port.rao(c)[0], rtol=RTOL, atol=1e-12)

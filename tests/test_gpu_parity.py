@@ -398,3 +398,23 @@ def test_gpu_posterior_matches_exact_enumeration(bmg, oracle, dr):
     rao, _ = ctx.rao(0)
     np.testing.assert_allclose(rao, pip, rtol=0, atol=0.005)
 
+
+
+def test_many_covariates_match_the_oracle(bmg, oracle, tmp_path):
+    """Twelve covariates besides the constant (the reference reads any m_e,
+    src/data.cpp:202-243): the chains equal the oracle's."""
+    opt, packed, y, _ = synth_case(bmg, tmp_path, "plain", n=800, p=2000, chains=2, iters=200, n_rao=5)
+    n, me = int(opt.n), 12
+    rng = np.random.default_rng(3)
+    e = rng.normal(size=(me, n))
+    y2 = y + 0.3 * e[0] - 0.2 * e[3] + 0.1 * e[11]
+    opt.m_e = me
+    opt.adapt_p_move_size = 0  # early tuning ties break on last bits of exp
+    ecol = np.ascontiguousarray(e.reshape(-1))
+    port = oracle.Port(opt, packed, y2, ecol)
+    colp = port.run(200)
+    ctx, colg = run_gpu(bmg, opt, packed, y2, ecol, 200)
+    for c in range(opt.n_chains):
+        H.compare(colp.chain(c), colg.chain(c), rtol=RTOL, label="chain %d" % c)
+        np.testing.assert_allclose(ctx.rao(c)[0], port.rao(c)[0], rtol=RTOL, atol=1e-12)
+    ctx.close()
