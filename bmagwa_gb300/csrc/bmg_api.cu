@@ -43,6 +43,7 @@ extern "C" __global__ void bmg_gsum_kernel(const uint8_t* geno, uint64_t n, uint
 extern "C" __global__ void bmg_init_kernel(DevConst K);
 extern "C" __global__ void bmg_rbprep_kernel(DevConst K, int from_yhat, double yhat_absmax);
 extern "C" __global__ void bmg_set_sigma2_kernel(DevConst K, double sigma2);
+extern "C" __global__ void bmg_miss_scan_kernel(DevConst K);
 extern "C" __global__ void bmg_move_kernel(DevConst K, int max_iters);
 extern "C" __global__ void bmg_scan_simt_kernel(DevConst K, const int64_t* resid_t);
 extern "C" __global__ void bmg_resid_transpose_kernel(DevConst K, int64_t* resid_t);
@@ -145,6 +146,9 @@ struct bmg_ctx {
   uint64_t graph_launches = 0;                 // kernels in the captured chunk
   double* lml_buf = nullptr;                   // per-SNP log odds of the scans (bmg_scan_logodds, learned proposal)
   double* yhat_given = nullptr;                // chains x n fitted values of bmg_scan_yhat
+  std::vector<int64_t> miss_off;               // missing calls per SNP (CSR offsets, p + 1)
+  std::vector<uint32_t> miss_ind;              // their individuals
+  std::vector<double> miss_prior;              // p x 3 cumulative counts of the calls 0, 1, 2
   uint32_t wait_limit = 0;                     // main-loop wait bound of the tensor-core scan (0: default)
   uint32_t dr = 0;                             // delayed rejection: largest move enumerated (0: off)
   int32_t* adam_t = nullptr;                   // learned proposal: optimiser step counter (device)
@@ -466,23 +470,44 @@ extern "C" bmg_status bmg_load_bed(bmg_ctx* ctx, const uint8_t* packed, uint64_t
   CK(cudaMemcpyAsync(ctx->cnt_h.data(), cnt, 8 * p, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaMemcpyAsync(miss_h.data(), miss, 4 * p, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
-  for (uint64_t j = 0; j < p; ++j)
-    if (miss_h[j] != 0)
-      throw bmg_error(BMG_EUNSUPPORTED, "missing genotype calls are not on the GPU path (SNP " +
-                                            std::to_string(j) + ")");
-  /* src/data.cpp:403-434 from the counts (no missing calls) */
+  // missing calls (src/data.cpp:341-376): per SNP the individuals without a
+  // call, ascending (CSR), and the cumulative counts of the calls 0, 1, 2
+  // after the recode, the prior of their imputation
+  ctx->miss_off.assign(p + 1, 0);
+  for (uint64_t j = 0; j < p; ++j) ctx->miss_off[j + 1] = ctx->miss_off[j] + miss_h[j];
+  const uint64_t G = (uint64_t)ctx->miss_off[p];
+  ctx->miss_ind.clear();
+  ctx->miss_prior.clear();
+  if (G) {
+    ctx->miss_ind.resize(G);
+    ctx->miss_prior.assign(3 * p, 0.0);
+    for (uint64_t j = 0; j < p; ++j) {
+      const double n1 = ctx->cnt_h[2 * j], n2 = ctx->cnt_h[2 * j + 1];
+      const double n0 = (double)n - miss_h[j] - n1 - n2;
+      ctx->miss_prior[3 * j] = n0;
+      ctx->miss_prior[3 * j + 1] = n0 + n1;
+      ctx->miss_prior[3 * j + 2] = n0 + n1 + n2;
+      if (!miss_h[j]) continue;
+      const uint8_t* row = packed + j * stride;
+      int64_t q = ctx->miss_off[j];
+      for (uint64_t i = 0; i < n; ++i)
+        if (((row[i >> 2] >> (2 * (i & 3))) & 3) == 1) ctx->miss_ind[q++] = (uint32_t)i;
+    }
+  }
+  /* src/data.cpp:403-434 from the counts over each SNP's calls */
   double total_var = 0, total_mean = 0;
   uint64_t nv = 0, nm = 0;
   for (uint64_t j = 0; j < p; ++j) {
     double n1 = ctx->cnt_h[2 * j], n2 = ctx->cnt_h[2 * j + 1];
     double sq = n1 + 4.0 * n2, s = n1 + 2.0 * n2;
-    double ng = (double)n;
-    if (n > 1) {
+    const uint64_t ngi = n - (uint64_t)miss_h[j];
+    double ng = (double)ngi;
+    if (ngi > 1) {
       total_mean += s / ng;
       total_var += (sq - s * s / ng) / (ng - 1);
       ++nm;
       ++nv;
-    } else {
+    } else if (ngi == 1) {
       total_mean += s / ng;
       ++nm;
     }
@@ -1058,6 +1083,41 @@ extern "C" bmg_status bmg_precompute(bmg_ctx* ctx)
   K.limbs = ctx->dalloc<uint16_t>((size_t)C * ctx->L * ctx->n_pad);
   ctx->resid_t = ctx->dalloc<int64_t>((size_t)C * ctx->n_pad);
   K.scratch = ctx->dalloc<double>((size_t)C * 2 * km);
+  // missing calls: the CSR, the imputation prior and every chain's values
+  // (all 0 at the start, as the reference's DataModel starts them)
+  K.miss_total = ctx->miss_ind.size();
+  K.miss_snps = 0;
+  if (K.miss_total) {
+    if (ctx->multi) throw bmg_error(BMG_EUNSUPPORTED, "missing genotype calls with several phenotypes are not on this path");
+    std::vector<int32_t> rank(p, -1);
+    std::vector<uint32_t> list;
+    for (uint64_t j = 0; j < p; ++j)
+      if (ctx->miss_off[j + 1] > ctx->miss_off[j]) {
+        rank[j] = (int32_t)list.size();
+        list.push_back((uint32_t)j);
+      }
+    K.miss_snps = (uint32_t)list.size();
+    int64_t* off = ctx->dalloc<int64_t>(p + 1, false);
+    uint32_t* ind = ctx->dalloc<uint32_t>(K.miss_total, false);
+    double* pri = ctx->dalloc<double>(3 * p, false);
+    int32_t* rk = ctx->dalloc<int32_t>(p, false);
+    uint32_t* ls = ctx->dalloc<uint32_t>(list.size(), false);
+    CK(cudaMemcpyAsync(off, ctx->miss_off.data(), 8 * (p + 1), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ind, ctx->miss_ind.data(), 4 * K.miss_total, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(pri, ctx->miss_prior.data(), 8 * 3 * p, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(rk, rank.data(), 4 * p, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ls, list.data(), 4 * list.size(), cudaMemcpyHostToDevice, ctx->stream));
+    K.miss_off = off;
+    K.miss_ind = ind;
+    K.miss_prior = pri;
+    K.miss_rank = rk;
+    K.miss_list = ls;
+    K.miss_val = ctx->dalloc<uint8_t>((size_t)C * K.miss_total);
+    K.miss_corr = ctx->dalloc<MissCorr>((size_t)C * list.size());
+    K.miss_fit = ctx->dalloc<long long>((size_t)C * ctx->n_pad);
+    K.miss_yh = ctx->dalloc<double>((size_t)C * n);
+    K.miss_inm = ctx->dalloc<long long>((size_t)C * 2 * km);
+  }
   K.dr = ctx->dr;
   if (ctx->dr) {
     K.dr_l = ctx->dalloc<double>((size_t)C * km * (km + 1) / 2);
@@ -1187,6 +1247,12 @@ extern "C" bmg_status bmg_get_precomputed(bmg_ctx* ctx, double* xx, uint32_t* of
 static void launch_scan(bmg_ctx* ctx)
 {
   DevConst& K = ctx->K;
+  if (K.miss_total) {
+    // the missing calls' part of the scan (imputation outside the model)
+    dim3 g((K.miss_snps + 7) / 8, ctx->C);
+    bmg_miss_scan_kernel<<<g, 256, 0, ctx->stream>>>(K);
+    LAUNCHED(ctx, "bmg_miss_scan_kernel");
+  }
   bool tc = ctx->opt.scan_impl == BMG_SCAN_TCGEN05 && bmg_scan_tc_supported(&K);
   if (tc) {
     int v = ctx->tc_forced >= 0 ? ctx->tc_forced : ctx->tc_variant;
@@ -1606,6 +1672,7 @@ extern "C" bmg_status bmg_scan_schur(bmg_ctx* ctx, double* dlml)
   API_BEGIN
   check_ready(ctx);
   if (ctx->multi) throw bmg_error(BMG_EUNSUPPORTED, "the Schur scan needs one phenotype per context");
+  if (ctx->K.miss_total) throw bmg_error(BMG_EUNSUPPORTED, "the Schur scan does not take missing genotype calls");
   const uint32_t C = ctx->C;
   const size_t out_n = (size_t)C * ctx->p * ctx->K.n_terms;
   if (!ctx->schur_out) ctx->schur_out = ctx->dalloc<double>(out_n, false);

@@ -44,6 +44,21 @@ __device__ __forceinline__ int geno_code(const uint8_t* row, uint64_t i)
   return (row[i >> 2] >> ((i & 3) * 2)) & 3;
 }
 
+// a genotype 0/1/2 in term coding t (A, H, D, R; src/genotype_tables.hpp)
+__device__ __forceinline__ int gval_term(int g, int t)
+{
+  return t == 0 ? g : (t == 1 ? (g == 1) : (t == 2 ? (g > 0) : (g == 2)));
+}
+
+// imputed genotype of a missing call from the cumulative counts of the SNP's
+// calls (DataModel::sample_missing, src/data_model.cpp:78-103, one uniform
+// through Utils::sample_discrete_naive, src/utils.cpp:46-57)
+__device__ __forceinline__ int miss_draw(const double* mp, double u)
+{
+  const double r = u * mp[2];
+  return r < mp[0] ? 0 : (r < mp[1] ? 1 : 2);
+}
+
 // genotype value of a term coding from a 2-bit code (00->0, 10->1, 11->2;
 // src/data.cpp:36 and src/genotype_tables.hpp).  Missing codes never reach
 // the device path (they are rejected at load).

@@ -15,6 +15,13 @@ static __device__ __forceinline__ bool in_model(const DevConst& K, int c, uint64
   return (K.inbits[(size_t)c * ((K.p + 31) / 32) + (j >> 5)] >> (j & 31)) & 1u;
 }
 
+// a SNP outside the model and without missing calls: the fast posterior
+// applies (SNPs with missing calls take rb_epilogue and their corrections)
+static __device__ __forceinline__ bool rb_plain(const DevConst& K, int c, uint64_t j)
+{
+  return !in_model(K, c, j) && !(K.miss_total && K.miss_rank[j] >= 0);
+}
+
 // The common case: one non-AH effect type and the chain's shared tau2.  For
 // a SNP outside the model the posterior needs no branch, so a thread can
 // evaluate two (SNP, chain) units back to back and their FP64 chains overlap.
@@ -118,8 +125,13 @@ static __device__ __noinline__ void rb_epilogue(const DevConst& K, int c, uint64
   const RbParams& rp = K.rb[c];
   const DevPheno& P = K.ph[K.pheno_of[c]];
   const double n = P.n;
+  // the SNP's missing calls at their imputed values (DataModel overlay,
+  // src/data_model.cpp:30-72, and update_prexx_cov, :105-167)
+  const MissCorr* mc = nullptr;
+  if (K.miss_total && K.miss_rank[j] >= 0) mc = &K.miss_corr[(size_t)c * K.miss_snps + K.miss_rank[j]];
   double xr[4];
-  for (int t = 0; t < 4; ++t) xr[t] = K.allow_terms[t] ? (double)xr_by_type[t] * rp.scale : 0.0;
+  for (int t = 0; t < 4; ++t)
+    xr[t] = K.allow_terms[t] ? (double)(xr_by_type[t] + (mc ? mc->dxr[t] : 0ll)) * rp.scale : 0.0;
   double mr = rp.mr;
   double itv[4] = {rp.itv[0], rp.itv[1], rp.itv[2], rp.itv[3]};
   if (K.use_individual_tau2) {
@@ -150,21 +162,22 @@ static __device__ __noinline__ void rb_epilogue(const DevConst& K, int c, uint64
       else itv[type] = M.inv[x1];
     }
     // r_om = r + x_j beta_j: products and mean from the genotype counts
-    double msum = b1 * (double)term_sum(P.cnt, j, t1);
+    // (and the imputed values of the missing calls)
+    double msum = b1 * (double)(term_sum(P.cnt, j, t1) + (mc ? mc->dsum[t1] : 0));
     for (int t = 0; t < 4; ++t)
-      if (K.allow_terms[t]) xr[t] += b1 * (double)term_cross_same(P.cnt, j, t, t1);
+      if (K.allow_terms[t]) xr[t] += b1 * (double)(term_cross_same(P.cnt, j, t, t1) + (mc ? mc->dcross[t][t1] : 0));
     if (type == 4) {
       int x2 = M.x_ind2[mi];
       int t2 = M.xc_type[x2];
       double b2 = M.beta[x2];
-      msum += b2 * (double)term_sum(P.cnt, j, t2);
+      msum += b2 * (double)(term_sum(P.cnt, j, t2) + (mc ? mc->dsum[t2] : 0));
       for (int t = 0; t < 4; ++t)
-        if (K.allow_terms[t]) xr[t] += b2 * (double)term_cross_same(P.cnt, j, t, t2);
+        if (K.allow_terms[t]) xr[t] += b2 * (double)(term_cross_same(P.cnt, j, t, t2) + (mc ? mc->dcross[t][t2] : 0));
     }
     mr = mr + msum / n;
     lmp = rp.lmp_rem[type];
   }
-  const double* pre = P.pre + j * (size_t)K.offset;
+  const double* pre = mc ? mc->pre : P.pre + j * (size_t)K.offset;
   const int nt = K.n_types;
   const bool ut = nt > 1;
   double pt[5];

@@ -703,6 +703,81 @@ struct Warp {
     helpers = false;
   }
 
+  // ------------------------------------------------------ missing calls
+  // The codes hold a missing call as 01, which every product above reads as
+  // 0; the chain's imputed values (K.miss_val, the reference's DataModel
+  // overlay, src/data_model.cpp:30-72) enter through the corrections below.
+  __device__ bool has_miss(uint32_t snp) const { return K.miss_total && K.miss_off[snp + 1] > K.miss_off[snp]; }
+  __device__ int code_g(uint32_t snp, uint32_t i) const
+  {
+    const int code = (K.geno[(size_t)snp * K.gs + (i >> 2)] >> (2 * (i & 3))) & 3;
+    return code == 2 ? 1 : (code == 3 ? 2 : 0);
+  }
+  // position of individual i among the SNP's missing calls, or -1
+  __device__ long long miss_pos(uint32_t snp, uint32_t i) const
+  {
+    long long lo = K.miss_off[snp], hi = K.miss_off[snp + 1];
+    while (lo < hi) {
+      const long long mid = (lo + hi) >> 1;
+      if (K.miss_ind[mid] < i) lo = mid + 1;
+      else hi = mid;
+    }
+    return (lo < K.miss_off[snp + 1] && K.miss_ind[lo] == i) ? lo : -1;
+  }
+  __device__ int mval(long long pos) const { return K.miss_val[(size_t)c * K.miss_total + pos]; }
+  // genotype of SNP snp at individual i with the chain's imputed values
+  __device__ int geno_imp(uint32_t snp, uint32_t i) const
+  {
+    const long long q = has_miss(snp) ? miss_pos(snp, i) : -1;
+    return q >= 0 ? mval(q) : code_g(snp, i);
+  }
+  /* DataModel::sample_missing_single (src/data_model.cpp:92-103): fresh
+     imputed values for a SNP's missing calls, one uniform each in call order */
+  __device__ void draw_missing(uint32_t snp)
+  {
+    const long long o0 = K.miss_off[snp], nm = K.miss_off[snp + 1] - o0;
+    const double* mp = K.miss_prior + 3 * (size_t)snp;
+    for (long long q = lane; q < nm; q += 32)
+      K.miss_val[(size_t)c * K.miss_total + o0 + q] =
+          (uint8_t)miss_draw(mp, bmg_uniform01_at(rng.key0, rng.key1, rng.slot + (uint64_t)q));
+    rng.slot += (uint64_t)nm;
+    __syncwarp();
+  }
+  // what the missing calls of SNPs a (term t) and b (term u) add to x_t(a)'
+  // x_u(b) over the product with the missing calls read as 0
+  __device__ long long cross_corr(uint32_t a, int t, uint32_t b, int u) const
+  {
+    long long acc = 0;
+    if (has_miss(a)) {
+      for (long long q = K.miss_off[a] + lane; q < K.miss_off[a + 1]; q += 32) {
+        const uint32_t i = K.miss_ind[q];
+        acc += gval_term(mval(q), t) * gval_term(a == b ? mval(q) : geno_imp(b, i), u);
+      }
+    }
+    if (has_miss(b) && a != b) {
+      for (long long q = K.miss_off[b] + lane; q < K.miss_off[b + 1]; q += 32) {
+        const uint32_t i = K.miss_ind[q];
+        if (has_miss(a) && miss_pos(a, i) >= 0) continue;  // counted above
+        acc += gval_term(code_g(a, i), t) * gval_term(mval(q), u);
+      }
+    }
+    return warp_sum_ll(acc);
+  }
+  // ... and to x_t(snp)' v for the fixed-point vector v (y: yint; covariate r: eint)
+  __device__ long long vec_corr(uint32_t snp, int t, const int64_t* v) const
+  {
+    long long acc = 0;
+    for (long long q = K.miss_off[snp] + lane; q < K.miss_off[snp + 1]; q += 32)
+      acc += (long long)gval_term(mval(q), t) * v[K.miss_ind[q]];
+    return warp_sum_ll(acc);
+  }
+  __device__ long long sum_corr(uint32_t snp, int t) const
+  {
+    long long acc = 0;
+    for (long long q = K.miss_off[snp] + lane; q < K.miss_off[snp + 1]; q += 32) acc += gval_term(mval(q), t);
+    return warp_sum_ll(acc);
+  }
+
   // --------------------------------------------------------- model updates
   /* src/model.hpp:432-506 with src/symmmatrix.cpp:144-164 */
   __device__ void upd_add(DevModel* M, uint32_t snp, int mi, int term, bool is2, double invv, bool update)
@@ -718,6 +793,8 @@ struct Warp {
       M->inv[col] = invv;
     }
     long long xyi = geno_dot_fixed(snp, term, 0);
+    const bool miss = has_miss(snp);
+    if (miss) xyi += vec_corr(snp, term, P.yint);
     double xyc = (double)xyi * ldexp(1.0, -P.sy);
     __syncwarp();
     if (lane == 0) M->xy[col] = xyc;
@@ -725,10 +802,28 @@ struct Warp {
     const int me = min((int)K.m_e, col);
     for (int r = 0; r < me; ++r) {
       double v = cross_col(M, r, snp, term);
+      if (miss) {
+        if (r == 0) v += (double)sum_corr(snp, term);
+        else v = (double)(geno_dot_fixed(snp, term, r) + vec_corr(snp, term, K.eint + (size_t)r * K.n)) *
+                 ldexp(1.0, -K.se[r]);
+      }
       if (lane == 0) xxcol[r] = v;
     }
     cross_cols(M, me, col, snp, term, xxcol);
-    if (lane == 0) xxcol[col] = (double)term_cross_same(P.cnt, snp, term, term);
+    long long self = term_cross_same(P.cnt, snp, term, term);
+    if (K.miss_total) {
+      // the missing calls of the new SNP and of the model's SNPs
+      for (int r = me; r < col; ++r) {
+        const uint32_t sr = M->xc_snp[r];
+        if (!miss && !has_miss(sr)) continue;
+        const long long d = cross_corr(sr, M->xc_type[r], snp, term);
+        __syncwarp();
+        if (lane == 0) xxcol[r] += (double)d;
+        __syncwarp();
+      }
+      if (miss) self += cross_corr(snp, term, snp, term);
+    }
+    if (lane == 0) xxcol[col] = (double)self;
     __syncwarp();
     if (!update) {
       if (lane == 0) { M->llen = col + 1; M->vlen = col + 1; }
@@ -1008,6 +1103,88 @@ struct Warp {
       if (b) { found = base + __ffs(b) - 1; break; }
     }
     return found;
+  }
+
+  /* Sampler::sample_missing (src/sampler.cpp:264-453): the missing calls of
+     the model's SNPs are drawn from their conditional given the residuals, SNP
+     by SNP in model order (one uniform per call, in call order; the calls of
+     one SNP are distinct individuals, so they are drawn lane-parallel), then
+     X'y and X'X of the changed columns are formed again from the codes and
+     the new values.  The reference's r^2 term cancels from the normalised
+     weights and is left out. */
+  __device__ void sample_missing_gibbs()
+  {
+    DevModel* M = cur;
+    if (!K.miss_total) return;
+    const double s2x2 = M->sigma2 * 2;
+    const int ncols = min(M->blen, M->xcols);
+    bool any = false;
+    for (int li = 0; li < M->k; ++li) {
+      const uint32_t ind = M->loci[li];
+      if (!has_miss(ind)) continue;
+      any = true;
+      const int type = K.types[M->type_inds[li]];
+      const int ct = (type == 4) ? 0 : type;  // the coding of the first column
+      const int x1 = M->x_ind1[li], x2 = (type == 4) ? (int)M->x_ind2[li] : 0;
+      const double b1 = M->beta[x1], b2 = (type == 4) ? M->beta[x2] : 0.0;
+      const double* mp = K.miss_prior + 3 * (size_t)ind;
+      const double lp1 = flog(mp[1] - mp[0]) - flog(mp[0]), lp2 = flog(mp[2] - mp[1]) - flog(mp[0]);
+      const long long o0 = K.miss_off[ind], nmc = K.miss_off[ind + 1] - o0;
+      for (long long q = lane; q < nmc; q += 32) {
+        const uint32_t im = K.miss_ind[o0 + q];
+        double yh = 0.0;
+        for (int col = 0; col < ncols; ++col) {
+          double xv;
+          if (col < (int)K.m_e) xv = (col == 0) ? 1.0 : K.e[(size_t)col * K.n + im];
+          else xv = (double)gval_term(geno_imp(M->xc_snp[col], im), M->xc_type[col]);
+          yh = fma(M->beta[col], xv, yh);
+        }
+        const double res = P.y[im] - yh;
+        const int cv = mval(o0 + q);
+        const double t1 = gval_term(cv, ct), t2 = (cv == 1);
+        double nt[3];
+        for (int k = 0; k < 3; ++k) {
+          nt[k] = res - b1 * (gval_term(k, ct) - t1);
+          if (type == 4) nt[k] -= b2 * ((k == 1) - t2);
+        }
+        const double l1 = lp1 - (nt[1] * nt[1] - nt[0] * nt[0]) / s2x2;
+        const double l2 = lp2 - (nt[2] * nt[2] - nt[0] * nt[0]) / s2x2;
+        const double c1 = exp(l1) + 1.0;
+        const double c2 = exp(l2) + c1;
+        const double r = bmg_uniform01_at(rng.key0, rng.key1, rng.slot + (uint64_t)q) * c2;
+        K.miss_val[(size_t)c * K.miss_total + o0 + q] = (uint8_t)(r < 1.0 ? 0 : (r < c1 ? 1 : 2));
+      }
+      rng.slot += (uint64_t)nmc;
+      __syncwarp();
+    }
+    if (!any) return;
+    // X'y and X'X of the columns of SNPs with missing calls, exact
+    const int xc = M->xcols, me = K.m_e;
+    for (int xi = me; xi < xc; ++xi) {
+      const uint32_t snp = M->xc_snp[xi];
+      if (!has_miss(snp)) continue;
+      const int t = M->xc_type[xi];
+      const long long xyi = geno_dot_fixed(snp, t, 0) + vec_corr(snp, t, P.yint);
+      __syncwarp();
+      if (lane == 0) M->xy[xi] = (double)xyi * ldexp(1.0, -P.sy);
+      for (int r = 0; r < xc; ++r) {
+        double v;
+        if (r < me) {
+          if (r == 0) v = (double)(term_sum(P.cnt, snp, t) + sum_corr(snp, t));
+          else v = (double)(geno_dot_fixed(snp, t, r) + vec_corr(snp, t, K.eint + (size_t)r * K.n)) *
+                   ldexp(1.0, -K.se[r]);
+        } else {
+          const uint32_t sr = M->xc_snp[r];
+          const int tr = M->xc_type[r];
+          v = (double)(geno_cross(sr, tr, snp, t) + cross_corr(sr, tr, snp, t));
+        }
+        __syncwarp();
+        if (lane == 0) M->xx[(size_t)max(r, xi) * km + min(r, xi)] = v;
+        __syncwarp();
+      }
+    }
+    if (lane == 0) M->mu_beta_computed = 0;
+    __syncwarp();
   }
 
   /* src/model.hpp:314-342, src/rand.hpp:144-168 */
@@ -1369,9 +1546,11 @@ struct Warp {
   }
 
   // ------------------------------------------------------------ moves
+  /* src/sampler.hpp:500-515: a new term's missing calls are imputed afresh
+     (DataModel::sample_missing_single) before its prior precision is drawn */
   __device__ void prepare_add(uint32_t snp, int type, double* itv, bool missing_draw)
   {
-    (void)snp; (void)missing_draw;  // no missing genotypes on the device path
+    if (missing_draw && has_miss(snp)) draw_missing(snp);
     if (type == 4) {
       itv[0] = sample_inv_tau2_prior(0);
       itv[1] = sample_inv_tau2_prior(1);
@@ -2436,6 +2615,22 @@ __device__ void bulk_phase(const DevConst& K, int c, MoveShared& s, BulkCols& bc
   __int128 ia = 0, ia2 = 0;
   double* yhat = K.yhat + (size_t)c * K.n;
   const int dsh = P.sy - sh;
+  // the model's missing calls at their imputed values: the codes give 0
+  // there, so coef x_t(value) goes into a per-individual correction first
+  long long* mfit = K.miss_total ? K.miss_fit + (size_t)c * K.n_pad : nullptr;
+  if (mfit && nt > 0) {
+    for (int j = 0; j < nt; ++j) {
+      const uint32_t sj = bc.snp[j];
+      const long long o0 = K.miss_off[sj], o1 = K.miss_off[sj + 1];
+      const long long cf = bc.coef[j];
+      const int t = bc.term[j];
+      for (long long q = o0 + tid; q < o1; q += nth) {
+        const long long add = cf * gval_term(K.miss_val[(size_t)c * K.miss_total + q], t);
+        if (add) atomicAdd(reinterpret_cast<unsigned long long*>(&mfit[K.miss_ind[q]]), (unsigned long long)add);
+      }
+    }
+    __syncthreads();
+  }
   // a thread takes 16 individuals at a time: one 32-bit word of every model
   // column's packed codes, so each column costs one coalesced load per word
   const uint32_t words = (uint32_t)(K.n_pad / 16);
@@ -2452,6 +2647,19 @@ __device__ void bulk_phase(const DevConst& K, int c, MoveShared& s, BulkCols& bc
         for (int q = 0; q < 16; ++q) {
           const uint32_t c2 = (code >> (2 * q)) & 3u;  // 2 = het, 3 = hom-alt
           yg16[q] += (c2 == 2u) ? vh : ((c2 == 3u) ? vr : 0ll);
+        }
+      }
+      if (mfit) {
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+          const uint64_t i = (uint64_t)16 * w + q;
+          if (i < K.n) {
+            const long long f = mfit[i];
+            if (f) {
+              yg16[q] += f;
+              mfit[i] = 0;
+            }
+          }
         }
       }
     }
@@ -2675,6 +2883,36 @@ __device__ void prep_rb(Warp& W, bool scan_only)
       ch->n_rao_burnin = burn;
     }
   }
+  // the missing calls outside the model are imputed before the scan
+  // (src/sampler.cpp:731-736, DataModel::sample_missing): one slot per call
+  // in SNP and call order, the model's SNPs skipped.  The model's SNPs go to
+  // K.miss_inm ascending, with the missing calls of the listed SNPs before
+  // each, so that the scan's imputation finds every call's slot.
+  if (do_scan && K.miss_total) {
+    long long* inm = K.miss_inm + (size_t)W.c * 2 * K.km;
+    const int k = M->k;
+    for (int i = W.lane; i < k; i += 32) {
+      const uint32_t si = M->loci[i];
+      int rank = 0;
+      for (int q = 0; q < k; ++q) rank += M->loci[q] < si;
+      inm[rank] = si;
+    }
+    __syncwarp();
+    long long tot_in = 0;
+    if (W.lane == 0) {
+      for (int q = 0; q < k; ++q) {
+        inm[K.km + q] = tot_in;
+        const uint32_t sq = (uint32_t)inm[q];
+        tot_in += K.miss_off[sq + 1] - K.miss_off[sq];
+      }
+      inm[K.km + k] = tot_in;
+      rp->miss_slot = W.rng.slot;
+      rp->n_inm = k;
+    }
+    tot_in = __shfl_sync(FULL_MASK, tot_in, 0);
+    W.rng.slot += K.miss_total - (uint64_t)tot_in;
+    __syncwarp();
+  }
   // per-SNP tau2 draws of the scan (src/sampler.cpp:99-106) take p * terms
   // consecutive slots, one per (SNP, allowed term) in the reference's order
   uint64_t slot0 = W.rng.slot;
@@ -2861,6 +3099,97 @@ bmg_rbprep_kernel(DevConst K, int from_yhat, double yhat_absmax)
   store_state(K, c, s);
 }
 
+// The corrections of the RB scan for the SNPs with missing calls, one warp
+// per (SNP, chain) that scans this step: outside the model the calls are
+// imputed from their prior at the slots prep_rb reserved (src/sampler.cpp:
+// 731-736, src/data_model.cpp:78-90; the values serve this scan only, a SNP
+// that enters the model is imputed afresh), in the model their current
+// values hold.  dxr = sum x_t(value) R_i over the calls, and the precomputed
+// values as DataModel::update_prexx_cov corrects them (src/data_model.cpp:
+// 105-167).  Grid (ceil(miss_snps / 8), chains) x 256 threads.
+extern "C" __global__ void __launch_bounds__(256) bmg_miss_scan_kernel(DevConst K)
+{
+  const int c = blockIdx.y, lane = threadIdx.x & 31;
+  const RbParams& rp = K.rb[c];
+  if (!rp.do_scan) return;
+  const uint32_t m = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (m >= K.miss_snps) return;
+  const uint32_t j = K.miss_list[m];
+  const long long o0 = K.miss_off[j], nmc = K.miss_off[j + 1] - o0;
+  const bool inm = (K.inbits[(size_t)c * ((K.p + 31) / 32) + (j >> 5)] >> (j & 31)) & 1u;
+  uint64_t base = 0;
+  if (!inm) {
+    // in-model SNPs below j and their missing calls
+    const long long* il = K.miss_inm + (size_t)c * 2 * K.km;
+    int lo = 0, hi = rp.n_inm;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if ((uint64_t)il[mid] < j) lo = mid + 1;
+      else hi = mid;
+    }
+    base = rp.miss_slot + (uint64_t)(o0 - il[K.km + lo]);
+  }
+  const double* mp = K.miss_prior + 3 * (size_t)j;
+  const int64_t* R = K.resid + (size_t)c * K.n_pad;
+  long long dxr[4] = {0, 0, 0, 0};
+  int sg[4] = {0, 0, 0, 0}, sg2[4] = {0, 0, 0, 0}, cr[4][4] = {{0}}, n1 = 0;
+  for (long long q = lane; q < nmc; q += 32) {
+    int v;
+    if (inm) {
+      v = K.miss_val[(size_t)c * K.miss_total + o0 + q];
+    } else {
+      v = miss_draw(mp, bmg_uniform01_at(rp.key0, rp.key1, base + (uint64_t)q));
+    }
+    const long long Ri = R[K.miss_ind[o0 + q]];
+    n1 += (v == 1);
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const int x = gval_term(v, t);
+      dxr[t] += x * Ri;
+      sg[t] += x;
+      sg2[t] += x * x;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) cr[t][u] += x * gval_term(v, u);
+    }
+  }
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    dxr[t] = warp_sum_ll(dxr[t]);
+    sg[t] = warp_sum_i(sg[t]);
+    sg2[t] = warp_sum_i(sg2[t]);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) cr[t][u] = warp_sum_i(cr[t][u]);
+  }
+  n1 = warp_sum_i(n1);
+  if (lane != 0) return;
+  MissCorr& mc = K.miss_corr[(size_t)c * K.miss_snps + m];
+  const DevPheno& P = K.ph[K.pheno_of[c]];
+  const double* pre = P.pre + (size_t)j * K.offset;
+  double pc[BMG_MAX_OFFSET];
+  for (int q = 0; q < K.offset; ++q) pc[q] = pre[q];
+  const double nn = P.n;
+  double* loc = pc;
+  const bool ah = K.allow_types[4];
+  const double sah = ah ? pc[0] * pc[2] : 0.0;
+  for (int t = 0; t < 4; ++t) {
+    if (!K.allow_terms[t]) continue;
+    const double old_sum = loc[0];
+    loc[0] += sg[t];
+    loc[1] += sg2[t] - sg[t] * (old_sum * 2.0 + sg[t]) / nn;
+    loc += 2;
+  }
+  if (ah) {
+    loc[0] += (sah - pc[0] * pc[2]) / nn;
+    loc[0] += (double)n1;
+  }
+  for (int q = 0; q < K.offset; ++q) mc.pre[q] = pc[q];
+  for (int t = 0; t < 4; ++t) {
+    mc.dxr[t] = dxr[t];
+    mc.dsum[t] = sg[t];
+    for (int u = 0; u < 4; ++u) mc.dcross[t][u] = cr[t][u];
+  }
+}
+
 // Every chain's current sigma2 (bmg_scan_yhat)
 extern "C" __global__ void bmg_set_sigma2_kernel(DevConst K, double sigma2)
 {
@@ -2935,7 +3264,10 @@ bmg_move_kernel(DevConst K, int max_iters)
     const bool rb_step = ((iter + 1) % K.n_rao) == 0;
     if (ns_step) {
       /* src/sampler.cpp:628-635 */
-      if (tid < 32) bulk_setup(W, bc, BULK_ALPHA);
+      if (tid < 32) {
+        W.sample_missing_gibbs();
+        bulk_setup(W, bc, BULK_ALPHA);
+      }
       __syncthreads();
       bulk_phase(K, c, s, bc);
       if (tid < 32) {

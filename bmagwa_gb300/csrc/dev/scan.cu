@@ -39,7 +39,7 @@ bmg_scan_simt_kernel(DevConst K, const int64_t* resid_t)
       }
     }
     if (need) {
-      if (rb_fast_ok(K) && !in_model(K, c, j)) {
+      if (rb_fast_ok(K) && rb_plain(K, c, j)) {
         double lo;
         const double pr = rb_fast_pr(K, c, j, acc[K.types[0]], &lo);
         rb_store1(K, c, j, pr, lo);

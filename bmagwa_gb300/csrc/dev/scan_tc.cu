@@ -145,7 +145,7 @@ bmg_scan_tc_kernel(DevConst K, TcParams P, const __grid_constant__ CUtensorMap m
           const long long xi[2] = {xa, xb};
           for (int h = 0; h < 2; ++h) {
             if (!live[h]) continue;
-            if (!in_model(K, (int)c[h], j[h])) {
+            if (rb_plain(K, (int)c[h], j[h])) {
               rb_store1(K, (int)c[h], j[h], pr[h], lo[h]);
             } else {
               long long xr[4] = {0, 0, 0, 0};

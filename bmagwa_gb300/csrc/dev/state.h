@@ -126,7 +126,20 @@ struct RbParams {
   uint32_t key0, key1;      // chain stream key
   int do_scan;              // compute p_r at all this step
   int acc_rao;              // n_rao_burnin <= 0: accumulate p_rao
+  uint64_t miss_slot;       // first stream slot of the imputation of the missing calls outside the model
+  int n_inm;                // in-model SNPs listed in DevConst::miss_inm
   int adapt;                // update p_proposal and the proposal weights
+};
+
+// Scan corrections of one (chain, SNP with missing calls) at an RB step: the
+// SNP's missing calls enter the scan's products as 0; these add what their
+// imputed values contribute (src/data_model.cpp:30-72, 105-167).
+#define BMG_MAX_OFFSET 9
+struct MissCorr {
+  long long dxr[4];              // sum over the missing calls of x_t(value) R_i (fixed point)
+  double pre[BMG_MAX_OFFSET];    // the precomputed values as DataModel::update_prexx_cov corrects them
+  int dsum[4];                   // sum of x_t(value)
+  int dcross[4][4];              // sum of x_t(value) x_u(value)
 };
 
 // Trace buffers of one chunk (device), per chain.
@@ -319,6 +332,20 @@ struct DevConst {
   uint32_t* dr_x1;      // chains x km: first column of each locus
   uint32_t* dr_x2;      // chains x km: second column (AH)
   double* dr_pm;        // chains x 2^dr
+  // missing genotype calls (src/data.cpp:341-376, src/data_model.cpp:30-167,
+  // src/sampler.cpp:264-453); miss_total = 0 when the data has none
+  uint64_t miss_total;        // G: missing calls in the data
+  uint32_t miss_snps;         // SNPs with missing calls
+  const int64_t* miss_off;    // p + 1: CSR offsets of each SNP's missing calls
+  const uint32_t* miss_ind;   // G: their individuals, ascending per SNP
+  const double* miss_prior;   // p x 3: cumulative counts of the calls 0, 1, 2
+  const int32_t* miss_rank;   // p: index among the SNPs with missing calls, -1 if none
+  const uint32_t* miss_list;  // miss_snps: the SNPs with missing calls, ascending
+  uint8_t* miss_val;          // chains x G: imputed genotype (0, 1, 2) of each missing call
+  MissCorr* miss_corr;        // chains x miss_snps: corrections of the last RB scan
+  long long* miss_fit;        // chains x n_pad: fitted-value corrections of a bulk phase (zero between uses)
+  double* miss_yh;            // chains x n: fitted values at missing calls during an imputation step
+  long long* miss_inm;        // chains x 2 km: in-model SNPs ascending and their missing calls before them
   DevTrace tr;
 };
 

@@ -3,8 +3,10 @@ file does not cover: the flat proposal with the beta trace and raw
 genotypes, a model past the 128 columns kept in shared memory, individual
 tau2 over five effect types, delayed rejection (the second stage over all
 sub-models of a rejected multi-SNP or state-change move: one and two effect
-types, and the reference example's delay_rejection = 10 with covariates), and
-the command-line entry end to end."""
+types, and the reference example's delay_rejection = 10 with covariates),
+missing genotype calls (imputed at every RB step and with every new term, and
+Gibbs-updated in the model: src/data_model.cpp:30-167, src/sampler.cpp:264-453)
+and the command-line entry end to end."""
 import numpy as np
 import pytest
 
@@ -15,14 +17,17 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("name", ["small_flat", "example_flat", "example_large", "example_types_indiv",
-                                  "small_dr", "example_dr", "small_types_dr"])
+                                  "small_dr", "example_dr", "small_types_dr",
+                                  "small_types_missing", "example_missing", "small_types_dr_missing"])
 def test_gpu_matches_reference_more_options(bmg, tmp_path, name):
     """A flat proposal with the beta trace and raw genotypes (small_flat,
     example_flat), a model that grows past the 128 columns the move kernel
     keeps in shared memory (example_large), individual tau2 draws over four
-    terms in the scan (example_types_indiv) and delayed rejection (small_dr,
+    terms in the scan (example_types_indiv), delayed rejection (small_dr,
     example_dr, small_types_dr: src/sampler.cpp:882-1049,
-    src/sampler.hpp:929-1098, 1547-1618), against the reference's traces."""
+    src/sampler.hpp:929-1098, 1547-1618) and missing calls (5 % of the calls
+    with A and AH, 2 % with covariates and individual tau2, and missing calls
+    with delayed rejection), against the reference's traces."""
     z = H.golden("ref_" + name)
     ini = H.materialize(z, tmp_path)
     opt = bmg.options_from_ini(ini)
