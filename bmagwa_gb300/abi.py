@@ -193,7 +193,7 @@ def default_options():
     for t in range(5):
         o.types_prior[t] = 1.0
     o.max_model_size = 1024
-    o.scan_limbs = 5
+    o.scan_limbs = 6
     o.scan_impl = SCAN_TCGEN05
     o.proposal = PROPOSAL_ADAPTIVE
     o.graph_iters = 64

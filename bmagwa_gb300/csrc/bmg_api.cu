@@ -348,7 +348,7 @@ extern "C" bmg_status bmg_create(const bmg_options* opt, bmg_ctx** out)
     c->p = opt->m_g;
     c->C = opt->n_chains;
     c->km = opt->max_model_size ? opt->max_model_size : 1024;
-    c->L = opt->scan_limbs ? opt->scan_limbs : 5;
+    c->L = opt->scan_limbs ? opt->scan_limbs : 6;
     if (c->L < 3 || c->L > 7) throw bmg_error(BMG_EINVAL, "scan_limbs must be 3..7");
     {
       // the scan's exact sums: |x| <= 2, |residual| < 2^(8 L - 3), n terms

@@ -254,7 +254,7 @@ extern "C" bmg_status bmg_options_default(bmg_options* o)
   o->inv_tau2_e_val = 0.0;
   for (int t = 0; t < 5; ++t) o->types_prior[t] = 1.0;
   o->max_model_size = 1024;
-  o->scan_limbs = 5;
+  o->scan_limbs = 6;
   o->scan_impl = BMG_SCAN_TCGEN05;
   o->proposal = BMG_PROPOSAL_ADAPTIVE;
   o->graph_iters = 64;
