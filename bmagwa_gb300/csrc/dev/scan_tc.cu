@@ -30,18 +30,21 @@
 namespace {
 
 // epilogue warps: a multiple of 4 (each TMEM lane quarter gets the same
-// number); the kernel is instantiated for 8 and 12 and the host picks
-template <int EPI>
+// number); decode warps 4 or 8; the kernel is instantiated for (8, 4),
+// (12, 4) and (8, 8) and the host picks
+template <int EPI, int DEC>
 struct TcShape {
-  static constexpr int threads = 192 + 32 * EPI;
+  static constexpr int main_warps = 6 + DEC - 4;
+  static constexpr int threads = 32 * (main_warps + EPI);
 };
 }  // namespace
 
-template <int TC_EPI_WARPS>
-__global__ void __launch_bounds__(TcShape<TC_EPI_WARPS>::threads, 1)
+template <int TC_EPI_WARPS, int TC_DEC_WARPS>
+__global__ void __launch_bounds__(TcShape<TC_EPI_WARPS, TC_DEC_WARPS>::threads, 1)
 bmg_scan_tc_kernel(DevConst K, TcParams P, const __grid_constant__ CUtensorMap map_b,
                    const __grid_constant__ CUtensorMap map_g)
 {
+  constexpr int MAIN = TcShape<TC_EPI_WARPS, TC_DEC_WARPS>::main_warps;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   // 1024-byte aligned base for the swizzled tiles; the int64 sums follow the stages
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -56,12 +59,12 @@ bmg_scan_tc_kernel(DevConst K, TcParams P, const __grid_constant__ CUtensorMap m
   const uint32_t my_tiles = (P.tiles > blockIdx.x) ? (P.tiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
   const uint32_t tmem = tc_setup(P, ctl, TC_EPI_WARPS);
 
-  if (warp < 6) {
+  if (warp < MAIN) {
     tc_main_roles(P, ctl, smem, tmem, my_tiles, map_b, map_g);
   } else {
     // epilogue warps: warp w reads TMEM lanes 32 (w % 4) .. +31 (the rows of
     // the tile); the TC_EPI_WARPS / 4 warps of a quarter split the chains
-    const uint32_t e = warp - 6;
+    const uint32_t e = warp - MAIN;
     const uint32_t quarter = warp & 3, part = e >> 2, nparts = TC_EPI_WARPS / 4;
     const uint32_t row = quarter * 32 + lane;
     const uint32_t c_lo = part * ct / nparts, c_hi = (part + 1) * ct / nparts;
@@ -233,9 +236,11 @@ struct TcVariant {
   int ct_div;  // chains per tile = ceil(chains / ct_div); 0: the widest tile whose
                // accumulators (two of 192 columns) leave A room in tensor memory
   int n_acc;   // TMEM accumulators
+  int dec;     // decode warps
 };
-static const TcVariant kTcVariants[] = {{12, 1, 2}, {8, 1, 2}, {12, 2, 2}, {8, 2, 2},
-                                        {12, 1, 1}, {8, 1, 1}, {12, 0, 2}, {8, 0, 2}};
+static const TcVariant kTcVariants[] = {{12, 1, 2, 4}, {8, 1, 2, 4}, {12, 2, 2, 4}, {8, 2, 2, 4},
+                                        {12, 1, 1, 4}, {8, 1, 1, 4}, {12, 0, 2, 4}, {8, 0, 2, 4},
+                                        {8, 1, 2, 8},  {8, 1, 1, 8},  {8, 0, 2, 8}};
 constexpr int kTcVariantCount = sizeof(kTcVariants) / sizeof(kTcVariants[0]);
 
 extern "C" int bmg_scan_tc_variants() { return kTcVariantCount; }
@@ -243,12 +248,13 @@ extern "C" int bmg_scan_tc_variants() { return kTcVariantCount; }
 extern "C" void bmg_scan_tc_variant_name(int v, char* buf, size_t len)
 {
   if (v < 0 || v >= kTcVariantCount) v = 0;
+  const char* dec = kTcVariants[v].dec == 8 ? " decode_warps=8" : "";
   if (kTcVariants[v].ct_div == 0)
-    snprintf(buf, len, "epilogue_warps=%d chains_per_tile=A-in-TMEM accumulators=%d", kTcVariants[v].epi,
-             kTcVariants[v].n_acc);
+    snprintf(buf, len, "epilogue_warps=%d chains_per_tile=A-in-TMEM accumulators=%d%s", kTcVariants[v].epi,
+             kTcVariants[v].n_acc, dec);
   else
-    snprintf(buf, len, "epilogue_warps=%d chains_per_tile=1/%d accumulators=%d", kTcVariants[v].epi,
-             kTcVariants[v].ct_div, kTcVariants[v].n_acc);
+    snprintf(buf, len, "epilogue_warps=%d chains_per_tile=1/%d accumulators=%d%s", kTcVariants[v].epi,
+             kTcVariants[v].ct_div, kTcVariants[v].n_acc, dec);
 }
 
 static uint32_t tc_cap(const DevConst* K, int v)
@@ -268,7 +274,8 @@ extern "C" int bmg_scan_tc_variant_redundant(const DevConst* K, int v)
   if (!tc_plan(K, &P, tc_cap(K, v), (uint32_t)kTcVariants[v].n_acc)) return 1;
   for (int u = 0; u < v; ++u) {
     TcParams Q;
-    if (kTcVariants[u].epi != kTcVariants[v].epi || !tc_plan(K, &Q, tc_cap(K, u), (uint32_t)kTcVariants[u].n_acc))
+    if (kTcVariants[u].epi != kTcVariants[v].epi || kTcVariants[u].dec != kTcVariants[v].dec ||
+        !tc_plan(K, &Q, tc_cap(K, u), (uint32_t)kTcVariants[u].n_acc))
       continue;
     if (Q.chains_tile == P.chains_tile && Q.n_acc == P.n_acc && Q.a_tmem == P.a_tmem) return 1;
   }
@@ -286,14 +293,15 @@ extern "C" int bmg_scan_tc_supported(const DevConst* K)
   return (major == 10 && minor == 3) ? 1 : 0;
 }
 
-template <int EPI>
-static int tc_launch_shape(const DevConst* K, const TcParams& P, const CUtensorMap& mb, const CUtensorMap& mg,
+template <int EPI, int DEC>
+static int tc_launch_shape(const DevConst* K, TcParams P, const CUtensorMap& mb, const CUtensorMap& mg,
                            cudaStream_t stream)
 {
+  P.dec_warps = DEC;
   const size_t smem = tc_smem_bytes(P);
   static size_t configured = 0;
   if (configured < smem) {
-    if (cudaFuncSetAttribute(bmg_scan_tc_kernel<EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+    if (cudaFuncSetAttribute(bmg_scan_tc_kernel<EPI, DEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
         cudaSuccess)
       return 6;
     configured = smem;
@@ -306,7 +314,7 @@ static int tc_launch_shape(const DevConst* K, const TcParams& P, const CUtensorM
     if (sms <= 0) sms = 1;
   }
   const unsigned grid = (unsigned)std::min<uint32_t>(P.tiles, (uint32_t)sms);
-  bmg_scan_tc_kernel<EPI><<<grid, TcShape<EPI>::threads, smem, stream>>>(*K, P, mb, mg);
+  bmg_scan_tc_kernel<EPI, DEC><<<grid, TcShape<EPI, DEC>::threads, smem, stream>>>(*K, P, mb, mg);
   return cudaGetLastError() == cudaSuccess ? 0 : 7;
 }
 
@@ -338,6 +346,7 @@ extern "C" int bmg_scan_tc_launch(const DevConst* K, cudaStream_t stream, int va
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
       return 4;
   }
-  return kTcVariants[variant].epi == 8 ? tc_launch_shape<8>(K, P, mb, mg, stream)
-                                       : tc_launch_shape<12>(K, P, mb, mg, stream);
+  if (kTcVariants[variant].dec == 8) return tc_launch_shape<8, 8>(K, P, mb, mg, stream);
+  return kTcVariants[variant].epi == 8 ? tc_launch_shape<8, 4>(K, P, mb, mg, stream)
+                                       : tc_launch_shape<12, 4>(K, P, mb, mg, stream);
 }

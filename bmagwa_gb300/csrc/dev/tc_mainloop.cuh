@@ -75,6 +75,10 @@ struct TcParams {
   // no FP32 partial sum runs over more than seg_chunks stages; the epilogue
   // adds the segments' exact integers.  0: one segment of all k_chunks.
   uint32_t seg_chunks = 0;
+  // decode warps: 4 (warps 0-3, a row of 128 individuals each) or 8 (warps
+  // 0-3 and 6-9, each row's two halves of 64 individuals; the epilogue then
+  // starts at warp 10)
+  uint32_t dec_warps = 4;
 };
 
 // stages of a tile's K segment s and the number of segments
@@ -147,7 +151,7 @@ __device__ __forceinline__ uint32_t tc_setup(const TcParams& P, TcCtl& ctl, int 
   const int tid = threadIdx.x, warp = tid >> 5;
   if (tid == 0) {
     for (uint32_t st = 0; st < P.stages; ++st) mbar_init(&ctl.full_bar[st], 1);
-    for (uint32_t t = 0; t < P.a_stages; ++t) mbar_init(&ctl.aready_bar[t], 4);
+    for (uint32_t t = 0; t < P.a_stages; ++t) mbar_init(&ctl.aready_bar[t], P.dec_warps);
     for (uint32_t r = 0; r < P.ring; ++r) mbar_init(&ctl.done_bar[r], 1);
     for (int b = 0; b < 2; ++b) {
       mbar_init(&ctl.acc_full[b], 1);
@@ -259,15 +263,18 @@ __device__ __forceinline__ void tc_main_roles(const TcParams& P, TcCtl& ctl, uin
       mma_commit(&ctl.drain_bar);
       if (!mbar_wait(&ctl.drain_bar, 0)) ctl.abort_flag = 1;
     }
-  } else if (warp < 4) {
-    // decode warps: packed 2-bit codes -> bf16 rows of A; thread = row = TMEM lane
-    const uint32_t row = tid;  // 0..127
+  } else if (warp < 4 || (warp >= 6 && warp < 6 + (int)P.dec_warps - 4)) {
+    // decode warps: packed 2-bit codes -> bf16 rows of A; thread = row = TMEM
+    // lane of the warp's lane quarter; with 8 decode warps a warp takes one
+    // half (64 individuals) of its rows
+    const uint32_t row = (warp & 3) * 32 + lane;  // 0..127
+    const int h0 = (P.dec_warps == 8 && warp >= 6) ? 1 : 0, nh = (P.dec_warps == 8) ? 1 : 2;
     const uint32_t sl = row / P.tpad, u = row % P.tpad;
     int value[4];  // this row's coding of the four codes (-1: a padding row, zeros)
     for (int c = 0; c < 4; ++c) value[c] = P.term_of_row[u] >= 0 ? term_value(c, P.term_of_row[u]) : -1;
     const DecTab tab = dec_tab(value);
     const uint32_t total = my_tiles * nk;
-    const uint32_t a_lane = tmem + ((uint32_t)(warp * 32) << 16) + P.n_acc * P.acc_cols;
+    const uint32_t a_lane = tmem + ((uint32_t)((warp & 3) * 32) << 16) + P.n_acc * P.acc_cols;
     TcRing full, aslot, done;  // this stage's slots; the done phase of stage g - SA
     for (uint32_t g = 0; g < total; ++g) {
       // A in shared memory: the TMA of this stage waited for the MMA of stage
@@ -300,6 +307,7 @@ __device__ __forceinline__ void tc_main_roles(const TcParams& P, TcCtl& ctl, uin
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
         for (int half = 0; half < 2; ++half) {
+          if (nh == 1 && half != h0) continue;  // the other decode warp's half
 #pragma unroll
           for (int kb = 0; kb < 16; ++kb) {
             const int k = 16 * half + kb;
@@ -312,6 +320,7 @@ __device__ __forceinline__ void tc_main_roles(const TcParams& P, TcCtl& ctl, uin
         uint8_t* a = sp + P.b_bytes;
 #pragma unroll
         for (int c = 0; c < 16; ++c) {
+          if (nh == 1 && (c >> 3) != h0) continue;  // the other decode warp's half
           // 16-byte chunk c of the row: individuals 8c .. 8c + 7 (code bytes
           // 2c, 2c + 1), in sub-tile c / 8 of 64 individuals
           const uint32_t h = w[c >> 1] >> ((c & 1) * 16);
