@@ -350,15 +350,6 @@ extern "C" bmg_status bmg_create(const bmg_options* opt, bmg_ctx** out)
     c->km = opt->max_model_size ? opt->max_model_size : 1024;
     c->L = opt->scan_limbs ? opt->scan_limbs : 6;
     if (c->L < 3 || c->L > 7) throw bmg_error(BMG_EINVAL, "scan_limbs must be 3..7");
-    {
-      // the scan's exact sums: |x| <= 2, |residual| < 2^(8 L - 3), n terms
-      // must stay inside int64
-      int lg = 0;
-      while ((1ull << lg) < opt->n) ++lg;
-      if (8 * (int)c->L - 2 + lg > 63)
-        throw bmg_error(BMG_EINVAL, "scan_limbs " + std::to_string(c->L) + " with " + std::to_string(opt->n) +
-                                        " individuals could overflow the scan's exact 64-bit sums");
-    }
     c->max_ms = (int)std::min<uint64_t>(std::min<uint64_t>(c->p, 255), opt->max_move_size);
     // delayed rejection enumerates 2^m sub-models of a rejected move of m
     // SNPs (src/sampler.hpp:163-169: m <= min(delay_rejection, max_move_size))

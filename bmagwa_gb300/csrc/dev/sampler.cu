@@ -2826,7 +2826,10 @@ __device__ void bulk_setup(Warp& W, BulkCols& bc, int mode)
     if (mode & BULK_YHAT) tot = W.P.y_absmax + W.s.yhat_given_max + 1e-300;
     else if (nt == 0 && me > 1) tot += W.ch->yhat_absmax;  // the accumulated y_hat
     int e2 = (int)ceil(log2(tot));
-    sh = (int)(8 * K.limbs_n - 3) - e2;
+    // the limbs hold |R| < 2^(8L-1); the scan's exact int64 sums of n
+    // products |x R| <= 2 |R| need |R| < 2^(61 - log2 n) as well
+    const int lgn = 64 - __clzll((long long)(K.n > 1 ? K.n - 1 : 1));
+    sh = min((int)(8 * K.limbs_n - 3), 61 - lgn) - e2;
   } else {
     // fitted genotype values stay below 2^52 so they convert to double exactly
     int e2 = (int)ceil(log2(bound + 1e-300));

@@ -109,7 +109,7 @@ typedef struct bmg_options {
   double eh_tau2[4];
   /* GB300 knobs (no reference counterpart) */
   uint32_t max_model_size;  /* columns of X_gamma incl. covariates (ref MAXMODELSIZE 1024) */
-  uint32_t scan_limbs;      /* 8-bit residual limbs in the scan GEMM, 3..7 (default 6); 8 L - 2 + log2 n <= 63 */
+  uint32_t scan_limbs;      /* 8-bit residual limbs in the scan GEMM, 3..7 (default 6) */
   int32_t scan_impl;        /* BMG_SCAN_TCGEN05 or BMG_SCAN_SIMT */
   int32_t proposal;         /* BMG_PROPOSAL_ADAPTIVE or BMG_PROPOSAL_LEARNED */
   uint32_t graph_iters;     /* iterations captured per CUDA graph chunk */
