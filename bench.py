@@ -375,7 +375,11 @@ def run_learned_compare(args, wl):
         chains = [col.chain(c) for c in range(wl["chains"])]
         e = ess.summarize([(t["modelsize"], t["loci"]) for t in chains], sec)
         acc = [ctx.state(c)[0].n_accepted / max(1, ctx.state(c)[0].n_iter) for c in range(wl["chains"])]
-        out[name] = dict(e, iter_per_s=samp * wl["chains"] / sec, seconds=sec,
+        mt = np.concatenate([np.asarray(t["move_type"]) for t in chains])
+        jd = np.concatenate([np.asarray(t["jumpdistance"]) for t in chains])
+        moves = {kind: [int(np.sum(mt == m)), int(np.sum((mt == m) & (jd > 0)))]
+                 for m, kind in enumerate(("addrem", "swap", "statechange", "typeswitch"))}
+        out[name] = dict(e, moves_proposed_accepted=moves, iter_per_s=samp * wl["chains"] / sec, seconds=sec,
                          mean_model_size=float(np.mean([len(t["loci"]) / max(1, len(t["modelsize"])) for t in chains])),
                          acceptance=float(np.mean(acc)))
         ctx.close()

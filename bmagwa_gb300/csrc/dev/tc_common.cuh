@@ -129,7 +129,9 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v)
 }
 
 // each thread of the warp writes 32 consecutive 32-bit columns of its own
-// TMEM lane (the warp's lane quarter is in taddr) and waits for the writes
+// TMEM lane (the warp's lane quarter is in taddr).  The store is
+// asynchronous: tmem_wait_st before another role reads the columns (the
+// source registers may be reused at once)
 __device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t* r)
 {
   asm volatile(
@@ -140,8 +142,10 @@ __device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t* r)
       "r"(r[17]), "r"(r[18]), "r"(r[19]), "r"(r[20]), "r"(r[21]), "r"(r[22]), "r"(r[23]), "r"(r[24]),
       "r"(r[25]), "r"(r[26]), "r"(r[27]), "r"(r[28]), "r"(r[29]), "r"(r[30]), "r"(r[31])
       : "memory");
-  asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
 }
+
+// waits until this thread's earlier tcgen05.st have been performed
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
 // the driver's tensor-map encoder, looked up once through the runtime
 static inline PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
