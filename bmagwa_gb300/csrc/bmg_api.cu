@@ -421,22 +421,14 @@ extern "C" bmg_status bmg_load_bed(bmg_ctx* ctx, const uint8_t* packed, uint64_t
   if (n != ctx->n || p != ctx->p) throw bmg_error(BMG_EINVAL, "genotype sizes differ from the options");
   const uint64_t stride = (n + 3) / 4, gs = ctx->gs;
   const int tail = (int)(n % 4);
-  // rows of `stride` bytes into the zeroed, padded device layout by one
-  // pitched copy from the caller's pageable memory (the driver's pageable
-  // path: 27 ms for 1.25 GB on a GB300's Grace host, against 37 ms for pinned
-  // staging with eight host threads, and a device kernel reading the pages
-  // over NVLink-C2C varied from 9 to 123 ms between calls); with
-  // BMG_HOST_STAGING=1, pitched copies from pinned staging chunks (host
-  // copies by several threads, the DMA of one chunk overlapping the host copy
-  // of the next), for hosts whose pageable copies are slow.  The unused codes
-  // of a row's last byte are then cleared.
+  // rows of `stride` bytes into the zeroed, padded device layout by pitched
+  // copies from pinned staging chunks (host copies by several threads, the
+  // DMA of one chunk overlapping the host copy of the next); the unused
+  // codes of a row's last byte are then cleared
   uint8_t* g = ctx->dalloc<uint8_t>(gs * p);
   int32_t* cnt = ctx->dalloc<int32_t>(2 * p);
   int32_t* miss = ctx->dalloc<int32_t>(p);
-  const char* stg = std::getenv("BMG_HOST_STAGING");
-  if (!(stg && stg[0] == '1')) {
-    CK(cudaMemcpy2DAsync(g, gs, packed, stride, stride, p, cudaMemcpyHostToDevice, ctx->stream));
-  } else {
+  {
     const size_t chunk_rows = std::min<size_t>(p, std::max<size_t>(1, (size_t(32) << 20) / stride));
     ctx->ensure_stage(chunk_rows * stride);
     const unsigned nth = std::max(1u, std::min(8u, std::thread::hardware_concurrency()));

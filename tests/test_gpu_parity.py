@@ -400,24 +400,6 @@ def test_gpu_posterior_matches_exact_enumeration(bmg, oracle, dr):
 
 
 
-def test_pageable_and_staged_genotype_loads_agree(bmg, tmp_path, monkeypatch):
-    """bmg_load_bed copies the caller's rows straight from pageable memory,
-    or through pinned staging with BMG_HOST_STAGING=1: both give the same
-    chains, with a ragged last code byte and junk in its unused bits."""
-    opt, packed, y, e = synth_case(bmg, tmp_path, "plain", n=1001, p=3000, chains=2, iters=60, n_rao=5)
-    n, p = int(opt.n), int(opt.m_g)
-    junk = packed.copy().reshape(p, (n + 3) // 4)
-    junk[:, -1] |= np.uint8(0xFF & ~((1 << (2 * (n % 4))) - 1))
-    junk = junk.reshape(-1)
-    monkeypatch.delenv("BMG_HOST_STAGING", raising=False)
-    _, a = run_gpu(bmg, opt, junk, y, e, 60)
-    monkeypatch.setenv("BMG_HOST_STAGING", "1")
-    _, b = run_gpu(bmg, opt, junk, y, e, 60)
-    for c in range(opt.n_chains):
-        for key in ("loci", "jumpdistance", "log_likelihood"):
-            np.testing.assert_array_equal(a.chain(c)[key], b.chain(c)[key])
-
-
 def test_many_covariates_match_the_oracle(bmg, oracle, tmp_path):
     """Twelve covariates besides the constant (the reference reads any m_e,
     src/data.cpp:202-243): the chains equal the oracle's."""
