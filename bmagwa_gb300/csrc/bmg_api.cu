@@ -39,8 +39,7 @@ extern "C" __global__ void bmg_pre_df_kernel(const double* pre, uint64_t p, uint
 extern "C" __global__ void bmg_pre_kernel(const int32_t* cnt, uint64_t p, uint32_t n_samples, const double* n_of,
                                           int allow_mask, int ah, int offset, double* pre);
 extern "C" __global__ void bmg_gsum_kernel(const uint8_t* geno, uint64_t n, uint64_t p, uint32_t gs,
-                                           const int64_t* yint, const int64_t* eint, uint32_t nv, uint32_t chunk,
-                                           int64_t* gsum);
+                                           const int64_t* yint, const int64_t* eint, uint32_t nv, int64_t* gsum);
 extern "C" __global__ void bmg_init_kernel(DevConst K);
 extern "C" __global__ void bmg_rbprep_kernel(DevConst K, int from_yhat, double yhat_absmax);
 extern "C" __global__ void bmg_set_sigma2_kernel(DevConst K, double sigma2);
@@ -750,13 +749,8 @@ extern "C" bmg_status bmg_precompute(bmg_ctx* ctx)
     // X'y and X'E of every SNP and term, from exact per-SNP H/R sums
     const uint32_t nv = std::max<uint32_t>(1, me);
     int64_t* gsum = ctx->dalloc<int64_t>((size_t)K.p * nv * 2, false);
-    // up to 12,288 entries of the vector (96 KB, two blocks per SM) per pass
-    const uint32_t chunk = (uint32_t)std::min<uint64_t>(12288, ((n + 127) / 128) * 128);
-    const size_t smem = 8 * (size_t)chunk;
-    CK(cudaFuncSetAttribute(bmg_gsum_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const uint64_t blocks = std::min<uint64_t>((K.p + 7) / 8, 152 * 2);
-    bmg_gsum_kernel<<<(unsigned)blocks, 256, smem, ctx->stream>>>(K.geno, n, K.p, K.gs, K.yint, dEi, nv, chunk,
-                                                                   gsum);
+    const uint64_t blocks = std::min<uint64_t>((K.p + 7) / 8, 152 * 8);
+    bmg_gsum_kernel<<<(unsigned)blocks, 256, 0, ctx->stream>>>(K.geno, n, K.p, K.gs, K.yint, dEi, nv, gsum);
     LAUNCHED(ctx, "bmg_gsum_kernel");
     K.gsum = gsum;
   }

@@ -74,44 +74,47 @@ extern "C" __global__ void bmg_trace_reset_kernel(DevChain* ch, int n_chains)
 // SNP: gsum[(j * nv + v) * 2 + {0, 1}].  A term's product with the vector is
 // then coefH * H-sum + coefR * R-sum, exactly the sum over individuals of
 // x_t(g_i) * vec_i that Model::update_add needs for X'y and X'E
-// (src/model.hpp:432-506).  A block stages `chunk` entries of the vector in
-// shared memory once and runs all its SNPs over them, one warp per SNP; lane
-// l takes individuals l, l + 32, ... so that the warp reads consecutive
-// 8-byte entries (no bank conflicts) and four lanes share a code byte.
+// (src/model.hpp:432-506).  One warp per SNP; each lane takes whole bytes
+// (4 individuals); the vectors are staged through shared memory in chunks.
+#define GSUM_CHUNK 2048
 extern "C" __global__ void __launch_bounds__(256)
 bmg_gsum_kernel(const uint8_t* geno, uint64_t n, uint64_t p, uint32_t gs, const int64_t* yint,
-                const int64_t* eint, uint32_t nv, uint32_t chunk, int64_t* gsum)
+                const int64_t* eint, uint32_t nv, int64_t* gsum)
 {
-  extern __shared__ int64_t vec[];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (uint32_t v = 0; v < nv; ++v) {
-    const int64_t* src = (v == 0) ? yint : eint + (size_t)v * n;
-    for (uint64_t c0 = 0; c0 < n; c0 += chunk) {
-      const uint64_t len = min((uint64_t)chunk, n - c0);
-      __syncthreads();
-      for (uint64_t i = threadIdx.x; i < len; i += blockDim.x) vec[i] = src[c0 + i];
-      __syncthreads();
-      for (uint64_t j = (uint64_t)blockIdx.x * nw + warp; j < p; j += (uint64_t)gridDim.x * nw) {
-        const uint8_t* row = geno + j * gs + (c0 >> 2);
-        long long sh = 0, sr = 0;
-        for (uint64_t i = lane; i < len; i += 32) {
-          const uint32_t code = (row[i >> 2] >> (2 * (i & 3))) & 3u;  // 2 = het, 3 = hom-alt
-          const long long val = vec[i];
-          sh += code == 2u ? val : 0ll;
-          sr += code == 3u ? val : 0ll;
-        }
-        sh = warp_sum_ll(sh);
-        sr = warp_sum_ll(sr);
-        if (lane == 0) {
-          int64_t* o = gsum + (j * nv + v) * 2;
-          if (c0 == 0) {
-            o[0] = sh;
-            o[1] = sr;
-          } else {
-            o[0] += sh;
-            o[1] += sr;
+  __shared__ int64_t vec[GSUM_CHUNK];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint64_t snps_per_block = blockDim.x >> 5;
+  for (uint64_t base = (uint64_t)blockIdx.x * snps_per_block; base < p; base += (uint64_t)gridDim.x * snps_per_block) {
+    const uint64_t j = base + warp;
+    const uint8_t* row = geno + (j < p ? j : 0) * gs;
+    for (uint32_t v = 0; v < nv; ++v) {
+      const int64_t* src = (v == 0) ? yint : eint + (size_t)v * n;
+      long long sh = 0, sr = 0;
+      for (uint64_t c0 = 0; c0 < n; c0 += GSUM_CHUNK) {
+        const uint64_t len = min((uint64_t)GSUM_CHUNK, n - c0);
+        __syncthreads();
+        for (uint64_t i = threadIdx.x; i < len; i += blockDim.x) vec[i] = src[c0 + i];
+        __syncthreads();
+        if (j < p) {
+          for (uint64_t b = lane; b < (len + 3) / 4; b += 32) {
+            uint32_t byte = row[(c0 >> 2) + b];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              const uint64_t i = 4 * b + q;
+              const int code = (byte >> (2 * q)) & 3;
+              if (i < len) {
+                if (code == 2) sh += vec[i];
+                else if (code == 3) sr += vec[i];
+              }
+            }
           }
         }
+      }
+      sh = warp_sum_ll(sh);
+      sr = warp_sum_ll(sr);
+      if (j < p && lane == 0) {
+        gsum[(j * nv + v) * 2] = sh;
+        gsum[(j * nv + v) * 2 + 1] = sr;
       }
     }
   }

@@ -181,13 +181,13 @@ bmg_scan_tc_kernel(DevConst K, TcParams P, const __grid_constant__ CUtensorMap m
 // dynamic shared memory of a plan: the stage ring, the int64 sums, alignment slack
 static size_t tc_smem_bytes(const TcParams& P)
 {
-  return (size_t)P.stages * P.stage_bytes + P.xr_bytes + (size_t)P.pk_stages * P.pk_bytes + 1024;
+  return (size_t)P.stages * P.stage_bytes + P.xr_bytes + 1024;
 }
 
 // static shared memory of the kernel (decode tables and barriers) is below 2 KB
 constexpr size_t TC_SMEM_LIMIT = 227 * 1024 - 2 * 1024;
 
-static bool tc_plan(const DevConst* K, TcParams* P, uint32_t ct_cap, uint32_t n_acc, bool codes_ring = false)
+static bool tc_plan(const DevConst* K, TcParams* P, uint32_t ct_cap, uint32_t n_acc)
 {
   uint32_t T = K->n_terms;
   P->tpad = T <= 1 ? 1 : (T <= 2 ? 2 : 4);
@@ -210,25 +210,11 @@ static bool tc_plan(const DevConst* K, TcParams* P, uint32_t ct_cap, uint32_t n_
     if (P->n_mma > TC_ACC_COLS || P->n_mma < 16) continue;
     P->b_bytes = P->n_mma * TC_BK * 2;  // two 128-byte-swizzled boxes of 64 individuals
     tc_place_a(*P, n_acc);
-    // the codes get a ring of their own only with A in TMEM (the decode
-    // then never writes a stage slot)
-    const bool ring = codes_ring && P->a_tmem;
-    P->stage_bytes = ((P->b_bytes + P->a_bytes + (ring ? 0 : P->pk_bytes) + 1023) / 1024) * 1024;
+    P->stage_bytes = ((P->b_bytes + P->a_bytes + P->pk_bytes + 1023) / 1024) * 1024;
     P->xr_bytes = TC_BM * (ct + 1) * 8;
     P->b_rows_per_tile = ct * L;
     for (uint32_t st = TC_MAX_STAGES; st >= 2; --st) {
       tc_set_rings(*P, st);
-      P->pk_stages = 0;
-      P->pk_off = 0;
-      if (ring) {
-        // at least one stage of lead over B; as many slots as fit, up to TC_MAX_PK
-        const size_t used = (size_t)st * P->stage_bytes + P->xr_bytes + 1024;
-        if (used >= TC_SMEM_LIMIT) continue;
-        const uint32_t sp = (uint32_t)std::min<size_t>(TC_MAX_PK, (TC_SMEM_LIMIT - used) / P->pk_bytes);
-        if (sp < st + 1) continue;
-        P->pk_stages = sp;
-        P->pk_off = st * P->stage_bytes + P->xr_bytes;
-      }
       if (tc_smem_bytes(*P) <= TC_SMEM_LIMIT) {
         P->m_tiles = (uint32_t)((K->p + P->snps_per_tile - 1) / P->snps_per_tile);
         P->n_tiles = (K->n_chains + ct - 1) / ct;
@@ -251,12 +237,10 @@ struct TcVariant {
                // accumulators (two of 192 columns) leave A room in tensor memory
   int n_acc;   // TMEM accumulators
   int dec;     // decode warps
-  int ring;    // 1: the packed codes in a deeper ring of their own
 };
-static const TcVariant kTcVariants[] = {{12, 1, 2, 4, 0}, {8, 1, 2, 4, 0}, {12, 2, 2, 4, 0}, {8, 2, 2, 4, 0},
-                                        {12, 1, 1, 4, 0}, {8, 1, 1, 4, 0}, {12, 0, 2, 4, 0}, {8, 0, 2, 4, 0},
-                                        {8, 1, 2, 8, 0},  {8, 1, 1, 8, 0},  {8, 0, 2, 8, 0},  {12, 1, 2, 4, 1},
-                                        {8, 1, 2, 4, 1},  {12, 2, 2, 4, 1}};
+static const TcVariant kTcVariants[] = {{12, 1, 2, 4}, {8, 1, 2, 4}, {12, 2, 2, 4}, {8, 2, 2, 4},
+                                        {12, 1, 1, 4}, {8, 1, 1, 4}, {12, 0, 2, 4}, {8, 0, 2, 4},
+                                        {8, 1, 2, 8},  {8, 1, 1, 8},  {8, 0, 2, 8}};
 constexpr int kTcVariantCount = sizeof(kTcVariants) / sizeof(kTcVariants[0]);
 
 extern "C" int bmg_scan_tc_variants() { return kTcVariantCount; }
@@ -264,7 +248,7 @@ extern "C" int bmg_scan_tc_variants() { return kTcVariantCount; }
 extern "C" void bmg_scan_tc_variant_name(int v, char* buf, size_t len)
 {
   if (v < 0 || v >= kTcVariantCount) v = 0;
-  const char* dec = kTcVariants[v].dec == 8 ? " decode_warps=8" : (kTcVariants[v].ring ? " codes_ring" : "");
+  const char* dec = kTcVariants[v].dec == 8 ? " decode_warps=8" : "";
   if (kTcVariants[v].ct_div == 0)
     snprintf(buf, len, "epilogue_warps=%d chains_per_tile=A-in-TMEM accumulators=%d%s", kTcVariants[v].epi,
              kTcVariants[v].n_acc, dec);
@@ -287,15 +271,13 @@ extern "C" int bmg_scan_tc_variant_redundant(const DevConst* K, int v)
 {
   if (v <= 0 || v >= kTcVariantCount) return 0;
   TcParams P;
-  if (!tc_plan(K, &P, tc_cap(K, v), (uint32_t)kTcVariants[v].n_acc, kTcVariants[v].ring != 0)) return 1;
+  if (!tc_plan(K, &P, tc_cap(K, v), (uint32_t)kTcVariants[v].n_acc)) return 1;
   for (int u = 0; u < v; ++u) {
     TcParams Q;
     if (kTcVariants[u].epi != kTcVariants[v].epi || kTcVariants[u].dec != kTcVariants[v].dec ||
-        !tc_plan(K, &Q, tc_cap(K, u), (uint32_t)kTcVariants[u].n_acc, kTcVariants[u].ring != 0))
+        !tc_plan(K, &Q, tc_cap(K, u), (uint32_t)kTcVariants[u].n_acc))
       continue;
-    if (Q.chains_tile == P.chains_tile && Q.n_acc == P.n_acc && Q.a_tmem == P.a_tmem &&
-        Q.pk_stages == P.pk_stages)
-      return 1;
+    if (Q.chains_tile == P.chains_tile && Q.n_acc == P.n_acc && Q.a_tmem == P.a_tmem) return 1;
   }
   return 0;
 }
@@ -340,8 +322,7 @@ extern "C" int bmg_scan_tc_launch(const DevConst* K, cudaStream_t stream, int va
 {
   if (variant < 0 || variant >= kTcVariantCount) variant = 0;
   TcParams P;
-  if (!tc_plan(K, &P, tc_cap(K, variant), (uint32_t)kTcVariants[variant].n_acc, kTcVariants[variant].ring != 0))
-    return 1;
+  if (!tc_plan(K, &P, tc_cap(K, variant), (uint32_t)kTcVariants[variant].n_acc)) return 1;
   auto enc = encode_fn();
   if (!enc) return 2;
   CUtensorMap mb, mg;

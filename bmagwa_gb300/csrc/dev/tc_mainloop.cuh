@@ -44,7 +44,6 @@ namespace {
 constexpr int TC_MAX_STAGES = 8;     // shared-memory ring (B and packed codes)
 constexpr int TC_MAX_A_STAGES = 10;  // TMEM ring of A when A is in tensor memory
 constexpr int TC_MAX_RING = 10;      // done_bar ring: max(stages, a_stages)
-constexpr int TC_MAX_PK = 12;        // ring of the packed codes when it is separate from B's
 constexpr int TC_BM = 128;           // rows of D per tile
 constexpr int TC_BK = 128;           // individuals per stage
 constexpr int TC_BK_SUB = 64;        // individuals per 128-byte swizzle atom (one TMA box of B)
@@ -80,12 +79,6 @@ struct TcParams {
   // 0-3 and 6-9, each row's two halves of 64 individuals; the epilogue then
   // starts at warp 10)
   uint32_t dec_warps = 4;
-  // the packed codes in a ring of their own (A in TMEM only): pk_stages
-  // slots of pk_bytes at pk_off, loaded pk_stages - stages stages ahead of
-  // B, so that the HBM latency of the codes is hidden deeper than the L2
-  // latency of B.  0: the codes share the stage slot with B.
-  uint32_t pk_stages = 0;
-  uint32_t pk_off = 0;
 };
 
 // stages of a tile's K segment s and the number of segments
@@ -147,7 +140,6 @@ struct TcRing {
 // barriers and flags of one CTA
 struct TcCtl {
   uint64_t full_bar[TC_MAX_STAGES], aready_bar[TC_MAX_RING], done_bar[TC_MAX_RING];
-  uint64_t pfull_bar[TC_MAX_PK], pempty_bar[TC_MAX_PK];  // the codes' ring (pk_stages > 0)
   uint64_t acc_full[2], acc_empty[2], drain_bar;
   uint32_t tmem_base;
   volatile int abort_flag;
@@ -161,10 +153,6 @@ __device__ __forceinline__ uint32_t tc_setup(const TcParams& P, TcCtl& ctl, int 
     for (uint32_t st = 0; st < P.stages; ++st) mbar_init(&ctl.full_bar[st], 1);
     for (uint32_t t = 0; t < P.a_stages; ++t) mbar_init(&ctl.aready_bar[t], P.dec_warps);
     for (uint32_t r = 0; r < P.ring; ++r) mbar_init(&ctl.done_bar[r], 1);
-    for (uint32_t q = 0; q < P.pk_stages; ++q) {
-      mbar_init(&ctl.pfull_bar[q], 1);
-      mbar_init(&ctl.pempty_bar[q], P.dec_warps);
-    }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&ctl.acc_full[b], 1);
       mbar_init(&ctl.acc_empty[b], epi_warps);
@@ -197,78 +185,33 @@ __device__ __forceinline__ void tc_main_roles(const TcParams& P, TcCtl& ctl, uin
   if (warp == 4) {
     if (lane == 0) {
       // TMA producer: packed genotype rows and the B rows of each stage
+      uint32_t issued = 0;
+      TcRing slot, done;  // this stage's shared-memory slot; the done phase of stage g - S
       const uint32_t b_half = P.b_bytes / 2;
-      if (P.pk_stages) {
-        // two streams: the codes of stage t and the B rows of stage t - D
-        const uint32_t SP = P.pk_stages, D = SP - S, total = my_tiles * nk;
-        uint32_t p_issued = 0, b_issued = 0;
-        uint32_t pi = 0, pk = 0, bi = 0, bk = 0;  // (tile, chunk) of the next codes and B loads
-        TcRing pslot, bslot, done;
+      for (uint32_t i = 0; i < my_tiles && !ctl.abort_flag; ++i) {
+        const uint32_t tile = blockIdx.x + i * gridDim.x;
+        const uint32_t snp0 = (tile % P.m_tiles) * P.snps_per_tile;
+        const uint32_t brow0 = (tile / P.m_tiles) * P.b_rows_per_tile;
         bool ok = true;
-        for (uint32_t t = 0; t < total + D && ok && !ctl.abort_flag; ++t) {
-          if (t < total) {
-            // the slot's last reader is the decode of stage t - SP
-            if (t >= SP && !mbar_wait(&ctl.pempty_bar[pslot.i], pslot.ph ^ 1u, P.wait_limit)) { ok = false; break; }
-            const uint32_t tile = blockIdx.x + pi * gridDim.x;
-            const uint32_t snp0 = (tile % P.m_tiles) * P.snps_per_tile;
-            uint64_t* fb = &ctl.pfull_bar[pslot.i];
-            mbar_arrive_tx(fb, P.pk_bytes);
-            tma_load_2d(smem + P.pk_off + pslot.i * P.pk_bytes, &map_g, fb, (int)(pk * (TC_BK / 4)), (int)snp0);
-            pslot.next(SP);
-            ++p_issued;
-            if (++pk == nk) { pk = 0; ++pi; }
+        for (uint32_t k = 0; k < nk; ++k) {
+          if (issued >= S) {  // the slot's last reader is the MMA of stage g - S
+            if (!mbar_wait(&done_bar[done.i], done.ph, P.wait_limit)) { ok = false; break; }
+            done.next(R);
           }
-          if (t >= D) {
-            // the slot's last reader is the MMA of stage g - S
-            if (b_issued >= S) {
-              if (!mbar_wait(&done_bar[done.i], done.ph, P.wait_limit)) { ok = false; break; }
-              done.next(R);
-            }
-            const uint32_t tile = blockIdx.x + bi * gridDim.x;
-            const uint32_t brow0 = (tile / P.m_tiles) * P.b_rows_per_tile;
-            uint8_t* sp = smem + bslot.i * P.stage_bytes;
-            uint64_t* fb = &full_bar[bslot.i];
-            mbar_arrive_tx(fb, P.b_bytes);
-            tma_load_2d(sp, &map_b, fb, (int)(bk * TC_BK), (int)brow0);
-            tma_load_2d(sp + b_half, &map_b, fb, (int)(bk * TC_BK + TC_BK_SUB), (int)brow0);
-            bslot.next(S);
-            ++b_issued;
-            if (++bk == nk) { bk = 0; ++bi; }
-          }
+          uint8_t* sp = smem + slot.i * P.stage_bytes;
+          uint64_t* fb = &full_bar[slot.i];
+          mbar_arrive_tx(fb, P.b_bytes + P.pk_bytes);
+          tma_load_2d(sp, &map_b, fb, (int)(k * TC_BK), (int)brow0);
+          tma_load_2d(sp + b_half, &map_b, fb, (int)(k * TC_BK + TC_BK_SUB), (int)brow0);
+          tma_load_2d(sp + P.b_bytes + P.a_bytes, &map_g, fb, (int)(k * (TC_BK / 4)), (int)snp0);
+          slot.next(S);
+          ++issued;
         }
-        if (!ok) ctl.abort_flag = 1;
-        // no load may still be landing in shared memory when the CTA exits
-        for (uint32_t g = b_issued > S ? b_issued - S : 0; g < b_issued; ++g) mbar_wait(&full_bar[g % S], (g / S) & 1);
-        for (uint32_t g = p_issued > SP ? p_issued - SP : 0; g < p_issued; ++g)
-          mbar_wait(&ctl.pfull_bar[g % SP], (g / SP) & 1);
-      } else {
-        uint32_t issued = 0;
-        TcRing slot, done;  // this stage's shared-memory slot; the done phase of stage g - S
-        for (uint32_t i = 0; i < my_tiles && !ctl.abort_flag; ++i) {
-          const uint32_t tile = blockIdx.x + i * gridDim.x;
-          const uint32_t snp0 = (tile % P.m_tiles) * P.snps_per_tile;
-          const uint32_t brow0 = (tile / P.m_tiles) * P.b_rows_per_tile;
-          bool ok = true;
-          for (uint32_t k = 0; k < nk; ++k) {
-            if (issued >= S) {  // the slot's last reader is the MMA of stage g - S
-              if (!mbar_wait(&done_bar[done.i], done.ph, P.wait_limit)) { ok = false; break; }
-              done.next(R);
-            }
-            uint8_t* sp = smem + slot.i * P.stage_bytes;
-            uint64_t* fb = &full_bar[slot.i];
-            mbar_arrive_tx(fb, P.b_bytes + P.pk_bytes);
-            tma_load_2d(sp, &map_b, fb, (int)(k * TC_BK), (int)brow0);
-            tma_load_2d(sp + b_half, &map_b, fb, (int)(k * TC_BK + TC_BK_SUB), (int)brow0);
-            tma_load_2d(sp + P.b_bytes + P.a_bytes, &map_g, fb, (int)(k * (TC_BK / 4)), (int)snp0);
-            slot.next(S);
-            ++issued;
-          }
-          if (!ok) { ctl.abort_flag = 1; break; }
-        }
-        // no load may still be landing in shared memory when the CTA exits:
-        // wait (bounded) for the last load of every slot
-        for (uint32_t g = issued > S ? issued - S : 0; g < issued; ++g) mbar_wait(&full_bar[g % S], (g / S) & 1);
+        if (!ok) { ctl.abort_flag = 1; break; }
       }
+      // no load may still be landing in shared memory when the CTA exits:
+      // wait (bounded) for the last load of every slot
+      for (uint32_t g = issued > S ? issued - S : 0; g < issued; ++g) mbar_wait(&full_bar[g % S], (g / S) & 1);
     }
   } else if (warp == 5) {
     if (lane == 0) {
@@ -332,7 +275,7 @@ __device__ __forceinline__ void tc_main_roles(const TcParams& P, TcCtl& ctl, uin
     const DecTab tab = dec_tab(value);
     const uint32_t total = my_tiles * nk;
     const uint32_t a_lane = tmem + ((uint32_t)((warp & 3) * 32) << 16) + P.n_acc * P.acc_cols;
-    TcRing full, aslot, done, pkr;  // this stage's slots; the done phase of stage g - SA; the codes' slot
+    TcRing full, aslot, done;  // this stage's slots; the done phase of stage g - SA
     for (uint32_t g = 0; g < total; ++g) {
       // A in shared memory: the TMA of this stage waited for the MMA of stage
       // g - S, the last reader of the slot.  A in TMEM: slot aslot is free
@@ -343,9 +286,7 @@ __device__ __forceinline__ void tc_main_roles(const TcParams& P, TcCtl& ctl, uin
       const bool need_slot = P.a_tmem && g >= SA;
       bool ok = false;
       if (lane == 0)
-        ok = !ctl.abort_flag &&
-             (P.pk_stages ? mbar_wait(&ctl.pfull_bar[pkr.i], pkr.ph, P.wait_limit)
-                          : mbar_wait(&full_bar[full.i], full.ph, P.wait_limit)) &&
+        ok = !ctl.abort_flag && mbar_wait(&full_bar[full.i], full.ph, P.wait_limit) &&
              (!need_slot || mbar_wait(&done_bar[done.i], done.ph, P.wait_limit));
       ok = __shfl_sync(0xffffffffu, ok, 0);
       __syncwarp();
@@ -355,15 +296,8 @@ __device__ __forceinline__ void tc_main_roles(const TcParams& P, TcCtl& ctl, uin
       }
       if (need_slot) done.next(R);
       uint8_t* sp = smem + full.i * P.stage_bytes;
-      const uint8_t* codes = P.pk_stages ? smem + P.pk_off + pkr.i * P.pk_bytes : sp + P.b_bytes + P.a_bytes;
-      const uint4* pk = reinterpret_cast<const uint4*>(codes + sl * (TC_BK / 4));
+      const uint4* pk = reinterpret_cast<const uint4*>(sp + P.b_bytes + P.a_bytes + sl * (TC_BK / 4));
       const uint4 c0 = pk[0], c1 = pk[1];
-      if (P.pk_stages) {
-        // the codes are in registers: the slot may be refilled
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&ctl.pempty_bar[pkr.i]);
-        pkr.next(P.pk_stages);
-      }
       const uint32_t w[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
       if (P.a_tmem) {
         // 128 individuals = 64 columns, column q = individuals 2q, 2q + 1
