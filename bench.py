@@ -449,6 +449,8 @@ def main():
     ap.add_argument("--p", type=int, default=None, help="override the SNP count (profiling)")
     ap.add_argument("--n", type=int, default=None, help="override the individuals (profiling)")
     ap.add_argument("--chains", type=int, default=None, help="override the chains (profiling)")
+    ap.add_argument("--max-move-size", type=int, default=None,
+                    help="override the largest multi-SNP move (profiling)")
     ap.add_argument("--no-e2e", dest="e2e", action="store_false")
     ap.add_argument("--no-ess", dest="ess", action="store_false",
                     help="skip the inclusion-ESS leg (burn-in + sampled iterations after the timed region)")
@@ -456,7 +458,7 @@ def main():
     if args.warmup < 3:
         args.warmup = 3
     wl = dict(WORKLOADS[args.workload])
-    for key in ("p", "n", "chains"):
+    for key in ("p", "n", "chains", "max_move_size"):
         if getattr(args, key):
             wl[key] = getattr(args, key)
     if "keep" in wl:

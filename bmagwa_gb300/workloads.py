@@ -58,7 +58,7 @@ def options(wl, seed0, iters, chains=None):
     o.thin = 1 if wl["n_rao"] < 10 else 10
     o.n_rao_burnin = max(1, iters // (2 * wl["n_rao"]))
     o.n_sample_tau2_and_missing = 10
-    o.max_move_size = 20
+    o.max_move_size = wl.get("max_move_size", 20)
     o.max_SNP_neighborhood_size = 20
     o.p_move_size, o.p_move_size_nbs, o.p_move_size_nbc = 0.2, 0.7, 0.25
     o.e_qg, o.var_qg, o.nu_sigma2, o.R2mode_sigma2, o.mu_alpha = 20, 300, 1, 0.2, 1
