@@ -312,7 +312,8 @@ def run_gb300(args, wl):
         "dtype": "f64 (moves) / bf16-limb exact int (scan)" if args.scan == 0 else "f64 / int64",
         "data": "synthetic (seeded LD-block genotypes and phenotypes)",
         "config": {"workload": args.workload, "n": n, "p": p, "chains": C, "n_rao": wl["n_rao"],
-                   "types": wl["types"], "parallelism": "replicas" if world > 1 else "single",
+                   "types": wl["types"], "max_move_size": wl.get("max_move_size", 20),
+                   "parallelism": "replicas" if world > 1 else "single",
                    "l2": "inputs larger than L2 (%.2f GB packed genotypes)" % (packed.nbytes / 1e9),
                    "scan_impl": "tcgen05" if args.scan == 0 else "simt",
                    "scan_shape": scan_shape, "scan_tuning_ms": scan_tuning},
