@@ -218,7 +218,9 @@ __device__ __forceinline__ void tc_main_roles(const TcParams& P, TcCtl& ctl, uin
       // MMA issuer: tile i accumulates into buffer i % n_acc
       const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((P.n_mma >> 3) << 17) | ((uint32_t)(TC_BM >> 4) << 24);
       const uint32_t a_base = tmem + P.n_acc * P.acc_cols;
-      const uint32_t b_half = P.b_bytes / 2;
+      const uint64_t d_base = smem_desc(smem);
+      const uint32_t st16 = P.stage_bytes >> 4, bh16 = (P.b_bytes / 2) >> 4, a16 = (P.b_bytes + 0u) >> 4;
+      const uint32_t asub16 = TC_A_SUB_BYTES >> 4;
       TcRing full, aslot;  // this stage's shared-memory slot and A slot
       uint32_t dn = 0;     // done_bar slot of this stage
       const uint32_t seg_len = tc_seg_len(P), n_seg = tc_n_seg(P);
@@ -237,19 +239,23 @@ __device__ __forceinline__ void tc_main_roles(const TcParams& P, TcCtl& ctl, uin
             break;
           }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-          uint8_t* sp = smem + full.i * P.stage_bytes;
+          // descriptors by addition: the start-address field (address / 16,
+          // 14 bits) of the ring base plus the slot's offset / 16 (shared
+          // memory addresses are below 2^18, so the field does not carry)
+          const uint64_t bd = d_base + full.i * st16;
+          const uint32_t acc0 = (k - k0) != 0;
           if (P.a_tmem) {
             const uint32_t at = a_base + aslot.i * TC_A_COLS;
+            mma_bf16_tmem_a(d, at, bd, idesc, acc0);
 #pragma unroll
-            for (int kk = 0; kk < TC_BK / 16; ++kk)  // 16 bf16: 8 TMEM columns of A, 2 descriptor units of B
-              mma_bf16_tmem_a(d, at + 8 * kk, smem_desc(sp + (kk >> 2) * b_half) + 2 * (kk & 3), idesc,
-                              ((k - k0) | kk) != 0);
+            for (int kk = 1; kk < TC_BK / 16; ++kk)  // 16 bf16: 8 TMEM columns of A, 2 descriptor units of B
+              mma_bf16_tmem_a(d, at + 8 * kk, bd + (kk >> 2) * bh16 + 2 * (kk & 3), idesc, 1u);
           } else {
-            uint8_t* a = sp + P.b_bytes;
+            const uint64_t ad = bd + a16;
+            mma_bf16(d, ad, bd, idesc, acc0);
 #pragma unroll
-            for (int kk = 0; kk < TC_BK / 16; ++kk)  // 16 bf16 = 32 bytes = 2 descriptor units
-              mma_bf16(d, smem_desc(a + (kk >> 2) * TC_A_SUB_BYTES) + 2 * (kk & 3),
-                       smem_desc(sp + (kk >> 2) * b_half) + 2 * (kk & 3), idesc, ((k - k0) | kk) != 0);
+            for (int kk = 1; kk < TC_BK / 16; ++kk)  // 16 bf16 = 32 bytes = 2 descriptor units
+              mma_bf16(d, ad + (kk >> 2) * asub16 + 2 * (kk & 3), bd + (kk >> 2) * bh16 + 2 * (kk & 3), idesc, 1u);
           }
           mma_commit(&done_bar[dn]);
           if (++dn == R) dn = 0;
