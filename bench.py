@@ -267,7 +267,7 @@ def run_gb300(args, wl):
         marks.append(("precompute", time.perf_counter()))
         col = ctx2.run(args.steps, collect=True)
         marks.append(("run", time.perf_counter()))
-        rao = [ctx2.rao(c)[0] for c in range(wl["chains"])]
+        rao = [ctx2.rao_all()[0]]
         torch.cuda.synchronize()
         e2e_s = time.perf_counter() - t0
         marks.append(("read_back", t0 + e2e_s))

@@ -62,6 +62,7 @@ def lib():
         L.bmg_run.argtypes = [vp, u64, C.POINTER(abi.TraceSink)]
         L.bmg_get_state.argtypes = [vp, u32, C.POINTER(abi.ChainState), vp, vp, u32]
         L.bmg_get_rao.argtypes = [vp, u32, vp, vp]
+        L.bmg_get_rao_all.argtypes = [vp, vp, vp]
         L.bmg_finish.argtypes = [vp]
         L.bmg_get_timings.argtypes = [vp, vp]
         L.bmg_get_proposal.argtypes = [vp, u32, vp, vp]
@@ -89,7 +90,7 @@ def lib():
         L.bmg_destroy.restype = None
         for name in ("bmg_create", "bmg_load_bed", "bmg_set_phenotypes", "bmg_set_covariates",
                      "bmg_precompute", "bmg_get_precomputed", "bmg_scan", "bmg_run", "bmg_get_state",
-                     "bmg_get_rao", "bmg_finish", "bmg_get_timings", "bmg_get_data_stats",
+                     "bmg_get_rao", "bmg_get_rao_all", "bmg_finish", "bmg_get_timings", "bmg_get_data_stats",
                      "bmg_get_proposal", "bmg_get_last_scan", "bmg_reset_timings"):
             getattr(L, name).restype = C.c_int
         _lib = L
@@ -277,6 +278,15 @@ class Context:
         pt = np.zeros(self.m_g * self.n_types) if self.n_types > 1 else None
         self._check(lib().bmg_get_rao(self.h, chain, _ptr(p), _ptr(pt)))
         return p, (pt.reshape(self.m_g, self.n_types) if pt is not None else None)
+
+    def rao_all(self):
+        """Rao-Blackwellised posteriors of every chain in one call:
+        (chains x m_g, chains x m_g x n_types or None)."""
+        p = np.zeros(self.opt.n_chains * self.m_g)
+        pt = np.zeros(self.opt.n_chains * self.m_g * self.n_types) if self.n_types > 1 else None
+        self._check(lib().bmg_get_rao_all(self.h, _ptr(p), _ptr(pt)))
+        return (p.reshape(self.opt.n_chains, self.m_g),
+                pt.reshape(self.opt.n_chains, self.m_g, self.n_types) if pt is not None else None)
 
     def proposal(self, chain=0):
         p = np.zeros(self.m_g)

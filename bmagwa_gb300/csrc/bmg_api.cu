@@ -1809,6 +1809,57 @@ extern "C" bmg_status bmg_get_rao(bmg_ctx* ctx, uint32_t chain, double* p_rao, d
   API_END
 }
 
+// Device -> caller's memory through the two pinned staging buffers: the DMA
+// of chunk i overlaps the host copy (several threads) of chunk i - 1.
+static void copy_out_staged(bmg_ctx* ctx, const uint8_t* src, uint8_t* dst, size_t bytes)
+{
+  const size_t chunk = std::min<size_t>(bytes, size_t(32) << 20);
+  ctx->ensure_stage(chunk);
+  const unsigned nth = std::max(1u, std::min(8u, std::thread::hardware_concurrency()));
+  auto host_copy = [&](const uint8_t* s, uint8_t* d, size_t n) {
+    std::vector<std::thread> th;
+    const size_t part = (n + nth - 1) / nth;
+    for (unsigned t = 0; t < nth && t * part < n; ++t)
+      th.emplace_back([=] { std::memcpy(d + t * part, s + t * part, std::min(part, n - t * part)); });
+    for (auto& x : th) x.join();
+  };
+  size_t prev_off = 0, prev_n = 0;
+  int b = 0, prev_b = -1;
+  for (size_t off = 0; off < bytes; off += chunk, b ^= 1) {
+    const size_t n = std::min(chunk, bytes - off);
+    CK(cudaEventSynchronize(ctx->stage_ev[b]));
+    CK(cudaMemcpyAsync(ctx->stage[b], src + off, n, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaEventRecord(ctx->stage_ev[b], ctx->stream));
+    if (prev_b >= 0) {
+      CK(cudaEventSynchronize(ctx->stage_ev[prev_b]));
+      host_copy(ctx->stage[prev_b], dst + prev_off, prev_n);
+    }
+    prev_b = b;
+    prev_off = off;
+    prev_n = n;
+  }
+  if (prev_b >= 0) {
+    CK(cudaEventSynchronize(ctx->stage_ev[prev_b]));
+    host_copy(ctx->stage[prev_b], dst + prev_off, prev_n);
+  }
+}
+
+extern "C" bmg_status bmg_get_rao_all(bmg_ctx* ctx, double* p_rao, double* p_rao_types)
+{
+  if (!ctx) return BMG_EINVAL;
+  API_BEGIN
+  check_ready(ctx);
+  const size_t p = ctx->p, C = ctx->C, nt = ctx->opt.n_types > 1 ? ctx->opt.n_types : 0;
+  if (p_rao)
+    copy_out_staged(ctx, reinterpret_cast<const uint8_t*>(ctx->K.p_rao), reinterpret_cast<uint8_t*>(p_rao),
+                    8 * p * C);
+  if (p_rao_types && nt)
+    copy_out_staged(ctx, reinterpret_cast<const uint8_t*>(ctx->K.p_rao_types),
+                    reinterpret_cast<uint8_t*>(p_rao_types), 8 * p * nt * C);
+  return BMG_OK;
+  API_END
+}
+
 extern "C" bmg_status bmg_get_proposal(bmg_ctx* ctx, uint32_t chain, double* p_prop, double* p_prop_types)
 {
   if (!ctx) return BMG_EINVAL;

@@ -282,6 +282,12 @@ bmg_status bmg_get_state(bmg_ctx* ctx, uint32_t chain, bmg_chain_state* st,
  * payloads, src/sampler.cpp:846-858).  p_rao_types may be NULL. */
 bmg_status bmg_get_rao(bmg_ctx* ctx, uint32_t chain, double* p_rao, double* p_rao_types);
 
+/* The same for every chain in one call: p_rao receives chains x m_g values
+ * (chain-major), p_rao_types chains x m_g x n_types or is NULL.  The copy is
+ * pipelined through the pinned staging buffers (no counterpart in the
+ * reference, which writes one _rao.dat per chain). */
+bmg_status bmg_get_rao_all(bmg_ctx* ctx, double* p_rao, double* p_rao_types);
+
 /* Adaptive proposal of a chain: the running mean p_proposal of the
  * Rao-Blackwellised probabilities that sets the add/remove weights
  * (Sampler::save_p_proposal, src/sampler.hpp:363-383).  p_prop_types may be NULL. */

@@ -400,6 +400,19 @@ def test_gpu_posterior_matches_exact_enumeration(bmg, oracle, dr):
 
 
 
+def test_rao_of_all_chains_in_one_call(bmg, tmp_path):
+    """bmg_get_rao_all (one pipelined copy through the staging buffers) gives
+    every chain's bmg_get_rao, with two effect types (the per-type array)."""
+    opt, packed, y, e = synth_case(bmg, tmp_path, "batched", n=900, p=4000, chains=3, iters=40, n_rao=2)
+    ctx, _ = run_gpu(bmg, opt, packed, y, e, 40)
+    allp, allt = ctx.rao_all()
+    for c in range(opt.n_chains):
+        p, pt = ctx.rao(c)
+        np.testing.assert_array_equal(allp[c], p)
+        np.testing.assert_array_equal(allt[c], pt)
+    ctx.close()
+
+
 def test_many_covariates_match_the_oracle(bmg, oracle, tmp_path):
     """Twelve covariates besides the constant (the reference reads any m_e,
     src/data.cpp:202-243): the chains equal the oracle's."""
